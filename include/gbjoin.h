@@ -1,0 +1,271 @@
+/*
+ * gbjoin.h -- C ABI of the GB300 relational hot path: radix partitioning,
+ * hash-join build/probe and hash group-by aggregation.
+ *
+ * Plain C types only (pointers, sizes, int32/int64).  Column pointers named
+ * d_* are device pointers that the caller owns; h_* are host pointers.  Every
+ * call that takes a `stream` (a cudaStream_t passed as void*, NULL = the
+ * context's own stream) is stream-ordered and returns without a device sync
+ * unless its comment says otherwise.  Every entry point returns a gbj_status;
+ * the text of the last error of a context is available from gbj_last_error().
+ * No entry point aborts the process.
+ *
+ * Each declaration cites the interface of chapeiro/proteus it stands in for
+ * (paths are relative to the proteus source tree).
+ */
+#ifndef GBJOIN_H
+#define GBJOIN_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ------------------------------------------------------------------ status */
+/* Replaces gpu_run()/gpuAssert aborts (core/platform/include/platform/common/
+ * gpu/gpu-common.hpp:93-110) and capacity asserts
+ * (core/olap/lib/operators/gpu/gpu-hash-join-chained.cpp:60-69). */
+typedef enum gbj_status {
+  GBJ_OK = 0,
+  GBJ_ERR_INVALID = 1,     /* bad argument (null pointer, size, enum)        */
+  GBJ_ERR_OOM = 2,         /* device pool cannot hold the request            */
+  GBJ_ERR_CAPACITY = 3,    /* a table or output buffer was too small         */
+  GBJ_ERR_TIMEOUT = 4,     /* a bounded device-side wait gave up             */
+  GBJ_ERR_CUDA = 5,        /* a CUDA runtime call failed                     */
+  GBJ_ERR_UNSUPPORTED = 6, /* valid request this build does not implement    */
+  GBJ_ERR_BUDGET = 7,      /* admission refused: HBM budget exhausted        */
+  GBJ_ERR_CANCELLED = 8    /* request cancelled before it ran                */
+} gbj_status;
+
+typedef struct gbj_ctx gbj_ctx;     /* one device, one resident pool     */
+typedef struct gbj_table gbj_table; /* a built join hash table           */
+
+/* --------------------------------------------------------------- context */
+/* Stands in for proteus::platform / MemoryManager::init + buffer_manager::init
+ * (core/platform/include/platform/common/common.hpp:177-183,
+ *  core/platform/include/platform/memory/memory-manager.hpp:152-154).
+ * Reserves `pool_bytes` of device memory once (0 = 40% of free memory); all
+ * scratch space of later calls comes from that resident pool. */
+int gbj_ctx_create(int device, uint64_t pool_bytes, gbj_ctx **out);
+int gbj_ctx_destroy(gbj_ctx *ctx);
+const char *gbj_last_error(gbj_ctx *ctx);
+/* Number of SMs and L2 bytes of the context's device (host query). */
+int gbj_ctx_device_info(gbj_ctx *ctx, int *sm_count, uint64_t *l2_bytes,
+                        uint64_t *smem_per_block_optin);
+/* Synchronises `stream` and reports (and clears) any error a kernel latched
+ * on the device (capacity overflow, bounded-wait timeout). */
+int gbj_sync(gbj_ctx *ctx, void *stream);
+/* Number of gbj kernels launched through this context so far. */
+uint64_t gbj_kernel_launches(gbj_ctx *ctx);
+
+/* Kernel timing, standing in for the reference's per-kernel cudaEvent
+ * timers and time_block registry (core/olap/lib/operators/gpu/
+ * gpu-partitioned-hash-join-chained.cpp:303-387, core/platform/include/
+ * platform/util/timing.hpp:65-140).  While enabled, an event is recorded on
+ * the launching stream after every kernel; a kernel's time is the interval
+ * since the previous event on that stream.  Enabling or disabling clears the
+ * totals.  gbj_profile_kernel / gbj_profile_dump synchronise the events. */
+int gbj_profile_enable(gbj_ctx *ctx, int on);
+int gbj_profile_kernel(gbj_ctx *ctx, const char *kernel, uint64_t *launches,
+                       double *total_ms);
+/* "name launches total_ms" lines, NUL-terminated. */
+int gbj_profile_dump(gbj_ctx *ctx, char *buf, uint64_t buflen);
+
+/* ---------------------------------------------------- resident device pool */
+/* Replaces MemoryManager::mallocGpu/freeGpu and the buffer-manager block
+ * pools (core/platform/lib/memory/memory-manager.cpp,
+ * core/platform/lib/memory/buffer-manager.cu).  Allocation is host-side
+ * bookkeeping over the block reserved at gbj_ctx_create; nothing calls
+ * cudaMalloc after that. */
+int gbj_pool_alloc(gbj_ctx *ctx, uint64_t bytes, void **d_ptr);
+int gbj_pool_free(gbj_ctx *ctx, void *d_ptr);
+int gbj_pool_stats(gbj_ctx *ctx, uint64_t *capacity, uint64_t *in_use,
+                   uint64_t *peak);
+
+/* ---------------------------------------------------- fused aggregations */
+/* Aggregates computed on join matches, standing in for the parent Reduce
+ * (core/olap/lib/operators/reduce-opt.cpp:52-481, gpu/gpu-reduce.cpp:155-198)
+ * with gpu::Monoid update semantics (core/olap/lib/operators/gpu/
+ * gmonoids.cpp:122-360).  SUM accumulates in int64, as the reference does
+ * after a CastExpression (core/olap/include/olap/expressions/
+ * expressions.hpp:1162).  On an empty input COUNT/SUM give 0, MIN gives
+ * INT64_MAX and MAX gives INT64_MIN. */
+typedef enum gbj_agg_op {
+  GBJ_AGG_COUNT = 0,
+  GBJ_AGG_SUM = 1,
+  GBJ_AGG_MIN = 2,
+  GBJ_AGG_MAX = 3
+} gbj_agg_op;
+
+/* Value a join aggregate reads for one matching (build row, probe row). */
+typedef enum gbj_operand {
+  GBJ_VAL_ONE = 0,         /* constant 1                                */
+  GBJ_VAL_BUILD = 1,       /* build payload column                      */
+  GBJ_VAL_PROBE = 2,       /* probe payload column                      */
+  GBJ_VAL_PRODUCT = 3,     /* (int64)build payload * probe payload      */
+  GBJ_VAL_BUILD_ROWID = 4, /* 0-based build row position                */
+  GBJ_VAL_PROBE_ROWID = 5, /* 0-based probe row position                */
+  GBJ_VAL_ROWID_XOR = 6,   /* build rowid XOR probe rowid               */
+  GBJ_VAL_BUILD_KEY = 7    /* the join key                              */
+} gbj_operand;
+
+typedef struct gbj_agg {
+  int32_t op;      /* gbj_agg_op  */
+  int32_t operand; /* gbj_operand */
+} gbj_agg;
+
+#define GBJ_MAX_AGGS 8
+
+/* ----------------------------------------------- chained hash join (plain) */
+/* HashJoinChained / GpuHashJoinChained build side
+ * (core/olap/lib/operators/hash-join-chained.cpp:262-319, open_build
+ * core/olap/lib/operators/gpu/gpu-hash-join-chained.cpp:31-58).
+ * Every build row is inserted (duplicate keys allowed).  `hash_bits` and
+ * `max_build` are the plan's sizing fields; 0 lets the library size the
+ * table from n.  A non-zero max_build smaller than n gives GBJ_ERR_CAPACITY
+ * (the reference asserts).  d_payload may be NULL.  The table references
+ * d_keys/d_payload: keep them alive until gbj_table_destroy. */
+int gbj_join_build(gbj_ctx *ctx, const int32_t *d_keys,
+                   const int32_t *d_payload, uint64_t n, int32_t hash_bits,
+                   uint64_t max_build, void *stream, gbj_table **out);
+
+/* Probe side with the parent's aggregate fused in
+ * (core/olap/lib/operators/hash-join-chained.cpp:321-566 feeding
+ *  gpu/gpu-reduce.cpp:155-198).  Writes n_aggs int64 results to d_out. */
+int gbj_join_probe_agg(gbj_ctx *ctx, const gbj_table *table,
+                       const int32_t *d_keys, const int32_t *d_payload,
+                       uint64_t n, const gbj_agg *aggs, int32_t n_aggs,
+                       int64_t *d_out, void *stream);
+
+/* Probe side emitting every match as a (build row, probe row) pair, the
+ * bindings HashJoinChained hands to its parent's consume().  Pairs are
+ * written in no particular order.  The match count goes to *d_count; if it
+ * exceeds `capacity` the pairs beyond it are dropped and gbj_sync reports
+ * GBJ_ERR_CAPACITY.  d_probe_rows may be NULL to use 0..n-1 as probe row ids,
+ * otherwise probe key i is reported as d_probe_rows[i]. */
+int gbj_join_probe_pairs(gbj_ctx *ctx, const gbj_table *table,
+                         const int32_t *d_keys, const int32_t *d_probe_rows,
+                         uint64_t n, int32_t *d_build_rows,
+                         int32_t *d_out_probe_rows, uint64_t capacity,
+                         uint64_t *d_count, void *stream);
+
+int gbj_table_destroy(gbj_ctx *ctx, gbj_table *table);
+/* Number of slots of the table (host query). */
+uint64_t gbj_table_slots(const gbj_table *table);
+
+/* ------------------------------------------------------ radix partitioning */
+/* HashPartitioner (core/olap/lib/operators/gpu/
+ * gpu-partitioned-hash-join-chained.cpp:120-404, kernels in
+ * gpu-partitioned-hash-join-chained-helpers.cpp:243-481) and
+ * radix_cluster_nopadding / partitionHT (core/platform/lib/util/radix/joins/
+ * radix-join.cpp:85-155,253-276).
+ * digit = (f(key) >> shift) & (2^bits - 1) with f = identity
+ * (GBJ_DIGIT_KEY, radix_cluster_nopadding) or the murmur3 32-bit finaliser
+ * (GBJ_DIGIT_HASH, the GPU partitioner's hashd).  Partition p holds exactly
+ * the tuples whose digit is p, contiguous and in partition order; inside a
+ * partition the order is unspecified (as with the reference's GPU
+ * HashPartitioner), so sorted per partition the result equals the
+ * counting-sort cluster of radix_cluster_nopadding.
+ * d_payload may be NULL: then the 0-based row position is carried instead.
+ * d_offsets receives 2^bits + 1 partition start offsets.  bits in [1, 15],
+ * shift + bits <= 32, n < 2^31.  No host synchronisation. */
+typedef enum gbj_digit { GBJ_DIGIT_KEY = 0, GBJ_DIGIT_HASH = 1 } gbj_digit;
+
+int gbj_partition(gbj_ctx *ctx, const int32_t *d_keys,
+                  const int32_t *d_payload, uint64_t n, int32_t digit,
+                  int32_t shift, int32_t bits, int32_t *d_out_keys,
+                  int32_t *d_out_payload, uint64_t *d_offsets, void *stream);
+
+/* ------------------------------------------------------ radix hash join */
+/* GpuPartitionedHashJoinChained (core/olap/lib/operators/gpu/
+ * gpu-partitioned-hash-join-chained.cpp:612-1586) and RJStepwise
+ * (core/platform/lib/util/radix/joins/radix-join.cpp:278-375): partition
+ * both sides on hash bits so each build partition's table fits on-chip,
+ * then build and probe per partition with the aggregate fused in.  Each side
+ * carries ONE 32-bit value into the partitions: its payload if an aggregate
+ * reads GBJ_VAL_BUILD/PROBE/PRODUCT, its row position if one reads a rowid
+ * operand (mixing both on one side gives GBJ_ERR_UNSUPPORTED).  Work items
+ * are sized on the device, so the call never synchronises with the host. */
+typedef struct gbj_radix_params {
+  int32_t bits;       /* radix bits, 0 = autotuned                        */
+  int32_t passes;     /* 1 or 2, 0 = autotuned                            */
+  int32_t block;      /* threads per block of the join kernel, 0 = auto   */
+  int32_t log_parts;  /* plan field log_parts (reference: 13), 0 = unset  */
+} gbj_radix_params;
+
+int gbj_radix_join_agg(gbj_ctx *ctx, const int32_t *d_build_keys,
+                       const int32_t *d_build_payload, uint64_t n_build,
+                       const int32_t *d_probe_keys,
+                       const int32_t *d_probe_payload, uint64_t n_probe,
+                       const gbj_radix_params *params, const gbj_agg *aggs,
+                       int32_t n_aggs, int64_t *d_out, void *stream);
+
+/* ------------------------------------------------------ hash group-by */
+/* GpuHashGroupByChained (core/olap/lib/operators/gpu/
+ * gpu-hash-group-by-chained.cpp:77-556) with HashGroupByChained's emit scan
+ * (core/olap/lib/operators/hash-group-by-chained.cpp:638-853).  One output
+ * row per distinct key with COUNT (int64), SUM of the value (int64), MIN and
+ * MAX (int32).  Groups come out in no particular order; *d_n_groups gets the
+ * group count.  More groups than out_capacity gives GBJ_ERR_CAPACITY at
+ * gbj_sync.  Any of the five output columns may be NULL. */
+typedef struct gbj_groupby_params {
+  int32_t hash_bits;        /* plan field, 0 = unset                     */
+  int32_t strategy;         /* 0 auto, 1 on-chip + global table,
+                               2 radix-partitioned                       */
+  uint64_t max_input_size;  /* plan field maxInputSize, 0 = unset        */
+  uint64_t expected_groups; /* cardinality hint, 0 = unknown             */
+} gbj_groupby_params;
+
+int gbj_groupby(gbj_ctx *ctx, const int32_t *d_keys, const int32_t *d_values,
+                uint64_t n, const gbj_groupby_params *params,
+                int32_t *d_out_keys, int64_t *d_out_count, int64_t *d_out_sum,
+                int32_t *d_out_min, int32_t *d_out_max, uint64_t out_capacity,
+                uint64_t *d_n_groups, void *stream);
+
+/* ------------------------------------------------------ column helpers */
+/* Global aggregate over one int32 column restricted to an optional row list
+ * (Reduce, core/olap/lib/operators/reduce-opt.cpp:52-481).  d_rows may be
+ * NULL for all rows 0..n-1. */
+int gbj_reduce(gbj_ctx *ctx, const int32_t *d_col, const int32_t *d_rows,
+               uint64_t n, const gbj_agg *aggs, int32_t n_aggs,
+               int64_t *d_out, void *stream);
+
+/* Gather d_out[i] = d_col[d_rows[i]] (late materialisation of a join side). */
+int gbj_gather(gbj_ctx *ctx, const int32_t *d_col, const int32_t *d_rows,
+               uint64_t n, int32_t *d_out, void *stream);
+
+/* Select (core/olap/lib/operators/select.cpp:26-37) for the predicate forms
+ * the workloads use: lo <= col <= hi (inclusive).  Writes the positions of
+ * passing rows (ascending) to d_rows_out and their number to *d_count. */
+int gbj_select_range(gbj_ctx *ctx, const int32_t *d_col, uint64_t n,
+                     int32_t lo, int32_t hi, int32_t *d_rows_out,
+                     uint64_t *d_count, void *stream);
+
+/* ------------------------------------------ seeded synthetic input (host) */
+/* Deterministic, thread-parallel generators for the workload shapes; pure
+ * functions of (seed, row), identical on every host.  threads <= 0 uses all
+ * hardware threads. */
+int gbj_gen_build_side(uint64_t seed, uint64_t n, int32_t *h_keys,
+                       int32_t *h_payload, int threads);
+int gbj_gen_probe_uniform(uint64_t seed, uint64_t n, uint64_t n_build,
+                          int32_t *h_keys, int32_t *h_payload, int threads);
+int gbj_gen_probe_zipf(uint64_t seed, uint64_t n, uint64_t n_build,
+                       double theta, double hit_rate, int32_t *h_keys,
+                       int32_t *h_payload, int threads);
+int gbj_gen_groupby(uint64_t seed, uint64_t n, uint64_t cardinality,
+                    double theta, int32_t *h_keys, int32_t *h_values,
+                    int threads);
+uint64_t gbj_gen_rand(uint64_t seed, uint64_t stream, uint64_t i);
+uint64_t gbj_gen_perm(uint64_t seed, uint64_t stream, uint64_t n, uint64_t i);
+uint64_t gbj_gen_zipf(uint64_t seed, uint64_t stream, uint64_t n, double theta,
+                      uint64_t i);
+double gbj_gen_det_log(double x);
+double gbj_gen_det_exp(double x);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GBJOIN_H */

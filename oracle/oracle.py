@@ -1,0 +1,217 @@
+"""ctypes wrapper of the oracle (liboracle.so) and of oracle/_ref.
+
+TEST INFRASTRUCTURE ONLY: the checker for the CUDA path and the benchmark's
+CPU-baseline leg.  The product never imports this module.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB = os.path.join(HERE, "liboracle.so")
+REF_LIB = os.path.join(HERE, "_ref", "libproteus_radix_ref.so")
+
+vp, u64, i32, i64 = C.c_void_p, C.c_uint64, C.c_int32, C.c_int64
+
+
+class ChainedTable(C.Structure):
+    _fields_ = [("head", vp), ("next", vp), ("key", vp), ("payload", vp), ("n", u64),
+                ("hash_bits", i32)]
+
+
+_lib = None
+_ref = None
+
+
+def build():
+    subprocess.run(["make", "-s", "-C", HERE, "all"], check=True)
+
+
+def build_ref(ref_root="/root/reference"):
+    """Compiles oracle/_ref from the reference sources, when they are present."""
+    if not os.path.isdir(os.path.join(ref_root, "core", "platform")):
+        return False
+    subprocess.run(["make", "-s", "-C", HERE, "ref", f"REF={ref_root}"], check=True)
+    return True
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB):
+            build()
+        L = C.CDLL(LIB)
+        L.orc_hash_int32.restype, L.orc_hash_int32.argtypes = u64, [i32]
+        L.orc_hashd.restype, L.orc_hashd.argtypes = C.c_uint32, [i32]
+        L.orc_join_build.restype = C.c_int
+        L.orc_join_build.argtypes = [vp, vp, u64, i32, C.POINTER(ChainedTable)]
+        L.orc_join_build_mt.restype = C.c_int
+        L.orc_join_build_mt.argtypes = [vp, vp, u64, i32, C.c_int, C.POINTER(ChainedTable)]
+        L.orc_join_free.restype, L.orc_join_free.argtypes = None, [C.POINTER(ChainedTable)]
+        L.orc_join_probe_agg.restype = C.c_int
+        L.orc_join_probe_agg.argtypes = [C.POINTER(ChainedTable), vp, vp, u64, vp, vp, i32, vp,
+                                         C.c_int]
+        L.orc_join_probe_pairs.restype = i64
+        L.orc_join_probe_pairs.argtypes = [C.POINTER(ChainedTable), vp, u64, vp, vp, u64]
+        L.orc_radix_cluster.restype = None
+        L.orc_radix_cluster.argtypes = [vp, vp, u64, i32, i32, i32, vp, vp, vp]
+        L.orc_rj_stepwise.restype, L.orc_rj_stepwise.argtypes = i64, [vp, u64, vp, u64]
+        L.orc_partition_ht_counts.restype = None
+        L.orc_partition_ht_counts.argtypes = [vp, u64, vp]
+        L.orc_radix_join_agg.restype = C.c_int
+        L.orc_radix_join_agg.argtypes = [vp, vp, u64, vp, vp, u64, i32, vp, vp, i32, vp, C.c_int]
+        L.orc_groupby.restype = i64
+        L.orc_groupby.argtypes = [vp, vp, u64, i32, C.c_int, vp, vp, vp, vp, vp, u64]
+        L.orc_reduce.restype = None
+        L.orc_reduce.argtypes = [vp, vp, u64, vp, vp, i32, vp]
+        _lib = L
+    return _lib
+
+
+def ref_lib():
+    """The reference's own RJStepwise / partitionHT (None if not built)."""
+    global _ref
+    if _ref is None and os.path.exists(REF_LIB):
+        R = C.CDLL(REF_LIB)
+        R.ref_rj_stepwise.restype = i64
+        R.ref_rj_stepwise.argtypes = [vp, C.c_uint32, vp, C.c_uint32]
+        R.ref_partition_ht.restype = None
+        R.ref_partition_ht.argtypes = [vp, C.c_uint32, vp, vp, vp]
+        R.ref_num_radix_bits.restype = i32
+        _ref = R
+    return _ref
+
+
+def _p(a):
+    return None if a is None else a.ctypes.data_as(vp)
+
+
+def _i32(a):
+    return None if a is None else np.ascontiguousarray(a, dtype=np.int32)
+
+
+def _aggs(aggs):
+    ops = np.array([a[0] for a in aggs], dtype=np.int32)
+    opd = np.array([a[1] for a in aggs], dtype=np.int32)
+    return ops, opd
+
+
+def join_agg(bkeys, bpay, pkeys, ppay, aggs, hash_bits=0, threads=1):
+    """HashJoinChained build + probe with the fused aggregates -> int64 list."""
+    L = lib()
+    bkeys, bpay, pkeys, ppay = _i32(bkeys), _i32(bpay), _i32(pkeys), _i32(ppay)
+    t = ChainedTable()
+    if threads > 1:
+        rc = L.orc_join_build_mt(_p(bkeys), _p(bpay), len(bkeys), hash_bits, threads, C.byref(t))
+    else:
+        rc = L.orc_join_build(_p(bkeys), _p(bpay), len(bkeys), hash_bits, C.byref(t))
+    assert rc == 0
+    ops, opd = _aggs(aggs)
+    out = np.zeros(len(aggs), dtype=np.int64)
+    rc = L.orc_join_probe_agg(C.byref(t), _p(pkeys), _p(ppay), len(pkeys), _p(ops), _p(opd),
+                              len(aggs), _p(out), threads)
+    L.orc_join_free(C.byref(t))
+    assert rc == 0
+    return [int(x) for x in out]
+
+
+def join_pairs(bkeys, pkeys, hash_bits=0):
+    L = lib()
+    bkeys, pkeys = _i32(bkeys), _i32(pkeys)
+    t = ChainedTable()
+    assert L.orc_join_build(_p(bkeys), None, len(bkeys), hash_bits, C.byref(t)) == 0
+    m = L.orc_join_probe_pairs(C.byref(t), _p(pkeys), len(pkeys), None, None, 0)
+    b = np.empty(max(m, 1), dtype=np.int32)
+    p = np.empty(max(m, 1), dtype=np.int32)
+    L.orc_join_probe_pairs(C.byref(t), _p(pkeys), len(pkeys), _p(b), _p(p), m)
+    L.orc_join_free(C.byref(t))
+    return b[:m], p[:m]
+
+
+def radix_cluster(keys, payload, R, D, hashed):
+    L = lib()
+    keys, payload = _i32(keys), _i32(payload)
+    n = len(keys)
+    ok = np.empty(max(n, 1), dtype=np.int32)
+    op = np.empty(max(n, 1), dtype=np.int32)
+    off = np.empty((1 << D) + 1, dtype=np.uint64)
+    L.orc_radix_cluster(_p(keys), _p(payload), n, R, D, int(hashed), _p(ok), _p(op), _p(off))
+    return ok[:n], op[:n], off
+
+
+def rj_stepwise(rkeys, skeys):
+    L = lib()
+    rkeys, skeys = _i32(rkeys), _i32(skeys)
+    return int(L.orc_rj_stepwise(_p(rkeys), len(rkeys), _p(skeys), len(skeys)))
+
+
+def partition_ht_counts(keys):
+    L = lib()
+    keys = _i32(keys)
+    c = np.empty(1 << 14, dtype=np.int32)
+    L.orc_partition_ht_counts(_p(keys), len(keys), _p(c))
+    return c
+
+
+def radix_join_agg(bkeys, bpay, pkeys, ppay, aggs, bits=0, threads=1):
+    L = lib()
+    bkeys, bpay, pkeys, ppay = _i32(bkeys), _i32(bpay), _i32(pkeys), _i32(ppay)
+    ops, opd = _aggs(aggs)
+    out = np.zeros(len(aggs), dtype=np.int64)
+    rc = L.orc_radix_join_agg(_p(bkeys), _p(bpay), len(bkeys), _p(pkeys), _p(ppay), len(pkeys),
+                              bits, _p(ops), _p(opd), len(aggs), _p(out), threads)
+    assert rc == 0
+    return [int(x) for x in out]
+
+
+def groupby(keys, values, hash_bits=0, threads=1):
+    """-> (keys, count, sum, min, max) sorted by key."""
+    L = lib()
+    keys, values = _i32(keys), _i32(values)
+    n = len(keys)
+    ng = L.orc_groupby(_p(keys), _p(values), n, hash_bits, threads, None, None, None, None, None, 0)
+    assert ng >= 0
+    k = np.empty(max(ng, 1), dtype=np.int32)
+    c = np.empty(max(ng, 1), dtype=np.int64)
+    s = np.empty(max(ng, 1), dtype=np.int64)
+    mn = np.empty(max(ng, 1), dtype=np.int32)
+    mx = np.empty(max(ng, 1), dtype=np.int32)
+    ng2 = L.orc_groupby(_p(keys), _p(values), n, hash_bits, threads, _p(k), _p(c), _p(s), _p(mn),
+                        _p(mx), ng)
+    assert ng2 == ng
+    return k[:ng], c[:ng], s[:ng], mn[:ng], mx[:ng]
+
+
+def reduce(col, aggs, rows=None):
+    L = lib()
+    col, rows = _i32(col), _i32(rows)
+    ops, opd = _aggs(aggs)
+    out = np.zeros(len(aggs), dtype=np.int64)
+    n = len(rows) if rows is not None else len(col)
+    L.orc_reduce(_p(col), _p(rows), n, _p(ops), _p(opd), len(aggs), _p(out))
+    return [int(x) for x in out]
+
+
+def ref_rj_stepwise(rkeys, skeys):
+    R = ref_lib()
+    if R is None:
+        return None
+    rkeys, skeys = _i32(rkeys), _i32(skeys)
+    return int(R.ref_rj_stepwise(_p(rkeys), len(rkeys), _p(skeys), len(skeys)))
+
+
+def ref_partition_ht(keys):
+    R = ref_lib()
+    if R is None:
+        return None
+    keys = _i32(keys)
+    n = len(keys)
+    c = np.empty(1 << 14, dtype=np.int32)
+    ok = np.empty(max(n, 1), dtype=np.int32)
+    orows = np.empty(max(n, 1), dtype=np.int64)
+    R.ref_partition_ht(_p(keys), n, _p(c), _p(ok), _p(orows))
+    return c, ok[:n], orows[:n]

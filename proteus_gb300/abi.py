@@ -1,0 +1,113 @@
+"""ctypes binding of libgbjoin.so (the C ABI declared in include/gbjoin.h).
+
+The product is the shared library; this module only loads it and gives the
+entry points Python signatures.  Importing it on a machine without the built
+library raises -- there is no fallback implementation.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libgbjoin.so")
+
+OK, ERR_INVALID, ERR_OOM, ERR_CAPACITY, ERR_TIMEOUT, ERR_CUDA, ERR_UNSUPPORTED, \
+    ERR_BUDGET, ERR_CANCELLED = range(9)
+STATUS_NAMES = {0: "OK", 1: "INVALID", 2: "OOM", 3: "CAPACITY", 4: "TIMEOUT", 5: "CUDA",
+                6: "UNSUPPORTED", 7: "BUDGET", 8: "CANCELLED"}
+
+AGG_COUNT, AGG_SUM, AGG_MIN, AGG_MAX = range(4)
+(VAL_ONE, VAL_BUILD, VAL_PROBE, VAL_PRODUCT, VAL_BUILD_ROWID, VAL_PROBE_ROWID,
+ VAL_ROWID_XOR, VAL_BUILD_KEY) = range(8)
+DIGIT_KEY, DIGIT_HASH = 0, 1
+MAX_AGGS = 8
+
+
+class Agg(C.Structure):
+    _fields_ = [("op", C.c_int32), ("operand", C.c_int32)]
+
+
+class RadixParams(C.Structure):
+    _fields_ = [("bits", C.c_int32), ("passes", C.c_int32), ("block", C.c_int32),
+                ("log_parts", C.c_int32)]
+
+
+class GroupbyParams(C.Structure):
+    _fields_ = [("hash_bits", C.c_int32), ("strategy", C.c_int32),
+                ("max_input_size", C.c_uint64), ("expected_groups", C.c_uint64)]
+
+
+vp, u64, i32, i64, dbl = C.c_void_p, C.c_uint64, C.c_int32, C.c_int64, C.c_double
+P = C.POINTER
+
+# name -> (restype, argtypes); mirrors include/gbjoin.h
+SIGNATURES = {
+    "gbj_ctx_create": (C.c_int, [C.c_int, u64, P(vp)]),
+    "gbj_ctx_destroy": (C.c_int, [vp]),
+    "gbj_last_error": (C.c_char_p, [vp]),
+    "gbj_ctx_device_info": (C.c_int, [vp, P(C.c_int), P(u64), P(u64)]),
+    "gbj_sync": (C.c_int, [vp, vp]),
+    "gbj_kernel_launches": (u64, [vp]),
+    "gbj_profile_enable": (C.c_int, [vp, C.c_int]),
+    "gbj_profile_kernel": (C.c_int, [vp, C.c_char_p, P(u64), P(dbl)]),
+    "gbj_profile_dump": (C.c_int, [vp, C.c_char_p, u64]),
+    "gbj_pool_alloc": (C.c_int, [vp, u64, P(vp)]),
+    "gbj_pool_free": (C.c_int, [vp, vp]),
+    "gbj_pool_stats": (C.c_int, [vp, P(u64), P(u64), P(u64)]),
+    "gbj_join_build": (C.c_int, [vp, vp, vp, u64, i32, u64, vp, P(vp)]),
+    "gbj_join_probe_agg": (C.c_int, [vp, vp, vp, vp, u64, P(Agg), i32, vp, vp]),
+    "gbj_join_probe_pairs": (C.c_int, [vp, vp, vp, vp, u64, vp, vp, u64, vp, vp]),
+    "gbj_table_destroy": (C.c_int, [vp, vp]),
+    "gbj_table_slots": (u64, [vp]),
+    "gbj_partition": (C.c_int, [vp, vp, vp, u64, i32, i32, i32, vp, vp, vp, vp]),
+    "gbj_radix_join_agg": (C.c_int, [vp, vp, vp, u64, vp, vp, u64, P(RadixParams), P(Agg), i32,
+                                     vp, vp]),
+    "gbj_groupby": (C.c_int, [vp, vp, vp, u64, P(GroupbyParams), vp, vp, vp, vp, vp, u64, vp,
+                              vp]),
+    "gbj_reduce": (C.c_int, [vp, vp, vp, u64, P(Agg), i32, vp, vp]),
+    "gbj_gather": (C.c_int, [vp, vp, vp, u64, vp, vp]),
+    "gbj_select_range": (C.c_int, [vp, vp, u64, i32, i32, vp, vp, vp]),
+    "gbj_gen_build_side": (C.c_int, [u64, u64, vp, vp, C.c_int]),
+    "gbj_gen_probe_uniform": (C.c_int, [u64, u64, u64, vp, vp, C.c_int]),
+    "gbj_gen_probe_zipf": (C.c_int, [u64, u64, u64, dbl, dbl, vp, vp, C.c_int]),
+    "gbj_gen_groupby": (C.c_int, [u64, u64, u64, dbl, vp, vp, C.c_int]),
+    "gbj_gen_rand": (u64, [u64, u64, u64]),
+    "gbj_gen_perm": (u64, [u64, u64, u64, u64]),
+    "gbj_gen_zipf": (u64, [u64, u64, u64, dbl, u64]),
+    "gbj_gen_det_log": (dbl, [dbl]),
+    "gbj_gen_det_exp": (dbl, [dbl]),
+}
+
+_lib = None
+
+
+def load(path: str = LIB_PATH) -> C.CDLL:
+    """Loads the library (once) and applies the signatures."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise RuntimeError(f"{path} is not built; run `python -m proteus_gb300.build`")
+    lib = C.CDLL(path)
+    for name, (res, args) in SIGNATURES.items():
+        f = getattr(lib, name, None)
+        if f is None:
+            continue
+        f.restype = res
+        f.argtypes = args
+    _lib = lib
+    return lib
+
+
+class GbjError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"{STATUS_NAMES.get(code, code)}: {msg}")
+        self.code = code
+
+
+def aggs_array(aggs):
+    arr = (Agg * len(aggs))()
+    for i, (op, operand) in enumerate(aggs):
+        arr[i].op, arr[i].operand = op, operand
+    return arr

@@ -1,0 +1,412 @@
+// Non-partitioned hash join: build, probe with fused aggregate, probe with
+// pair materialisation; plus the column helpers (reduce, gather, select).
+//
+// Replaces the JIT'd build / probe loops of HashJoinChained and
+// GpuHashJoinChained (core/olap/lib/operators/hash-join-chained.cpp:262-566,
+// core/olap/lib/operators/gpu/gpu-hash-join-chained.cpp:31-73).  The
+// reference chains entries behind a head array; here the table is an
+// open-addressing array of 64-bit slots {key, row+1} (0 = empty) sized to a
+// power of two with load factor <= 1/2, so a probe is one L2 sector in the
+// common case and the table for a 2^20-row build side (16 MiB) stays
+// resident in the 129 MB L2 while the probe side streams from HBM.
+// Semantics are the reference's: every build row is inserted (duplicates
+// allowed) and a probe row meets every build row with an equal key.
+#include <cooperative_groups.h>
+
+#include "gbj_internal.cuh"
+#include "scan.cuh"
+
+namespace cg = cooperative_groups;
+using namespace gbj;
+
+namespace {
+
+constexpr int kThreads = 512;
+
+__device__ __forceinline__ uint64_t make_slot(int32_t key, uint64_t row) {
+  return ((row + 1) << 32) | (uint32_t)key;
+}
+__device__ __forceinline__ int32_t slot_key(uint64_t e) { return (int32_t)(uint32_t)e; }
+__device__ __forceinline__ uint32_t slot_row(uint64_t e) { return (uint32_t)(e >> 32) - 1; }
+
+// meta[0] = 1 once a duplicate build key was seen (probes may then not stop
+// at the first match).
+__global__ void __launch_bounds__(kThreads)
+    k_join_build(const int32_t *__restrict__ keys, uint64_t n,
+                 uint64_t *__restrict__ slots, uint64_t mask,
+                 uint32_t *__restrict__ meta, uint32_t *status) {
+  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += stride) {
+    const int32_t k = keys[i];
+    const uint64_t entry = make_slot(k, i);
+    uint64_t h = gbjd::fmix32((uint32_t)k) & mask;
+    bool dup = false, placed = false;
+    for (uint64_t probe = 0; probe <= mask; ++probe) {
+      uint64_t cur = *(volatile uint64_t *)&slots[h];
+      if (cur == 0) {
+        cur = atomicCAS((unsigned long long *)&slots[h], 0ull, (unsigned long long)entry);
+        if (cur == 0) {
+          placed = true;
+          break;
+        }
+      }
+      dup |= (slot_key(cur) == k);
+      h = (h + 1) & mask;
+    }
+    if (dup) meta[0] = 1;
+    if (!placed) gbjd::latch(status, GBJ_DEV_CAPACITY);
+  }
+}
+
+// Probe with fused aggregate.  Four probe keys per thread: their first slot
+// loads are issued together so each thread keeps several L2 requests in
+// flight; chains past the first slot are walked afterwards.
+template <bool kVec>
+__global__ void __launch_bounds__(kThreads)
+    k_join_probe_agg(const int32_t *__restrict__ keys,
+                     const int32_t *__restrict__ pay, uint64_t n,
+                     const uint64_t *__restrict__ slots, uint64_t mask,
+                     const int32_t *__restrict__ bpay,
+                     const uint32_t *__restrict__ meta, gbj::AggSpec spec,
+                     int64_t *out) {
+  __shared__ int64_t red[32 * GBJ_MAX_AGGS];
+  gbjd::Acc acc;
+  acc.init(spec);
+  const bool unique = meta[0] == 0;
+  const uint64_t nq = n / 4;
+  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  auto probe_one = [&](int32_t k, int64_t pv, uint64_t prow, uint64_t h,
+                       uint64_t e) {
+    for (uint64_t step = 0; step <= mask; ++step) {
+      if (e == 0) break;
+      if (slot_key(e) == k) {
+        const uint32_t r = slot_row(e);
+        const int64_t bv = bpay ? __ldg(&bpay[r]) : 0;
+        acc.update(spec, k, bv, pv, r, prow);
+        if (unique) break;
+      }
+      h = (h + 1) & mask;
+      e = __ldg(&slots[h]);
+    }
+  };
+  if (kVec) {
+    for (uint64_t q = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; q < nq; q += stride) {
+      const int4 k4 = __ldcs(reinterpret_cast<const int4 *>(keys) + q);
+      int4 p4 = make_int4(0, 0, 0, 0);
+      if (pay) p4 = __ldcs(reinterpret_cast<const int4 *>(pay) + q);
+      const int32_t kk[4] = {k4.x, k4.y, k4.z, k4.w};
+      const int32_t pp[4] = {p4.x, p4.y, p4.z, p4.w};
+      uint64_t h[4], e[4];
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        h[j] = gbjd::fmix32((uint32_t)kk[j]) & mask;
+        e[j] = __ldg(&slots[h[j]]);
+      }
+#pragma unroll
+      for (int j = 0; j < 4; ++j) probe_one(kk[j], pp[j], q * 4 + j, h[j], e[j]);
+    }
+    // tail (n % 4 rows) by the first threads of block 0
+    if (blockIdx.x == 0 && threadIdx.x < (n & 3)) {
+      const uint64_t i = nq * 4 + threadIdx.x;
+      const int32_t k = keys[i];
+      const uint64_t h = gbjd::fmix32((uint32_t)k) & mask;
+      probe_one(k, pay ? pay[i] : 0, i, h, __ldg(&slots[h]));
+    }
+  } else {
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += stride) {
+      const int32_t k = keys[i];
+      const uint64_t h = gbjd::fmix32((uint32_t)k) & mask;
+      probe_one(k, pay ? pay[i] : 0, i, h, __ldg(&slots[h]));
+    }
+  }
+  gbjd::block_flush(spec, acc, red, out);
+}
+
+// Probe emitting (build row, probe row) pairs through warp-aggregated
+// reservations of the output cursor.
+__global__ void __launch_bounds__(kThreads)
+    k_join_probe_pairs(const int32_t *__restrict__ keys,
+                       const int32_t *__restrict__ prows, uint64_t n,
+                       const uint64_t *__restrict__ slots, uint64_t mask,
+                       const uint32_t *__restrict__ meta,
+                       int32_t *__restrict__ out_b, int32_t *__restrict__ out_p,
+                       uint64_t cap, unsigned long long *count,
+                       uint32_t *status) {
+  const bool unique = meta[0] == 0;
+  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += stride) {
+    const int32_t k = keys[i];
+    const int32_t pr = prows ? prows[i] : (int32_t)i;
+    uint64_t h = gbjd::fmix32((uint32_t)k) & mask;
+    for (uint64_t step = 0; step <= mask; ++step) {
+      const uint64_t e = __ldg(&slots[h]);
+      if (e == 0) break;
+      if (slot_key(e) == k) {
+        cg::coalesced_group g = cg::coalesced_threads();
+        unsigned long long base = 0;
+        if (g.thread_rank() == 0) base = atomicAdd(count, (unsigned long long)g.size());
+        base = g.shfl(base, 0) + g.thread_rank();
+        if (base < cap) {
+          out_b[base] = (int32_t)slot_row(e);
+          out_p[base] = pr;
+        } else {
+          gbjd::latch(status, GBJ_DEV_CAPACITY);
+        }
+        if (unique) break;
+      }
+      h = (h + 1) & mask;
+    }
+  }
+}
+
+// Column reduce (Reduce over one column, optional row list).
+__global__ void __launch_bounds__(kThreads)
+    k_reduce(const int32_t *__restrict__ col, const int32_t *__restrict__ rows,
+             uint64_t n, gbj::AggSpec spec, int64_t *out) {
+  __shared__ int64_t red[32 * GBJ_MAX_AGGS];
+  gbjd::Acc acc;
+  acc.init(spec);
+  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += stride) {
+    const int64_t r = rows ? rows[i] : (int64_t)i;
+    const int64_t v = col ? col[r] : 0;
+    acc.update(spec, (int32_t)v, v, v, r, r);
+  }
+  gbjd::block_flush(spec, acc, red, out);
+}
+
+__global__ void k_gather(const int32_t *__restrict__ col,
+                         const int32_t *__restrict__ rows, uint64_t n,
+                         int32_t *__restrict__ out) {
+  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += stride)
+    out[i] = col[rows[i]];
+}
+
+constexpr int kSelTile = 4096;  // rows per select tile (one block)
+
+__global__ void __launch_bounds__(1024)
+    k_select_count(const int32_t *__restrict__ col, uint64_t n, int32_t lo,
+                   int32_t hi, uint64_t *tile_counts) {
+  __shared__ uint32_t c;
+  if (threadIdx.x == 0) c = 0;
+  __syncthreads();
+  uint32_t mine = 0;
+  const uint64_t base = (uint64_t)blockIdx.x * kSelTile;
+  for (int j = threadIdx.x; j < kSelTile; j += blockDim.x) {
+    uint64_t i = base + j;
+    if (i < n) {
+      int32_t v = col[i];
+      mine += (v >= lo && v <= hi);
+    }
+  }
+  mine = __reduce_add_sync(0xffffffffu, mine);
+  if ((threadIdx.x & 31) == 0) atomicAdd(&c, mine);
+  __syncthreads();
+  if (threadIdx.x == 0) tile_counts[blockIdx.x] = c;
+}
+
+// Stable compaction: rows of a tile are emitted in order, chunk by chunk.
+__global__ void __launch_bounds__(1024)
+    k_select_write(const int32_t *__restrict__ col, uint64_t n, int32_t lo,
+                   int32_t hi, const uint64_t *tile_off, int32_t *out) {
+  __shared__ uint32_t warp_cnt[32];
+  __shared__ uint64_t run;
+  if (threadIdx.x == 0) run = tile_off[blockIdx.x];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const uint64_t base = (uint64_t)blockIdx.x * kSelTile;
+  for (int j0 = 0; j0 < kSelTile; j0 += blockDim.x) {
+    __syncthreads();
+    const uint64_t i = base + j0 + threadIdx.x;
+    const bool pass = i < n && col[i] >= lo && col[i] <= hi;
+    const uint32_t b = __ballot_sync(0xffffffffu, pass);
+    if (lane == 0) warp_cnt[warp] = __popc(b);
+    __syncthreads();
+    uint64_t before = run;
+    for (int w = 0; w < warp; ++w) before += warp_cnt[w];
+    if (pass) out[before + __popc(b & ((1u << lane) - 1))] = (int32_t)i;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      uint64_t t = 0;
+      for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += warp_cnt[w];
+      run += t;
+    }
+  }
+}
+
+__global__ void k_copy_total(const uint64_t *off, uint64_t ntiles, uint64_t *dst) {
+  *dst = off[ntiles];
+}
+
+int grid_for(gbj_ctx *ctx, uint64_t work, int threads, int per_sm = 4) {
+  uint64_t blocks = (work + threads - 1) / threads;
+  uint64_t cap = (uint64_t)ctx->sm_count * per_sm;
+  if (blocks > cap) blocks = cap;
+  if (blocks == 0) blocks = 1;
+  return (int)blocks;
+}
+
+}  // namespace
+
+extern "C" {
+
+int gbj_join_build(gbj_ctx *ctx, const int32_t *d_keys,
+                   const int32_t *d_payload, uint64_t n, int32_t hash_bits,
+                   uint64_t max_build, void *stream, gbj_table **out) {
+  if (!ctx || !out) return GBJ_ERR_INVALID;
+  *out = nullptr;
+  if (n && !d_keys) return set_error(ctx, GBJ_ERR_INVALID, "join_build: null keys");
+  if (n >= (1ULL << 31)) return set_error(ctx, GBJ_ERR_INVALID, "join_build: n >= 2^31");
+  if (hash_bits < 0 || hash_bits > 31)
+    return set_error(ctx, GBJ_ERR_INVALID, "join_build: hash_bits out of range");
+  if (max_build && n > max_build)
+    return set_error(ctx, GBJ_ERR_CAPACITY,
+                     "Build input size exceeded given parameter (maxBuildInputSize)");
+  cudaStream_t s = pick_stream(ctx, stream);
+  prof_mark(ctx, s);
+  uint64_t slots = next_pow2(2 * (n ? n : 1));
+  if (hash_bits && (1ULL << hash_bits) > slots) slots = 1ULL << hash_bits;
+  if (slots < 64) slots = 64;
+  gbj_table *t = new gbj_table();
+  void *mem = nullptr;
+  int rc = pool_alloc(ctx, slots * sizeof(uint64_t) + 256, s, &mem);
+  if (rc) {
+    delete t;
+    return rc;
+  }
+  t->slots = (uint64_t *)mem;
+  t->mask = slots - 1;
+  t->keys = d_keys;
+  t->payload = d_payload;
+  t->n = n;
+  uint32_t *meta = (uint32_t *)(t->slots + slots);
+  cudaError_t e = cudaMemsetAsync(mem, 0, slots * sizeof(uint64_t) + 256, s);
+  if (e != cudaSuccess) {
+    pool_release(ctx, mem, s);
+    delete t;
+    return cuda_error(ctx, e, "cudaMemsetAsync(table)");
+  }
+  if (n) {
+    k_join_build<<<grid_for(ctx, n, kThreads), kThreads, 0, s>>>(d_keys, n, t->slots, t->mask,
+                                                                 meta, ctx->d_status);
+    rc = after_launch(ctx, "k_join_build", s);
+    if (rc) {
+      pool_release(ctx, mem, s);
+      delete t;
+      return rc;
+    }
+  }
+  *out = t;
+  return GBJ_OK;
+}
+
+int gbj_table_destroy(gbj_ctx *ctx, gbj_table *table) {
+  if (!ctx || !table) return GBJ_ERR_INVALID;
+  int rc = pool_release(ctx, table->slots, ctx->stream);
+  delete table;
+  return rc;
+}
+
+uint64_t gbj_table_slots(const gbj_table *table) { return table ? table->mask + 1 : 0; }
+
+int gbj_join_probe_agg(gbj_ctx *ctx, const gbj_table *t, const int32_t *d_keys,
+                       const int32_t *d_payload, uint64_t n, const gbj_agg *aggs,
+                       int32_t n_aggs, int64_t *d_out, void *stream) {
+  if (!ctx || !t || !d_out) return GBJ_ERR_INVALID;
+  if (n && !d_keys) return set_error(ctx, GBJ_ERR_INVALID, "join_probe: null keys");
+  GBJ_TRY(validate_aggs(ctx, aggs, n_aggs));
+  AggSpec spec = make_spec(aggs, n_aggs);
+  for (int j = 0; j < n_aggs; ++j) {
+    int o = spec.operand[j];
+    if ((o == GBJ_VAL_BUILD || o == GBJ_VAL_PRODUCT) && !t->payload)
+      return set_error(ctx, GBJ_ERR_INVALID, "aggregate reads the build payload, table has none");
+    if ((o == GBJ_VAL_PROBE || o == GBJ_VAL_PRODUCT) && !d_payload)
+      return set_error(ctx, GBJ_ERR_INVALID, "aggregate reads the probe payload, none given");
+  }
+  cudaStream_t s = pick_stream(ctx, stream);
+  prof_mark(ctx, s);
+  GBJ_TRY(init_agg_out(ctx, spec, d_out, s));
+  if (n == 0) return GBJ_OK;
+  const uint32_t *meta = (const uint32_t *)(t->slots + t->mask + 1);
+  const bool vec = ((uintptr_t)d_keys % 16 == 0) &&
+                   (!d_payload || (uintptr_t)d_payload % 16 == 0);
+  if (vec) {
+    k_join_probe_agg<true><<<grid_for(ctx, (n + 3) / 4, kThreads), kThreads, 0, s>>>(
+        d_keys, d_payload, n, t->slots, t->mask, t->payload, meta, spec, d_out);
+  } else {
+    k_join_probe_agg<false><<<grid_for(ctx, n, kThreads), kThreads, 0, s>>>(
+        d_keys, d_payload, n, t->slots, t->mask, t->payload, meta, spec, d_out);
+  }
+  return after_launch(ctx, "k_join_probe_agg", s);
+}
+
+int gbj_join_probe_pairs(gbj_ctx *ctx, const gbj_table *t, const int32_t *d_keys,
+                         const int32_t *d_probe_rows, uint64_t n,
+                         int32_t *d_build_rows, int32_t *d_out_probe_rows,
+                         uint64_t capacity, uint64_t *d_count, void *stream) {
+  if (!ctx || !t || !d_count || !d_build_rows || !d_out_probe_rows)
+    return GBJ_ERR_INVALID;
+  if (n && !d_keys) return set_error(ctx, GBJ_ERR_INVALID, "join_probe: null keys");
+  cudaStream_t s = pick_stream(ctx, stream);
+  prof_mark(ctx, s);
+  GBJ_CHECK_CUDA(ctx, cudaMemsetAsync(d_count, 0, sizeof(uint64_t), s));
+  if (n == 0) return GBJ_OK;
+  const uint32_t *meta = (const uint32_t *)(t->slots + t->mask + 1);
+  k_join_probe_pairs<<<grid_for(ctx, n, kThreads), kThreads, 0, s>>>(
+      d_keys, d_probe_rows, n, t->slots, t->mask, meta, d_build_rows, d_out_probe_rows,
+      capacity, (unsigned long long *)d_count, ctx->d_status);
+  return after_launch(ctx, "k_join_probe_pairs", s);
+}
+
+int gbj_reduce(gbj_ctx *ctx, const int32_t *d_col, const int32_t *d_rows,
+               uint64_t n, const gbj_agg *aggs, int32_t n_aggs, int64_t *d_out,
+               void *stream) {
+  if (!ctx || !d_out) return GBJ_ERR_INVALID;
+  GBJ_TRY(validate_aggs(ctx, aggs, n_aggs));
+  AggSpec spec = make_spec(aggs, n_aggs);
+  for (int j = 0; j < n_aggs; ++j)
+    if (spec.operand[j] != GBJ_VAL_ONE && !d_col)
+      return set_error(ctx, GBJ_ERR_INVALID, "reduce: aggregate reads a null column");
+  cudaStream_t s = pick_stream(ctx, stream);
+  prof_mark(ctx, s);
+  GBJ_TRY(init_agg_out(ctx, spec, d_out, s));
+  if (n == 0) return GBJ_OK;
+  k_reduce<<<grid_for(ctx, n, kThreads), kThreads, 0, s>>>(d_col, d_rows, n, spec, d_out);
+  return after_launch(ctx, "k_reduce", s);
+}
+
+int gbj_gather(gbj_ctx *ctx, const int32_t *d_col, const int32_t *d_rows,
+               uint64_t n, int32_t *d_out, void *stream) {
+  if (!ctx || (n && (!d_col || !d_rows || !d_out))) return GBJ_ERR_INVALID;
+  if (n == 0) return GBJ_OK;
+  cudaStream_t s = pick_stream(ctx, stream);
+  prof_mark(ctx, s);
+  k_gather<<<grid_for(ctx, n, 256, 8), 256, 0, s>>>(d_col, d_rows, n, d_out);
+  return after_launch(ctx, "k_gather", s);
+}
+
+int gbj_select_range(gbj_ctx *ctx, const int32_t *d_col, uint64_t n, int32_t lo,
+                     int32_t hi, int32_t *d_rows_out, uint64_t *d_count,
+                     void *stream) {
+  if (!ctx || !d_count || (n && (!d_col || !d_rows_out))) return GBJ_ERR_INVALID;
+  if (n >= (1ULL << 31)) return set_error(ctx, GBJ_ERR_INVALID, "select: n >= 2^31");
+  cudaStream_t s = pick_stream(ctx, stream);
+  prof_mark(ctx, s);
+  if (n == 0) {
+    GBJ_CHECK_CUDA(ctx, cudaMemsetAsync(d_count, 0, sizeof(uint64_t), s));
+    return GBJ_OK;
+  }
+  const uint64_t ntiles = (n + kSelTile - 1) / kSelTile;
+  Scratch scratch(ctx, s);
+  uint64_t *cnt;
+  GBJ_TRY(scratch.get(ntiles + 1, &cnt));
+  k_select_count<<<(unsigned)ntiles, 1024, 0, s>>>(d_col, n, lo, hi, cnt);
+  GBJ_TRY(after_launch(ctx, "k_select_count", s));
+  GBJ_TRY(scan_u64(ctx, cnt, cnt, ntiles, s));
+  k_select_write<<<(unsigned)ntiles, 1024, 0, s>>>(d_col, n, lo, hi, cnt, d_rows_out);
+  GBJ_TRY(after_launch(ctx, "k_select_write", s));
+  k_copy_total<<<1, 1, 0, s>>>(cnt, ntiles, d_count);
+  return after_launch(ctx, "k_copy_total", s);
+}
+
+}  // extern "C"

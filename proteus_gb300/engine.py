@@ -1,0 +1,258 @@
+"""Python wrapper over the C ABI for callers that hold torch CUDA tensors.
+
+Device memory comes from torch tensors (the caller's) or from the library's
+resident pool (scratch); kernels run on torch's current CUDA stream unless a
+stream is given.  Host-side generators return numpy arrays.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import abi
+
+
+def _ptr(t) -> int | None:
+    if t is None:
+        return None
+    return t.data_ptr()
+
+
+def _cur_stream():
+    import torch
+
+    return torch.cuda.current_stream().cuda_stream
+
+
+class Table:
+    """A built join hash table (gbj_table); keeps its input tensors alive."""
+
+    def __init__(self, ctx: "Context", handle: int, keep):
+        self.ctx, self.handle, self._keep = ctx, handle, keep
+
+    @property
+    def slots(self) -> int:
+        return int(self.ctx.lib.gbj_table_slots(self.handle))
+
+    def destroy(self):
+        if self.handle:
+            self.ctx.lib.gbj_table_destroy(self.ctx.handle, self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.destroy()
+        except Exception:
+            pass
+
+
+class Context:
+    """One device context with its resident pool (gbj_ctx)."""
+
+    def __init__(self, device: int = 0, pool_bytes: int = 0):
+        self.lib = abi.load()
+        h = C.c_void_p()
+        rc = self.lib.gbj_ctx_create(device, pool_bytes, C.byref(h))
+        if rc != abi.OK:
+            raise abi.GbjError(rc, "gbj_ctx_create failed")
+        self.handle = h.value
+        self.device = device
+
+    # ------------------------------------------------------------ basics
+    def check(self, rc: int):
+        if rc != abi.OK:
+            msg = self.lib.gbj_last_error(self.handle)
+            raise abi.GbjError(rc, msg.decode() if msg else "")
+
+    def sync(self, stream=None):
+        self.check(self.lib.gbj_sync(self.handle, stream if stream is not None else _cur_stream()))
+
+    def launches(self) -> int:
+        return int(self.lib.gbj_kernel_launches(self.handle))
+
+    def device_info(self):
+        sm, l2, smem = C.c_int(), C.c_uint64(), C.c_uint64()
+        self.check(self.lib.gbj_ctx_device_info(self.handle, C.byref(sm), C.byref(l2), C.byref(smem)))
+        return {"sm_count": sm.value, "l2_bytes": l2.value, "smem_optin": smem.value}
+
+    def pool_stats(self):
+        a, b, c = C.c_uint64(), C.c_uint64(), C.c_uint64()
+        self.check(self.lib.gbj_pool_stats(self.handle, C.byref(a), C.byref(b), C.byref(c)))
+        return {"capacity": a.value, "in_use": b.value, "peak": c.value}
+
+    def profile(self, on: bool):
+        self.check(self.lib.gbj_profile_enable(self.handle, 1 if on else 0))
+
+    def profile_kernel(self, name: str):
+        n, ms = C.c_uint64(), C.c_double()
+        self.check(self.lib.gbj_profile_kernel(self.handle, name.encode(), C.byref(n), C.byref(ms)))
+        return n.value, ms.value
+
+    def profile_dump(self):
+        buf = C.create_string_buffer(1 << 16)
+        self.check(self.lib.gbj_profile_dump(self.handle, buf, len(buf)))
+        out = {}
+        for line in buf.value.decode().splitlines():
+            name, cnt, ms = line.split()
+            out[name] = (int(cnt), float(ms))
+        return out
+
+    def close(self):
+        if getattr(self, "handle", None):
+            self.lib.gbj_ctx_destroy(self.handle)
+            self.handle = None
+
+    def _s(self, stream):
+        return stream if stream is not None else _cur_stream()
+
+    # ------------------------------------------------------------- joins
+    def join_build(self, keys, payload=None, hash_bits=0, max_build=0, stream=None) -> Table:
+        h = C.c_void_p()
+        self.check(self.lib.gbj_join_build(self.handle, _ptr(keys), _ptr(payload), keys.numel(),
+                                           hash_bits, max_build, self._s(stream), C.byref(h)))
+        return Table(self, h.value, (keys, payload))
+
+    def join_probe_agg(self, table: Table, keys, payload, aggs, out=None, stream=None):
+        import torch
+
+        if out is None:
+            out = torch.empty(len(aggs), dtype=torch.int64, device=keys.device)
+        arr = abi.aggs_array(aggs)
+        self.check(self.lib.gbj_join_probe_agg(self.handle, table.handle, _ptr(keys), _ptr(payload),
+                                               keys.numel(), arr, len(aggs), _ptr(out),
+                                               self._s(stream)))
+        return out
+
+    def join_probe_pairs(self, table: Table, keys, capacity, probe_rows=None, stream=None):
+        import torch
+
+        dev = keys.device
+        b = torch.empty(max(capacity, 1), dtype=torch.int32, device=dev)
+        p = torch.empty(max(capacity, 1), dtype=torch.int32, device=dev)
+        cnt = torch.zeros(1, dtype=torch.int64, device=dev)
+        self.check(self.lib.gbj_join_probe_pairs(self.handle, table.handle, _ptr(keys),
+                                                 _ptr(probe_rows), keys.numel(), _ptr(b), _ptr(p),
+                                                 capacity, _ptr(cnt), self._s(stream)))
+        return b, p, cnt
+
+    def radix_join_agg(self, bkeys, bpay, pkeys, ppay, aggs, out=None, bits=0, passes=0,
+                       log_parts=0, stream=None):
+        import torch
+
+        if out is None:
+            out = torch.empty(len(aggs), dtype=torch.int64, device=bkeys.device)
+        prm = abi.RadixParams(bits, passes, 0, log_parts)
+        arr = abi.aggs_array(aggs)
+        self.check(self.lib.gbj_radix_join_agg(self.handle, _ptr(bkeys), _ptr(bpay), bkeys.numel(),
+                                               _ptr(pkeys), _ptr(ppay), pkeys.numel(),
+                                               C.byref(prm), arr, len(aggs), _ptr(out),
+                                               self._s(stream)))
+        return out
+
+    def partition(self, keys, payload, bits, shift=0, digit=abi.DIGIT_HASH, stream=None):
+        import torch
+
+        dev = keys.device
+        n = keys.numel()
+        ok = torch.empty(max(n, 1), dtype=torch.int32, device=dev)
+        op = torch.empty(max(n, 1), dtype=torch.int32, device=dev)
+        off = torch.empty((1 << bits) + 1, dtype=torch.int64, device=dev)
+        self.check(self.lib.gbj_partition(self.handle, _ptr(keys), _ptr(payload), n, digit, shift,
+                                          bits, _ptr(ok), _ptr(op), _ptr(off), self._s(stream)))
+        return ok[:n], op[:n], off
+
+    # ----------------------------------------------------------- group-by
+    def groupby(self, keys, values, out_capacity, expected_groups=0, max_input_size=0,
+                hash_bits=0, strategy=0, stream=None):
+        import torch
+
+        dev = keys.device
+        cap = max(out_capacity, 1)
+        ok = torch.empty(cap, dtype=torch.int32, device=dev)
+        oc = torch.empty(cap, dtype=torch.int64, device=dev)
+        osum = torch.empty(cap, dtype=torch.int64, device=dev)
+        omin = torch.empty(cap, dtype=torch.int32, device=dev)
+        omax = torch.empty(cap, dtype=torch.int32, device=dev)
+        ng = torch.zeros(1, dtype=torch.int64, device=dev)
+        prm = abi.GroupbyParams(hash_bits, strategy, max_input_size, expected_groups)
+        self.check(self.lib.gbj_groupby(self.handle, _ptr(keys), _ptr(values), keys.numel(),
+                                        C.byref(prm), _ptr(ok), _ptr(oc), _ptr(osum), _ptr(omin),
+                                        _ptr(omax), out_capacity, _ptr(ng), self._s(stream)))
+        return ok, oc, osum, omin, omax, ng
+
+    # ------------------------------------------------------------ columns
+    def reduce(self, col, aggs, rows=None, out=None, stream=None):
+        import torch
+
+        n = rows.numel() if rows is not None else col.numel()
+        if out is None:
+            out = torch.empty(len(aggs), dtype=torch.int64, device=col.device)
+        arr = abi.aggs_array(aggs)
+        self.check(self.lib.gbj_reduce(self.handle, _ptr(col), _ptr(rows), n, arr, len(aggs),
+                                       _ptr(out), self._s(stream)))
+        return out
+
+    def gather(self, col, rows, stream=None):
+        import torch
+
+        out = torch.empty(max(rows.numel(), 1), dtype=torch.int32, device=col.device)
+        self.check(self.lib.gbj_gather(self.handle, _ptr(col), _ptr(rows), rows.numel(), _ptr(out),
+                                       self._s(stream)))
+        return out[: rows.numel()]
+
+    def select_range(self, col, lo, hi, stream=None):
+        import torch
+
+        n = col.numel()
+        rows = torch.empty(max(n, 1), dtype=torch.int32, device=col.device)
+        cnt = torch.zeros(1, dtype=torch.int64, device=col.device)
+        self.check(self.lib.gbj_select_range(self.handle, _ptr(col), n, lo, hi, _ptr(rows), _ptr(cnt),
+                                             self._s(stream)))
+        return rows, cnt
+
+
+# ------------------------------------------------------ host generators
+def _np_ptr(a):
+    return a.ctypes.data_as(C.c_void_p) if a is not None else None
+
+
+def gen_build_side(seed: int, n: int, payload=True, threads=0):
+    lib = abi.load()
+    k = np.empty(n, dtype=np.int32)
+    p = np.empty(n, dtype=np.int32) if payload else None
+    rc = lib.gbj_gen_build_side(seed, n, _np_ptr(k), _np_ptr(p), threads)
+    if rc:
+        raise abi.GbjError(rc, "gen_build_side")
+    return k, p
+
+
+def gen_probe_uniform(seed: int, n: int, n_build: int, payload=True, threads=0):
+    lib = abi.load()
+    k = np.empty(n, dtype=np.int32)
+    p = np.empty(n, dtype=np.int32) if payload else None
+    rc = lib.gbj_gen_probe_uniform(seed, n, n_build, _np_ptr(k), _np_ptr(p), threads)
+    if rc:
+        raise abi.GbjError(rc, "gen_probe_uniform")
+    return k, p
+
+
+def gen_probe_zipf(seed: int, n: int, n_build: int, theta: float, hit_rate=0.5, payload=False,
+                   threads=0):
+    lib = abi.load()
+    k = np.empty(n, dtype=np.int32)
+    p = np.empty(n, dtype=np.int32) if payload else None
+    rc = lib.gbj_gen_probe_zipf(seed, n, n_build, theta, hit_rate, _np_ptr(k), _np_ptr(p), threads)
+    if rc:
+        raise abi.GbjError(rc, "gen_probe_zipf")
+    return k, p
+
+
+def gen_groupby(seed: int, n: int, cardinality: int, theta: float = 0.0, threads=0):
+    lib = abi.load()
+    k = np.empty(n, dtype=np.int32)
+    v = np.empty(n, dtype=np.int32)
+    rc = lib.gbj_gen_groupby(seed, n, cardinality, theta, _np_ptr(k), _np_ptr(v), threads)
+    if rc:
+        raise abi.GbjError(rc, "gen_groupby")
+    return k, v

@@ -1,0 +1,175 @@
+"""Generates the golden fixtures under tests/golden/.
+
+1. reference_cases.json -- the integer columns of the reference's own test
+   inputs (tests/inputs/{sailors,reserves,boats}.csv,
+   tests/inputs/tpch/lineitem10.csv) and the expected outputs of the
+   reference tests that exercise joins, reduces and group-bys over them
+   (golden files under tests/olap/outputs/).  Read from the reference tree.
+2. rjstepwise_cases.json -- match counts of the reference's RJStepwise and
+   cluster counts of its partitionHT (core/platform/lib/util/radix/joins/
+   radix-join.cpp), compiled from source into oracle/_ref, on seeded
+   synthetic inputs, plus checksums of those inputs so a test can confirm
+   the generator reproduces them.
+
+Run from the repository root:  python tests/golden/make_golden.py
+(requires the reference tree at /root/reference or $PROTEUS_REF).
+"""
+from __future__ import annotations
+
+import csv
+import hashlib
+import json
+import os
+import sys
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+sys.path.insert(0, ROOT)
+REF = os.environ.get("PROTEUS_REF", "/root/reference")
+OUT = os.path.dirname(os.path.abspath(__file__))
+
+
+def read_csv(rel, delim, cols):
+    rows = []
+    with open(os.path.join(REF, rel)) as f:
+        for r in csv.reader(f, delimiter=delim):
+            if r:
+                rows.append(r)
+    return {name: [int(float(r[i])) for r in rows] for name, i in cols.items()}
+
+
+def read_text(rel):
+    with open(os.path.join(REF, rel)) as f:
+        return f.read().strip()
+
+
+def reference_cases():
+    sailors = read_csv("tests/inputs/sailors.csv", ";", {"sid": 0, "rating": 2})
+    reserves = read_csv("tests/inputs/reserves.csv", ";", {"sid": 0, "bid": 1})
+    boats = read_csv("tests/inputs/boats.csv", ";", {"bid": 0})
+    # l_quantity is an integral float column in this file; read as int
+    lineitem = read_csv("tests/inputs/tpch/lineitem10.csv", "|",
+                        {"l_orderkey": 0, "l_linenumber": 3, "l_quantity": 4})
+    left3 = read_text("tests/olap/outputs/tests-sailors/sailorsJoinLeft3.csv").split(",")
+    wayjoin = json.loads(read_text("tests/olap/outputs/tests-output/3wayJoin.json"))[0]
+    radix_cnt = int(read_text("tests/olap/outputs/tests-plan-parsing/reduce-join-log.json"))
+    nest = json.loads(read_text("tests/olap/outputs/tests-output/nestReserves.json"))
+    multinest = json.loads(read_text("tests/olap/outputs/tests-output/multinestReserves.json"))
+    bag = json.loads(read_text("tests/olap/outputs/tests-output/nestBagTPCH.json"))
+    cases = [
+        {
+            "name": "sailorsJoinLeft3",
+            "reference_test": "core/olap/tests/operator-tests/tests-join-sailors.cpp:127-165",
+            "golden": "tests/olap/outputs/tests-sailors/sailorsJoinLeft3.csv",
+            "plan": "sailors.join(reserves on sid, hash_bits 16, maxBuild 128)"
+                    ".join(boats on bid).reduce(MAX sid, SUM sid, SUM 1)",
+            "expected": {"max_sid": int(left3[0]), "sum_sid": int(left3[1]),
+                         "count": int(left3[2])},
+        },
+        {
+            "name": "3wayJoin",
+            "reference_test": "tests/olap/tests-output.cpp:240-281",
+            "golden": "tests/olap/outputs/tests-output/3wayJoin.json",
+            "plan": "reserves.join(build=sailors on sid, 4, 16).join(build=boats on bid)"
+                    ".reduce(MAX sid, SUM sid, SUM 1)",
+            "expected": {"max_sid": wayjoin["max_sid"], "sum_sid": wayjoin["sum_sid"],
+                         "count": wayjoin["cnt"]},
+        },
+        {
+            "name": "reduce-join",
+            "reference_test": "tests/olap/tests-plan-parsing.cpp:96-101",
+            "golden": "tests/olap/outputs/tests-plan-parsing/reduce-join-log.json",
+            "plan": "tests/inputs/plans/reduce-join.json: radix join sailors.sid = reserves.sid,"
+                    " reduce SUM 1",
+            "expected": {"count": radix_cnt},
+        },
+        {
+            "name": "nestReserves",
+            "reference_test": "tests/olap/tests-output.cpp:283-307",
+            "golden": "tests/olap/outputs/tests-output/nestReserves.json",
+            "plan": "reserves.groupby(sid; SUM 1, hash_bits 4, maxInputSize 16)",
+            "expected": {"counts": sorted(r["_groupCount"] for r in nest)},
+        },
+        {
+            "name": "multinestReserves",
+            "reference_test": "tests/olap/tests-output.cpp:309-335",
+            "golden": "tests/olap/outputs/tests-output/multinestReserves.json",
+            "plan": "reserves.groupby(sid; SUM 1, MAX bid, hash_bits 4, maxInputSize 16)",
+            "expected": {"count_max": sorted([r["_outCount"], r["_outMax"]] for r in multinest)},
+        },
+        {
+            "name": "nestBagTPCH",
+            "reference_test": "tests/olap/tests-output.cpp:208-238",
+            "golden": "tests/olap/outputs/tests-output/nestBagTPCH.json",
+            "plan": "lineitem.filter(l_orderkey < 4).groupby(l_linenumber; SUM 1, MAX l_quantity,"
+                    " hash_bits 4, maxInputSize 16)",
+            "expected": {"count_max": sorted([r["cnt"], int(r["max_qty"])] for r in bag)},
+        },
+    ]
+    return {
+        "about": "Integer columns of the reference's test inputs and the expected results of its "
+                 "join / reduce / group-by tests (outputs compared unordered, as the reference "
+                 "does).",
+        "tables": {"sailors": sailors, "reserves": reserves, "boats": boats,
+                   "lineitem10": lineitem},
+        "cases": cases,
+    }
+
+
+def checksum(a: np.ndarray) -> str:
+    return hashlib.sha256(np.ascontiguousarray(a, dtype=np.int32).tobytes()).hexdigest()[:16]
+
+
+def rjstepwise_cases():
+    from oracle import oracle as O
+    from proteus_gb300 import engine as E
+
+    O.build()
+    if not O.build_ref(REF):
+        raise SystemExit("reference tree not found; cannot build oracle/_ref")
+    cases = []
+    specs = [
+        ("plain", 11, 1 << 12, 1 << 16, None),
+        ("plain", 12, 1 << 16, 1 << 18, None),
+        ("zipf", 13, 1 << 14, 1 << 17, 0.0),
+        ("zipf", 14, 1 << 14, 1 << 17, 0.5),
+        ("zipf", 15, 1 << 14, 1 << 17, 1.0),
+        ("zipf", 16, 1 << 17, 1 << 19, 1.0),
+        ("zipf", 17, 3001, 50000, 1.0),
+    ]
+    for kind, seed, nr, ns, theta in specs:
+        rk, _ = E.gen_build_side(seed, nr, payload=False)
+        if kind == "plain":
+            sk, _ = E.gen_probe_uniform(seed, ns, nr, payload=False)
+        else:
+            sk, _ = E.gen_probe_zipf(seed, ns, nr, theta, 0.5)
+        m = O.ref_rj_stepwise(rk, sk)
+        counts, _, _ = O.ref_partition_ht(rk)
+        cases.append({
+            "kind": kind, "seed": seed, "n_build": nr, "n_probe": ns, "theta": theta,
+            "build_sha": checksum(rk), "probe_sha": checksum(sk),
+            "rjstepwise_matches": m,
+            "partition_ht_counts_sha": hashlib.sha256(counts.astype(np.int32).tobytes())
+            .hexdigest()[:16],
+            "partition_ht_nonempty": int((counts > 0).sum()),
+        })
+    return {
+        "about": "RJStepwise match counts and partitionHT cluster counts of the reference's "
+                 "core/platform/lib/util/radix/joins/radix-join.cpp, compiled from source by "
+                 "oracle/Makefile (target ref), on inputs from the seeded generators "
+                 "gbj_gen_build_side / gbj_gen_probe_uniform / gbj_gen_probe_zipf.",
+        "cases": cases,
+    }
+
+
+def main():
+    with open(os.path.join(OUT, "reference_cases.json"), "w") as f:
+        json.dump(reference_cases(), f, indent=1)
+    with open(os.path.join(OUT, "rjstepwise_cases.json"), "w") as f:
+        json.dump(rjstepwise_cases(), f, indent=1)
+    print("wrote", OUT)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,131 @@
+"""Radix partitioning and the partitioned join on the GPU vs the oracle."""
+import numpy as np
+import pytest
+
+from gpu_util import CONFIG1_AGGS, CONFIG2_AGGS, cpu_threads, dev, host
+from proteus_gb300 import abi, engine
+
+pytestmark = pytest.mark.gpu
+
+
+def canonical_partitions(keys, payload, offsets):
+    """Each partition's tuples sorted, so unordered partitions compare."""
+    out = []
+    for p in range(len(offsets) - 1):
+        a, b = int(offsets[p]), int(offsets[p + 1])
+        kk, pp = keys[a:b], payload[a:b]
+        o = np.lexsort((pp, kk))
+        out.append((kk[o], pp[o]))
+    return out
+
+
+@pytest.mark.parametrize("n,bits,digit,shift,with_payload", [
+    (1 << 16, 1, abi.DIGIT_HASH, 0, True),
+    (100003, 7, abi.DIGIT_KEY, 0, False),
+    (1 << 18, 13, abi.DIGIT_HASH, 0, True),
+    (1 << 18, 15, abi.DIGIT_HASH, 0, False),
+    (50000, 7, abi.DIGIT_KEY, 7, True),
+    (3, 4, abi.DIGIT_HASH, 0, True),
+])
+def test_partition_matches_radix_cluster(ctx, oracle, n, bits, digit, shift, with_payload):
+    rng = np.random.default_rng(n + bits)
+    keys = rng.integers(np.iinfo(np.int32).min, np.iinfo(np.int32).max, n, dtype=np.int64)
+    keys = keys.astype(np.int32)
+    pay = rng.integers(-10**6, 10**6, n).astype(np.int32) if with_payload else None
+    ok, op, off = ctx.partition(dev(keys), dev(pay) if pay is not None else None, bits,
+                                shift=shift, digit=digit)
+    ctx.sync()
+    ek, ep, eoff = oracle.radix_cluster(keys, pay, shift, bits, digit == abi.DIGIT_HASH)
+    got_off = host(off).astype(np.uint64)
+    assert (got_off == eoff).all()
+    a = canonical_partitions(host(ok), host(op), got_off)
+    b = canonical_partitions(ek, ep, eoff)
+    for (k1, p1), (k2, p2) in zip(a, b):
+        assert (k1 == k2).all() and (p1 == p2).all()
+
+
+def test_partition_empty_and_invalid(ctx):
+    import torch
+
+    e = torch.zeros(0, dtype=torch.int32, device="cuda")
+    ok, op, off = ctx.partition(e, e, 5)
+    ctx.sync()
+    assert (host(off) == 0).all()
+    with pytest.raises(abi.GbjError):
+        ctx.partition(dev(np.arange(10, dtype=np.int32)), None, 16)
+
+
+@pytest.mark.parametrize("theta", [0.0, 0.5, 1.0])
+@pytest.mark.parametrize("nr,ns", [(1 << 12, 1 << 16), (1 << 18, 1 << 21)])
+def test_radix_join_zipf(ctx, oracle, theta, nr, ns):
+    rk, _ = engine.gen_build_side(31, nr, payload=False)
+    sk, _ = engine.gen_probe_zipf(31, ns, nr, theta, 0.5)
+    out = ctx.radix_join_agg(dev(rk), None, dev(sk), None, CONFIG2_AGGS)
+    ctx.sync()
+    exp = oracle.radix_join_agg(rk, None, sk, None, CONFIG2_AGGS, threads=cpu_threads())
+    assert host(out).tolist() == exp
+    assert exp[0] == oracle.rj_stepwise(rk, sk)
+
+
+def test_radix_join_payload_aggregates(ctx, oracle):
+    rk, rp = engine.gen_build_side(7, 1 << 16)
+    sk, sp = engine.gen_probe_uniform(7, 1 << 20, 1 << 16)
+    aggs = CONFIG1_AGGS + [(abi.AGG_MIN, abi.VAL_BUILD), (abi.AGG_MAX, abi.VAL_PROBE),
+                           (abi.AGG_SUM, abi.VAL_BUILD_KEY)]
+    out = ctx.radix_join_agg(dev(rk), dev(rp), dev(sk), dev(sp), aggs)
+    ctx.sync()
+    assert host(out).tolist() == oracle.join_agg(rk, rp, sk, sp, aggs, threads=cpu_threads())
+
+
+def test_radix_join_heavy_duplicates(ctx, oracle):
+    """A build partition larger than the on-chip table is split into chunks."""
+    rng = np.random.default_rng(3)
+    rk = np.concatenate([np.full(30000, 77, dtype=np.int32),
+                         rng.integers(0, 1 << 20, 100000).astype(np.int32)])
+    sk = np.concatenate([np.full(500, 77, dtype=np.int32),
+                         rng.integers(0, 1 << 20, 200000).astype(np.int32)])
+    out = ctx.radix_join_agg(dev(rk), None, dev(sk), None, CONFIG2_AGGS, bits=4)
+    ctx.sync()
+    assert host(out).tolist() == oracle.join_agg(rk, None, sk, None, CONFIG2_AGGS)
+
+
+@pytest.mark.parametrize("bits", [1, 6, 13, 15])
+def test_radix_join_explicit_bits(ctx, oracle, bits):
+    rk, _ = engine.gen_build_side(4, 50000, payload=False)
+    sk, _ = engine.gen_probe_zipf(4, 300000, 50000, 1.0, 0.7)
+    out = ctx.radix_join_agg(dev(rk), None, dev(sk), None, CONFIG2_AGGS, bits=bits)
+    ctx.sync()
+    assert host(out).tolist() == oracle.join_agg(rk, None, sk, None, CONFIG2_AGGS)
+
+
+def test_radix_join_unsupported_mix(ctx):
+    rk, rp = engine.gen_build_side(1, 1000)
+    with pytest.raises(abi.GbjError) as e:
+        ctx.radix_join_agg(dev(rk), dev(rp), dev(rk), dev(rp),
+                           [(abi.AGG_SUM, abi.VAL_BUILD), (abi.AGG_SUM, abi.VAL_BUILD_ROWID)])
+    assert e.value.code == abi.ERR_UNSUPPORTED
+
+
+def test_radix_join_empty(ctx, oracle):
+    rk, _ = engine.gen_build_side(1, 1000, payload=False)
+    e = np.zeros(0, dtype=np.int32)
+    out = ctx.radix_join_agg(dev(e), None, dev(rk), None, CONFIG2_AGGS)
+    ctx.sync()
+    assert host(out).tolist() == [0, 0]
+
+
+@pytest.mark.parametrize("theta", [0.0, 0.5, 1.0])
+def test_radix_join_full_config(ctx, oracle, theta):
+    """R = 2^27 unique keys, S = 2^29 (50% hits, Zipf theta): full size."""
+    nr, ns = 1 << 27, 1 << 29
+    rk, _ = engine.gen_build_side(1000 + int(theta * 10), nr, payload=False)
+    sk, _ = engine.gen_probe_zipf(1000 + int(theta * 10), ns, nr, theta, 0.5)
+    drk, dsk = dev(rk), dev(sk)
+    out = ctx.radix_join_agg(drk, None, dsk, None, CONFIG2_AGGS)
+    ctx.sync()
+    got = host(out).tolist()
+    del drk, dsk
+    exp = oracle.radix_join_agg(rk, None, sk, None, CONFIG2_AGGS, threads=cpu_threads())
+    assert got == exp
+    # hits are ~50% of the probe side and every hit matches exactly once
+    assert abs(got[0] / ns - 0.5) < 0.001

@@ -1,0 +1,134 @@
+"""The oracle pinned against the reference: its golden outputs and its own
+RJStepwise / partitionHT compiled from source (committed counts)."""
+import hashlib
+
+import numpy as np
+import pytest
+
+from proteus_gb300 import abi, engine
+
+COUNT1 = (abi.AGG_COUNT, abi.VAL_ONE)
+
+
+def _col(golden, table, col):
+    return np.array(golden["reference"]["tables"][table][col], dtype=np.int32)
+
+
+def _case(golden, name):
+    return next(c for c in golden["reference"]["cases"] if c["name"] == name)
+
+
+def three_way_join_oracle(O, sailors_sid, reserves_sid, reserves_bid, boats_bid):
+    """probe sailors x build reserves on sid, then x build boats on bid."""
+    b1, p1 = O.join_pairs(reserves_sid, sailors_sid, hash_bits=16)
+    bid = reserves_bid[b1]
+    sid = sailors_sid[p1]
+    b2, p2 = O.join_pairs(boats_bid, bid, hash_bits=16)
+    return O.reduce(sid, [(abi.AGG_MAX, abi.VAL_PROBE), (abi.AGG_SUM, abi.VAL_PROBE), COUNT1],
+                    rows=p2)
+
+
+def test_sailors_join_left3(oracle, golden):
+    exp = _case(golden, "sailorsJoinLeft3")["expected"]
+    r = three_way_join_oracle(oracle, _col(golden, "sailors", "sid"),
+                              _col(golden, "reserves", "sid"), _col(golden, "reserves", "bid"),
+                              _col(golden, "boats", "bid"))
+    assert r == [exp["max_sid"], exp["sum_sid"], exp["count"]]
+
+
+def test_3way_join_other_build_side(oracle, golden):
+    # tests-output.cpp: reserves probes, sailors builds
+    exp = _case(golden, "3wayJoin")["expected"]
+    s_sid, r_sid = _col(golden, "sailors", "sid"), _col(golden, "reserves", "sid")
+    r_bid, b_bid = _col(golden, "reserves", "bid"), _col(golden, "boats", "bid")
+    b1, p1 = oracle.join_pairs(s_sid, r_sid, hash_bits=4)
+    bid, sid = r_bid[p1], s_sid[b1]
+    b2, p2 = oracle.join_pairs(b_bid, bid, hash_bits=4)
+    got = oracle.reduce(sid, [(abi.AGG_MAX, abi.VAL_PROBE), (abi.AGG_SUM, abi.VAL_PROBE), COUNT1],
+                        rows=p2)
+    assert got == [exp["max_sid"], exp["sum_sid"], exp["count"]]
+
+
+def test_reduce_join_radix(oracle, golden):
+    exp = _case(golden, "reduce-join")["expected"]
+    s_sid, r_sid = _col(golden, "sailors", "sid"), _col(golden, "reserves", "sid")
+    assert oracle.rj_stepwise(s_sid, r_sid) == exp["count"]
+    assert oracle.radix_join_agg(s_sid, None, r_sid, None, [COUNT1], bits=2)[0] == exp["count"]
+
+
+def test_groupby_reserves(oracle, golden):
+    k, c, s, mn, mx = oracle.groupby(_col(golden, "reserves", "sid"),
+                                     _col(golden, "reserves", "bid"), hash_bits=4)
+    assert sorted(c.tolist()) == _case(golden, "nestReserves")["expected"]["counts"]
+    assert sorted([int(a), int(b)] for a, b in zip(c, mx)) == \
+        _case(golden, "multinestReserves")["expected"]["count_max"]
+
+
+def test_groupby_lineitem_filtered(oracle, golden):
+    ok = _col(golden, "lineitem10", "l_orderkey")
+    sel = np.nonzero(ok < 4)[0]
+    k, c, s, mn, mx = oracle.groupby(_col(golden, "lineitem10", "l_linenumber")[sel],
+                                     _col(golden, "lineitem10", "l_quantity")[sel], hash_bits=4)
+    assert sorted([int(a), int(b)] for a, b in zip(c, mx)) == \
+        _case(golden, "nestBagTPCH")["expected"]["count_max"]
+
+
+def _sha(a):
+    return hashlib.sha256(np.ascontiguousarray(a, dtype=np.int32).tobytes()).hexdigest()[:16]
+
+
+def _regen(case):
+    rk, _ = engine.gen_build_side(case["seed"], case["n_build"], payload=False)
+    if case["kind"] == "plain":
+        sk, _ = engine.gen_probe_uniform(case["seed"], case["n_probe"], case["n_build"],
+                                         payload=False)
+    else:
+        sk, _ = engine.gen_probe_zipf(case["seed"], case["n_probe"], case["n_build"],
+                                      case["theta"], 0.5)
+    return rk, sk
+
+
+@pytest.mark.parametrize("i", range(7))
+def test_rjstepwise_golden(lib, oracle, golden, i):
+    case = golden["rjstepwise"]["cases"][i]
+    rk, sk = _regen(case)
+    # the generator reproduces the inputs the reference was run on
+    assert _sha(rk) == case["build_sha"] and _sha(sk) == case["probe_sha"]
+    m = case["rjstepwise_matches"]
+    assert oracle.rj_stepwise(rk, sk) == m
+    assert oracle.join_agg(rk, None, sk, None, [COUNT1])[0] == m
+    assert oracle.radix_join_agg(rk, None, sk, None, [COUNT1], threads=4)[0] == m
+    counts = oracle.partition_ht_counts(oracle.radix_cluster(rk, None, 0, 14, 0)[0])
+    assert hashlib.sha256(counts.astype(np.int32).tobytes()).hexdigest()[:16] == \
+        case["partition_ht_counts_sha"]
+
+
+def test_radix_cluster_equals_reference_order(oracle):
+    """Two stable passes (7 + 7 bits) reproduce partitionHT's order exactly."""
+    if oracle.ref_lib() is None and not oracle.build_ref():
+        pytest.skip("reference tree not present (oracle/_ref cannot be built here)")
+    rk, _ = engine.gen_build_side(5, 50000, payload=False)
+    counts, keys, rows = oracle.ref_partition_ht(rk)
+    k1, p1, _ = oracle.radix_cluster(rk, None, 0, 7, 0)
+    k2, p2, _ = oracle.radix_cluster(k1, p1, 7, 7, 0)
+    assert (k2 == keys).all() and (p2 == rows).all()
+    assert (oracle.partition_ht_counts(k2) == counts).all()
+
+
+def test_planted_mistake_is_caught(oracle, golden):
+    """A wrong oracle answer must fail the golden comparison."""
+    case = golden["rjstepwise"]["cases"][0]
+    rk, sk = _regen(case)
+    sk = sk.copy()
+    sk[0] = np.int32(-7)  # a probe key that cannot match: one match fewer
+    assert oracle.rj_stepwise(rk, sk) == case["rjstepwise_matches"] - 1
+
+
+def test_groupby_threads_agree(oracle):
+    k, v = engine.gen_groupby(3, 200000, 5000, 1.0)
+    a = oracle.groupby(k, v, threads=1)
+    b = oracle.groupby(k, v, threads=8)
+    for x, y in zip(a, b):
+        assert (x == y).all()
+    assert a[1].sum() == len(k)
+    assert a[2].sum() == int(v.astype(np.int64).sum())
