@@ -318,9 +318,9 @@ int gbj_join_probe_agg(gbj_ctx *ctx, const gbj_table *t, const int32_t *d_keys,
   AggSpec spec = make_spec(aggs, n_aggs);
   for (int j = 0; j < n_aggs; ++j) {
     int o = spec.operand[j];
-    if ((o == GBJ_VAL_BUILD || o == GBJ_VAL_PRODUCT) && !t->payload)
+    if ((o == GBJ_VAL_BUILD || o == GBJ_VAL_PRODUCT) && !t->payload && t->n)
       return set_error(ctx, GBJ_ERR_INVALID, "aggregate reads the build payload, table has none");
-    if ((o == GBJ_VAL_PROBE || o == GBJ_VAL_PRODUCT) && !d_payload)
+    if ((o == GBJ_VAL_PROBE || o == GBJ_VAL_PRODUCT) && !d_payload && n)
       return set_error(ctx, GBJ_ERR_INVALID, "aggregate reads the probe payload, none given");
   }
   cudaStream_t s = pick_stream(ctx, stream);

@@ -394,7 +394,7 @@ int gbj_radix_join_agg(gbj_ctx *ctx, const int32_t *d_build_keys,
   if ((b_row && b_pay) || (p_row && p_pay))
     return set_error(ctx, GBJ_ERR_UNSUPPORTED,
                      "radix_join: one side cannot carry both its payload and its row id");
-  if ((b_pay && !d_build_payload) || (p_pay && !d_probe_payload))
+  if ((b_pay && !d_build_payload && n_build) || (p_pay && !d_probe_payload && n_probe))
     return set_error(ctx, GBJ_ERR_INVALID, "radix_join: aggregate reads a missing payload");
   cudaStream_t s = pick_stream(ctx, stream);
   prof_mark(ctx, s);

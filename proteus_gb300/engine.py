@@ -19,10 +19,17 @@ def _ptr(t) -> int | None:
     return t.data_ptr()
 
 
+CUDA_STREAM_LEGACY = 1  # cudaStreamLegacy
+
+
 def _cur_stream():
+    """torch's current stream as a cudaStream_t for the ABI.  torch reports
+    its default stream as handle 0, which the ABI reads as "the context's own
+    stream"; pass cudaStreamLegacy instead so library kernels stay ordered
+    with torch's copies on that stream."""
     import torch
 
-    return torch.cuda.current_stream().cuda_stream
+    return torch.cuda.current_stream().cuda_stream or CUDA_STREAM_LEGACY
 
 
 class Table:

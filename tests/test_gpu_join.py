@@ -81,8 +81,8 @@ def test_unaligned_inputs(ctx, oracle):
     sk, sp = engine.gen_probe_uniform(8, 40001, 5000)
     import torch
 
-    dsk = torch.cat([torch.zeros(1, dtype=torch.int32), dev(sk)])[1:]
-    dsp = torch.cat([torch.zeros(1, dtype=torch.int32), dev(sp)])[1:]
+    dsk = torch.cat([torch.zeros(1, dtype=torch.int32, device="cuda"), dev(sk)])[1:]
+    dsp = torch.cat([torch.zeros(1, dtype=torch.int32, device="cuda"), dev(sp)])[1:]
     assert dsk.data_ptr() % 16 != 0
     t = ctx.join_build(dev(rk), dev(rp))
     out = ctx.join_probe_agg(t, dsk, dsp, ALL_AGGS)

@@ -129,3 +129,28 @@ def test_radix_join_full_config(ctx, oracle, theta):
     assert got == exp
     # hits are ~50% of the probe side and every hit matches exactly once
     assert abs(got[0] / ns - 0.5) < 0.001
+
+
+def test_stream_ordering_with_torch(ctx, oracle):
+    """Library kernels run on torch's current stream: async host->device
+    copies before the call and the read-back after it need no library sync."""
+    import torch
+
+    rk, _ = engine.gen_build_side(12, 1 << 20, payload=False)
+    sk, _ = engine.gen_probe_zipf(12, 1 << 23, 1 << 20, 0.5, 0.5)
+    h_r, h_s = torch.from_numpy(rk).pin_memory(), torch.from_numpy(sk).pin_memory()
+    d_r = torch.empty_like(h_r, device="cuda")
+    d_s = torch.empty_like(h_s, device="cuda")
+    exp = oracle.radix_join_agg(rk, None, sk, None, CONFIG2_AGGS, threads=cpu_threads())
+    for _ in range(3):
+        d_r.fill_(0)
+        d_s.fill_(0)
+        d_r.copy_(h_r, non_blocking=True)
+        d_s.copy_(h_s, non_blocking=True)
+        out = ctx.radix_join_agg(d_r, None, d_s, None, CONFIG2_AGGS)
+        assert out.cpu().tolist() == exp
+    with torch.cuda.stream(torch.cuda.Stream()):
+        d_s.copy_(h_s, non_blocking=True)
+        out = ctx.radix_join_agg(d_r, None, d_s, None, CONFIG2_AGGS)
+        got = out.cpu().tolist()
+    assert got == exp
