@@ -243,6 +243,40 @@ int gbj_select_range(gbj_ctx *ctx, const int32_t *d_col, uint64_t n,
                      int32_t lo, int32_t hi, int32_t *d_rows_out,
                      uint64_t *d_count, void *stream);
 
+/* --------------------------------------- allocation-free join + aggregate */
+/* This entry point has no counterpart in the reference.  It is for callers
+ * that may not allocate device memory at the moment they call: a host engine
+ * whose buffer manager has already reserved the device memory it is allowed
+ * to use (the reference's buffer manager pre-reserves its GPU block pools at
+ * start-up), a code path with a fixed memory budget checked at admission
+ * time, or a latency-critical path where cudaMalloc's implicit device
+ * synchronisation cannot be paid.  It needs no gbj_ctx and calls no
+ * allocating routine (no cudaMalloc, cudaFree or library allocator).
+ *
+ * It builds the same table as gbj_join_build and probes it as
+ * gbj_join_probe_agg does, with the same results, but the table lives in one
+ * fixed array inside the library's device code: 16 MiB, enough for build
+ * sides of up to GBJ_NOALLOC_MAX_BUILD rows.  Every GPU that loads the
+ * library holds that array until the process exits.  A larger build side is
+ * rejected with GBJ_ERR_CAPACITY and a message.
+ *
+ * Runs on `stream` (NULL = the legacy default stream) of the current device.
+ * The first call on a device looks up the array's device address for that
+ * device (cudaGetSymbolAddress); make that first call before any stream
+ * capture.  All calls share the one array and it keeps the previous call's
+ * contents: each call clears the part it uses first, and calls whose work
+ * overlaps on the GPU (other streams, other host threads) race on the table,
+ * so the caller must order them.  On failure the message is available from
+ * gbj_last_error(NULL) on the calling thread. */
+#define GBJ_NOALLOC_MAX_BUILD (1u << 20)
+
+int gbj_join_agg_noalloc(const int32_t *d_build_keys,
+                         const int32_t *d_build_payload, uint64_t n_build,
+                         const int32_t *d_probe_keys,
+                         const int32_t *d_probe_payload, uint64_t n_probe,
+                         const gbj_agg *aggs, int32_t n_aggs, int64_t *d_out,
+                         void *stream);
+
 /* ------------------------------------------ seeded synthetic input (host) */
 /* Deterministic, thread-parallel generators for the workload shapes; pure
  * functions of (seed, row), identical on every host.  threads <= 0 uses all

@@ -21,6 +21,7 @@ AGG_COUNT, AGG_SUM, AGG_MIN, AGG_MAX = range(4)
 (VAL_ONE, VAL_BUILD, VAL_PROBE, VAL_PRODUCT, VAL_BUILD_ROWID, VAL_PROBE_ROWID,
  VAL_ROWID_XOR, VAL_BUILD_KEY) = range(8)
 DIGIT_KEY, DIGIT_HASH = 0, 1
+NOALLOC_MAX_BUILD = 1 << 20
 MAX_AGGS = 8
 
 
@@ -68,6 +69,7 @@ SIGNATURES = {
     "gbj_reduce": (C.c_int, [vp, vp, vp, u64, P(Agg), i32, vp, vp]),
     "gbj_gather": (C.c_int, [vp, vp, vp, u64, vp, vp]),
     "gbj_select_range": (C.c_int, [vp, vp, u64, i32, i32, vp, vp, vp]),
+    "gbj_join_agg_noalloc": (C.c_int, [vp, vp, u64, vp, vp, u64, P(Agg), i32, vp, vp]),
     "gbj_gen_build_side": (C.c_int, [u64, u64, vp, vp, C.c_int]),
     "gbj_gen_probe_uniform": (C.c_int, [u64, u64, u64, vp, vp, C.c_int]),
     "gbj_gen_probe_zipf": (C.c_int, [u64, u64, u64, dbl, dbl, vp, vp, C.c_int]),

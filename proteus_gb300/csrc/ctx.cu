@@ -282,7 +282,7 @@ int gbj_ctx_destroy(gbj_ctx *ctx) {
 }
 
 const char *gbj_last_error(gbj_ctx *ctx) {
-  return ctx ? ctx->last_error.c_str() : "null context";
+  return ctx ? ctx->last_error.c_str() : noalloc_error_text_impl();
 }
 
 int gbj_ctx_device_info(gbj_ctx *ctx, int *sm_count, uint64_t *l2_bytes,

@@ -120,6 +120,9 @@ inline int log2_ceil(uint64_t v) {
   return b;
 }
 
+// Text of the last failure of gbj_join_agg_noalloc on the calling thread.
+const char *noalloc_error_text_impl();
+
 // Counts a kernel launch, records its timing event when profiling is on,
 // and turns a launch error into a status.
 int after_launch(gbj_ctx *ctx, const char *name, cudaStream_t s);

@@ -238,15 +238,52 @@ __global__ void k_copy_total(const uint64_t *off, uint64_t ntiles, uint64_t *dst
   *dst = off[ntiles];
 }
 
-int grid_for(gbj_ctx *ctx, uint64_t work, int threads, int per_sm = 4) {
+int grid_for_sms(int sm_count, uint64_t work, int threads, int per_sm = 4) {
   uint64_t blocks = (work + threads - 1) / threads;
-  uint64_t cap = (uint64_t)ctx->sm_count * per_sm;
+  uint64_t cap = (uint64_t)sm_count * per_sm;
   if (blocks > cap) blocks = cap;
   if (blocks == 0) blocks = 1;
   return (int)blocks;
 }
 
+int grid_for(gbj_ctx *ctx, uint64_t work, int threads, int per_sm = 4) {
+  return grid_for_sms(ctx->sm_count, work, threads, per_sm);
+}
+
+// ------------------------------------------------ allocation-free variant
+// Hash table of gbj_join_agg_noalloc: a fixed array in the module's device
+// memory, so that entry point never allocates.  Slots for build sides of up
+// to GBJ_NOALLOC_MAX_BUILD rows at load factor 1/2, then 32 words of table
+// metadata (duplicate flag) and status.
+constexpr uint64_t kNoAllocSlots = 2ull * GBJ_NOALLOC_MAX_BUILD;
+static __device__ __align__(256) uint64_t g_noalloc_scratch[kNoAllocSlots + 32];
+
+__global__ void k_noalloc_init_out(gbj::AggSpec s, int64_t *out) {
+  const int j = threadIdx.x;
+  if (j < s.n) out[j] = gbjd::agg_identity(s.op[j]);
+}
+
+// Per-device set-up of the allocation-free entry point: the device address
+// of g_noalloc_scratch (host code cannot use the symbol itself) and the SM
+// count, looked up once per device with that device current.
+struct NoAllocDevice {
+  uint64_t *scratch = nullptr;
+  int sm_count = 0;
+};
+std::mutex g_noalloc_mu;
+std::unordered_map<int, NoAllocDevice> g_noalloc_devices;
+thread_local std::string g_noalloc_error;
+
+int noalloc_fail(int code, const char *msg) {
+  g_noalloc_error = msg;
+  return code;
+}
+
 }  // namespace
+
+namespace gbj {
+const char *noalloc_error_text_impl() { return g_noalloc_error.c_str(); }
+}  // namespace gbj
 
 extern "C" {
 
@@ -407,6 +444,90 @@ int gbj_select_range(gbj_ctx *ctx, const int32_t *d_col, uint64_t n, int32_t lo,
   GBJ_TRY(after_launch(ctx, "k_select_write", s));
   k_copy_total<<<1, 1, 0, s>>>(cnt, ntiles, d_count);
   return after_launch(ctx, "k_copy_total", s);
+}
+
+int gbj_join_agg_noalloc(const int32_t *d_build_keys, const int32_t *d_build_payload,
+                         uint64_t n_build, const int32_t *d_probe_keys,
+                         const int32_t *d_probe_payload, uint64_t n_probe, const gbj_agg *aggs,
+                         int32_t n_aggs, int64_t *d_out, void *stream) {
+  g_noalloc_error.clear();
+  if (!d_out || !aggs || n_aggs < 1 || n_aggs > GBJ_MAX_AGGS)
+    return noalloc_fail(GBJ_ERR_INVALID, "join_agg_noalloc: null output or bad aggregate count");
+  if ((n_build && !d_build_keys) || (n_probe && !d_probe_keys))
+    return noalloc_fail(GBJ_ERR_INVALID, "join_agg_noalloc: null key column");
+  if (n_build > GBJ_NOALLOC_MAX_BUILD)
+    return noalloc_fail(GBJ_ERR_CAPACITY,
+                        "join_agg_noalloc: build side larger than GBJ_NOALLOC_MAX_BUILD "
+                        "(1048576 rows); use gbj_join_build / gbj_join_probe_agg instead");
+  if (n_probe >= (1ULL << 32))
+    return noalloc_fail(GBJ_ERR_INVALID, "join_agg_noalloc: probe side must have < 2^32 rows");
+  for (int j = 0; j < n_aggs; ++j) {
+    if (aggs[j].op < GBJ_AGG_COUNT || aggs[j].op > GBJ_AGG_MAX || aggs[j].operand < GBJ_VAL_ONE ||
+        aggs[j].operand > GBJ_VAL_BUILD_KEY)
+      return noalloc_fail(GBJ_ERR_INVALID, "join_agg_noalloc: bad aggregate");
+    const int o = aggs[j].operand;
+    if ((o == GBJ_VAL_BUILD || o == GBJ_VAL_PRODUCT) && !d_build_payload && n_build)
+      return noalloc_fail(GBJ_ERR_INVALID, "join_agg_noalloc: aggregate reads a null build payload");
+    if ((o == GBJ_VAL_PROBE || o == GBJ_VAL_PRODUCT) && !d_probe_payload && n_probe)
+      return noalloc_fail(GBJ_ERR_INVALID, "join_agg_noalloc: aggregate reads a null probe payload");
+  }
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) {
+    (void)cudaGetLastError();
+    return noalloc_fail(GBJ_ERR_CUDA, "join_agg_noalloc: no current CUDA device");
+  }
+  NoAllocDevice d;
+  {
+    std::lock_guard<std::mutex> g(g_noalloc_mu);
+    auto it = g_noalloc_devices.find(dev);
+    if (it == g_noalloc_devices.end()) {
+      // first call on this device: resolve the array's device address
+      void *ptr = nullptr;
+      cudaError_t e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
+      if (e != cudaSuccess || !ptr) {
+        (void)cudaGetLastError();
+        return noalloc_fail(GBJ_ERR_CUDA, "join_agg_noalloc: cudaGetSymbolAddress failed");
+      }
+      NoAllocDevice nd;
+      nd.scratch = static_cast<uint64_t *>(ptr);
+      if (cudaDeviceGetAttribute(&nd.sm_count, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) {
+        (void)cudaGetLastError();
+        return noalloc_fail(GBJ_ERR_CUDA, "join_agg_noalloc: device query failed");
+      }
+      it = g_noalloc_devices.emplace(dev, nd).first;
+    }
+    d = it->second;
+  }
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  AggSpec spec = make_spec(aggs, n_aggs);
+  uint64_t slots = next_pow2(2 * (n_build ? n_build : 1));
+  if (slots < 64) slots = 64;
+  uint64_t *table = d.scratch;
+  uint32_t *meta = reinterpret_cast<uint32_t *>(d.scratch + kNoAllocSlots);
+  uint32_t *status = meta + 1;
+  // the array keeps the previous call's table: clear the part this call uses
+  if (cudaMemsetAsync(table, 0, slots * sizeof(uint64_t), s) != cudaSuccess ||
+      cudaMemsetAsync(meta, 0, 2 * sizeof(uint32_t), s) != cudaSuccess) {
+    (void)cudaGetLastError();
+    return noalloc_fail(GBJ_ERR_CUDA, "join_agg_noalloc: cudaMemsetAsync failed");
+  }
+  k_noalloc_init_out<<<1, 32, 0, s>>>(spec, d_out);
+  if (n_build)
+    k_join_build<<<grid_for_sms(d.sm_count, n_build, kThreads), kThreads, 0, s>>>(
+        d_build_keys, n_build, table, slots - 1, meta, status);
+  if (n_probe) {
+    const bool vec = ((uintptr_t)d_probe_keys % 16 == 0) &&
+                     (!d_probe_payload || (uintptr_t)d_probe_payload % 16 == 0);
+    if (vec)
+      k_join_probe_agg<true><<<grid_for_sms(d.sm_count, (n_probe + 3) / 4, kThreads), kThreads, 0, s>>>(
+          d_probe_keys, d_probe_payload, n_probe, table, slots - 1, d_build_payload, meta, spec, d_out);
+    else
+      k_join_probe_agg<false><<<grid_for_sms(d.sm_count, n_probe, kThreads), kThreads, 0, s>>>(
+          d_probe_keys, d_probe_payload, n_probe, table, slots - 1, d_build_payload, meta, spec, d_out);
+  }
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return noalloc_fail(GBJ_ERR_CUDA, cudaGetErrorString(e));
+  return GBJ_OK;
 }
 
 }  // extern "C"
