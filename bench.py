@@ -127,13 +127,12 @@ def hbm_peak():
 
 def kernel_bytes(name, n_r, n_s):
     """Algorithmic HBM bytes of one join's launches of `name` (all launches
-    of that kernel in one join together), per the kernel's definition:
-    count = key read; scatter = key read + (key, rowid) pair write;
-    join = both sides' pairs read once."""
+    of that kernel in one join together), per the kernel's definition."""
     tuples = n_r + n_s
-    return {"k_part_count": 4 * tuples,
-            "k_part_scatter": 12 * tuples,
-            "k_radix_join": 8 * tuples}.get(name)
+    return {"k_pid_hist": 4 * tuples,          # key read
+            "k_tile_pass": 28 * tuples,        # pass 1: key read + pair write (12 B),
+                                               # pass 2: pair read + pair write (16 B)
+            "k_radix_join": 8 * tuples}.get(name)  # partitioned pairs read once
 
 
 def traffic_from_profiles(kernel):

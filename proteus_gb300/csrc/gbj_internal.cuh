@@ -149,7 +149,7 @@ int init_agg_out(gbj_ctx *ctx, const AggSpec &spec, int64_t *d_out,
 namespace gbjd {
 
 // murmur3 fmix32 (32-bit), the placement hash of every table and partition.
-__device__ __forceinline__ uint32_t fmix32(uint32_t h) {
+__host__ __device__ __forceinline__ uint32_t fmix32(uint32_t h) {
   h ^= h >> 16;
   h *= 0x85ebca6bu;
   h ^= h >> 13;

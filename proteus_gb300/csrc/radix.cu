@@ -7,22 +7,30 @@
 // per-partition shared-memory build/probe loop of
 // GpuPartitionedHashJoinChained (gpu-partitioned-hash-join-chained.cpp:
 // 612-1586), and for the CPU RJStepwise / partitionHT path
-// (core/platform/lib/util/radix/joins/radix-join.cpp:253-375).
+// (core/platform/lib/util/radix/joins/radix-join.cpp:253-375).  Like the
+// reference's GPU partitioner it uses two passes for wide fan-outs (there
+// 7 + 6 bits); each pass here is a tile sort rather than bucket chains.
 //
 // GB300 layout:
-//  * one partitioning pass of up to 15 bits of fmix32(key): a count kernel
-//    builds one shared-memory histogram per CTA segment, a scan turns the
-//    [partition][cta] counts into write cursors, and a scatter kernel
-//    re-reads its segment and writes (key, value) pairs with shared-memory
-//    cursors -- no global atomics, one read of the input per pass, 8 B per
-//    tuple written;
-//  * radix bits chosen so an average build partition holds about half of
-//    an on-chip table (kRMax tuples), so build partitions never leave
-//    shared memory;
-//  * the join kernel is persistent: CTAs pull work items (partition,
-//    build chunk, probe chunk) from an atomic counter, so one skewed probe
-//    partition (Zipf keys) is spread over many SMs.
+//  * a histogram kernel counts the final partition ids (<= 2^15) once;
+//  * each pass (<= 8 digit bits) sorts 4096-tuple tiles by digit in shared
+//    memory (one histogram row per warp gives every tuple its rank), takes
+//    one output range per digit with a single global atomic, and writes the
+//    tile digit-run by digit-run, so stores are coalesced and at most 256
+//    output regions are open per pass (the first pass of a 2^14 fan-out
+//    writes 128 regions; the second writes inside one 32 MB bucket);
+//  * radix bits are chosen so the largest build partition fits an on-chip
+//    table of kRMax tuples (the bench's 2^27-row side: 16384 partitions of
+//    8192 +- 90 tuples);
+//  * the join kernel is persistent: CTAs pull work items (partition, build
+//    chunk, probe chunk) from an atomic counter, so a skewed probe partition
+//    (Zipf keys) is spread over many SMs.  The on-chip table stores keys and
+//    values in two arrays; a probe reads four keys per 16-byte shared load
+//    and resolves match / empty with bit masks, so nearly every probe is one
+//    load.  The partition that INT32_MIN (the empty marker) hashes to uses
+//    an index table instead.
 #include <algorithm>
+#include <cmath>
 
 #include "gbj_internal.cuh"
 #include "radix.cuh"
@@ -32,102 +40,185 @@ using namespace gbj;
 
 namespace {
 
-constexpr int kPartThreads = 1024;
+constexpr int kTile = 4096;          // tuples per tile of a partition pass
+constexpr int kTileThreads = 1024;   // 4 tuples per thread
+constexpr int kMaxDigits = 256;      // <= 8 digit bits per pass
+constexpr int32_t kEmpty = INT32_MIN;
 
 template <int kDigit>
-__device__ __forceinline__ uint32_t digit_of(int32_t key, int shift, uint32_t pmask) {
+__device__ __forceinline__ uint32_t digit_of(int32_t key, int shift, uint32_t mask) {
   const uint32_t v = kDigit == GBJ_DIGIT_HASH ? gbjd::fmix32((uint32_t)key) : (uint32_t)key;
-  return (v >> shift) & pmask;
+  return (v >> shift) & mask;
 }
 
-// Count pass: CTA c histograms segment [c*seg, (c+1)*seg) into shared
-// memory and stores it column c of hist[P][G].
+// Global histogram of partition ids (shared-memory counts, one global
+// atomic per non-empty bin and CTA).
 template <int kDigit>
-__global__ void __launch_bounds__(kPartThreads)
-    k_part_count(const int32_t *__restrict__ keys, uint64_t n, int shift,
-                 uint32_t pmask, uint64_t seg, uint32_t *__restrict__ hist) {
+__global__ void __launch_bounds__(1024)
+    k_pid_hist(const int32_t *__restrict__ keys, uint64_t n, int shift, uint32_t pmask,
+               uint32_t *__restrict__ ghist) {
   extern __shared__ uint32_t sh[];
   const uint32_t P = pmask + 1;
   for (uint32_t p = threadIdx.x; p < P; p += blockDim.x) sh[p] = 0;
   __syncthreads();
-  const uint64_t lo = blockIdx.x * seg;
-  const uint64_t hi = lo + seg < n ? lo + seg : n;
-  if (lo < hi) {
-    const uint64_t qlo = lo / 4, qhi = hi / 4;  // seg % 4 == 0
-    const int4 *k4 = reinterpret_cast<const int4 *>(keys);
-    for (uint64_t q = qlo + threadIdx.x; q < qhi; q += blockDim.x) {
-      const int4 k = __ldcs(k4 + q);
-      atomicAdd(&sh[digit_of<kDigit>(k.x, shift, pmask)], 1u);
-      atomicAdd(&sh[digit_of<kDigit>(k.y, shift, pmask)], 1u);
-      atomicAdd(&sh[digit_of<kDigit>(k.z, shift, pmask)], 1u);
-      atomicAdd(&sh[digit_of<kDigit>(k.w, shift, pmask)], 1u);
-    }
-    for (uint64_t i = qhi * 4 + threadIdx.x; i < hi; i += blockDim.x)
-      atomicAdd(&sh[digit_of<kDigit>(keys[i], shift, pmask)], 1u);
-  }
-  __syncthreads();
-  const uint32_t G = gridDim.x;
-  for (uint32_t p = threadIdx.x; p < P; p += blockDim.x) hist[(uint64_t)p * G + blockIdx.x] = sh[p];
-}
-
-// Scatter pass: same segments; cursors start at the scanned offsets.
-template <int kDigit, bool kAoS>
-__global__ void __launch_bounds__(kPartThreads)
-    k_part_scatter(const int32_t *__restrict__ keys, const int32_t *__restrict__ vals,
-                   uint64_t n, int shift, uint32_t pmask, uint64_t seg,
-                   const uint64_t *__restrict__ base, int2 *__restrict__ out_pairs,
-                   int32_t *__restrict__ out_k, int32_t *__restrict__ out_v) {
-  extern __shared__ uint32_t cur[];
-  const uint32_t P = pmask + 1, G = gridDim.x;
-  for (uint32_t p = threadIdx.x; p < P; p += blockDim.x)
-    cur[p] = (uint32_t)base[(uint64_t)p * G + blockIdx.x];
-  __syncthreads();
-  const uint64_t lo = blockIdx.x * seg;
-  const uint64_t hi = lo + seg < n ? lo + seg : n;
-  auto put = [&](int32_t k, int32_t v) {
-    const uint32_t pos = atomicAdd(&cur[digit_of<kDigit>(k, shift, pmask)], 1u);
-    if (kAoS) {
-      out_pairs[pos] = make_int2(k, v);
-    } else {
-      out_k[pos] = k;
-      out_v[pos] = v;
-    }
-  };
-  if (lo < hi) {
-    const uint64_t qlo = lo / 4, qhi = hi / 4;
-    const int4 *k4 = reinterpret_cast<const int4 *>(keys);
-    const int4 *v4 = reinterpret_cast<const int4 *>(vals);
-    for (uint64_t q = qlo + threadIdx.x; q < qhi; q += blockDim.x) {
-      const int4 k = __ldcs(k4 + q);
-      int4 v;
-      if (vals) {
-        v = __ldcs(v4 + q);
-      } else {
-        const int32_t r = (int32_t)(q * 4);
-        v = make_int4(r, r + 1, r + 2, r + 3);
-      }
-      put(k.x, v.x);
-      put(k.y, v.y);
-      put(k.z, v.z);
-      put(k.w, v.w);
-    }
-    for (uint64_t i = qhi * 4 + threadIdx.x; i < hi; i += blockDim.x)
-      put(keys[i], vals ? vals[i] : (int32_t)i);
-  }
-}
-
-__global__ void k_part_offsets(const uint64_t *__restrict__ base, uint32_t P, uint32_t G,
-                               uint64_t n, uint64_t *__restrict__ offsets) {
-  const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
-  if (p < P) offsets[p] = base[(uint64_t)p * G];
-  if (p == 0) offsets[P] = n;
-}
-
-// Scalar count/scatter for inputs whose pointers are not 16-byte aligned:
-// copy into aligned scratch first (one extra pass, only for odd callers).
-__global__ void k_copy_i32(const int32_t *__restrict__ in, int32_t *__restrict__ out, uint64_t n) {
   const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
-  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += stride) out[i] = in[i];
+  uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+  for (; i + 3 * stride < n; i += 4 * stride) {
+    int32_t k[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) k[u] = __ldg(keys + i + u * stride);
+#pragma unroll
+    for (int u = 0; u < 4; ++u) atomicAdd(&sh[digit_of<kDigit>(k[u], shift, pmask)], 1u);
+  }
+  for (; i < n; i += stride) atomicAdd(&sh[digit_of<kDigit>(__ldg(keys + i), shift, pmask)], 1u);
+  __syncthreads();
+  for (uint32_t p = threadIdx.x; p < P; p += blockDim.x)
+    if (sh[p]) atomicAdd(&ghist[p], sh[p]);
+}
+
+struct TileSmem {
+  uint32_t whist[32][kMaxDigits];  // per-warp digit counts, then run offsets
+  int2 sorted[kTile];
+  uint16_t sdig[kTile];
+  uint32_t dstart[kMaxDigits];
+  uint32_t gpos[kMaxDigits];
+  uint32_t wsum[8];
+};
+
+// One partition pass.  Tiles of kTile tuples: contiguous from the SoA input
+// (kPairsIn = false), or, for a second pass, kTile-tuple pieces of each
+// parent bucket of the AoS input (tile_off = prefix of tiles per bucket).
+// digit = (f(key) >> dshift) & dmask; the output cursor of (bucket b,
+// digit d) is cursor[b * (dmask + 1) + d].
+template <int kDigit, bool kPairsIn, bool kAoSOut>
+__global__ void __launch_bounds__(kTileThreads, 2)
+    k_tile_pass(const int32_t *__restrict__ keys, const int32_t *__restrict__ vals,
+                const int2 *__restrict__ pin, uint64_t n, int dshift, uint32_t dmask,
+                const uint64_t *__restrict__ bucket_off, const uint64_t *__restrict__ tile_off,
+                uint32_t nb, uint32_t *__restrict__ cursor, int2 *__restrict__ out_pairs,
+                int32_t *__restrict__ out_k, int32_t *__restrict__ out_v) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  TileSmem &S = *reinterpret_cast<TileSmem *>(smem_raw);
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const uint32_t ndig = dmask + 1;
+  const uint64_t ntiles = kPairsIn ? tile_off[nb] : (n + kTile - 1) / kTile;
+  for (uint64_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
+    uint64_t lo, hi;
+    uint32_t b = 0;
+    if (kPairsIn) {
+      uint32_t a = 0, z = nb;  // tile_off[a] <= t < tile_off[z]
+      while (z - a > 1) {
+        const uint32_t mid = (a + z) >> 1;
+        if (tile_off[mid] <= t) a = mid; else z = mid;
+      }
+      b = a;
+      lo = bucket_off[b] + (t - tile_off[b]) * kTile;
+      hi = lo + kTile < bucket_off[b + 1] ? lo + kTile : bucket_off[b + 1];
+    } else {
+      lo = t * kTile;
+      hi = lo + kTile < n ? lo + kTile : n;
+    }
+    for (uint32_t d = lane; d < ndig; d += 32) S.whist[warp][d] = 0;
+    __syncwarp();
+    int2 tup[4];
+    uint32_t dg[4], rk[4];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const uint64_t i = lo + tid + j * kTileThreads;
+      if (i < hi) {
+        if (kPairsIn) {
+          tup[j] = __ldcs(pin + i);
+        } else {
+          tup[j].x = __ldcs(keys + i);
+          tup[j].y = vals ? __ldcs(vals + i) : (int32_t)i;
+        }
+      }
+    }
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      if (lo + tid + j * kTileThreads < hi) {
+        dg[j] = digit_of<kDigit>(tup[j].x, dshift, dmask);
+        rk[j] = atomicAdd(&S.whist[warp][dg[j]], 1u);
+      }
+    }
+    __syncthreads();
+    // per digit: prefix over warps (in place) and the tile total
+    uint32_t tot = 0;
+    if ((uint32_t)tid < ndig) {
+      for (int w = 0; w < 32; ++w) {
+        const uint32_t c = S.whist[w][tid];
+        S.whist[w][tid] = tot;
+        tot += c;
+      }
+    }
+    // exclusive scan of the digit totals (ndig <= 256: warps 0..7)
+    uint32_t incl = 0;
+    if (tid < kMaxDigits) {
+      incl = tot;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += y;
+      }
+      if (lane == 31) S.wsum[warp] = incl;
+    }
+    __syncthreads();
+    if ((uint32_t)tid < ndig) {
+      uint32_t add = 0;
+      for (int w = 0; w < warp; ++w) add += S.wsum[w];
+      S.dstart[tid] = add + incl - tot;
+      S.gpos[tid] = tot ? atomicAdd(&cursor[(uint64_t)b * ndig + tid], tot) : 0u;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      if (lo + tid + j * kTileThreads < hi) {
+        const uint32_t pos = S.dstart[dg[j]] + S.whist[warp][dg[j]] + rk[j];
+        S.sorted[pos] = tup[j];
+        S.sdig[pos] = (uint16_t)dg[j];
+      }
+    }
+    __syncthreads();
+    const uint32_t cnt = (uint32_t)(hi - lo);
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const uint32_t i = tid + j * kTileThreads;
+      if (i < cnt) {
+        const uint32_t d = S.sdig[i];
+        const uint32_t g = S.gpos[d] + (i - S.dstart[d]);
+        const int2 v = S.sorted[i];
+        if (kAoSOut) {
+          out_pairs[g] = v;
+        } else {
+          out_k[g] = v.x;
+          out_v[g] = v.y;
+        }
+      }
+    }
+    __syncthreads();
+  }
+}
+
+// cursor2[p] = off[p]; for a two-pass partition also the pass-1 bucket
+// starts cursor1[b] = bucket_off[b] = off[b << bits2] (bucket_off[B1] = n).
+__global__ void k_cursors(const uint64_t *__restrict__ off, uint32_t P, int bits2,
+                          uint32_t *__restrict__ cursor1, uint32_t *__restrict__ cursor2,
+                          uint64_t *__restrict__ bucket_off) {
+  const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p < P) {
+    cursor2[p] = (uint32_t)off[p];
+    if (cursor1 && (p & ((1u << bits2) - 1)) == 0) {
+      cursor1[p >> bits2] = (uint32_t)off[p];
+      bucket_off[p >> bits2] = off[p];
+    }
+  }
+  if (cursor1 && p == 0) bucket_off[P >> bits2] = off[P];
+}
+
+__global__ void k_bucket_tiles(const uint64_t *__restrict__ bucket_off, uint32_t nb,
+                               uint64_t *__restrict__ tiles) {
+  const uint32_t b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b < nb) tiles[b] = (bucket_off[b + 1] - bucket_off[b] + kTile - 1) / kTile;
 }
 
 // ---------------------------------------------------------------- join
@@ -142,40 +233,97 @@ __global__ void k_join_items(const uint64_t *__restrict__ ro, const uint64_t *__
   items[p] = (nr && ns) ? ((nr + rmax - 1) / rmax) * ((ns + w - 1) / w) : 0;
 }
 
-// Persistent partition join.  Shared memory: build keys and values of one
-// build chunk (kRMax each) and an open-addressing index of 16-bit
-// (position + 1) entries, 2 * kRMax slots, probed with the fmix32 bits
-// above the partition bits.
-template <int kRMax, int kThreads>
-__global__ void __launch_bounds__(kThreads)
+// Partition of work item `item`: largest p with item_off[p] <= item, where
+// item_off[0] = 0 <= item < item_off[P] = total.  Starts from the
+// proportional guess and gallops, so the common case (about one item per
+// partition) costs two or three dependent loads.
+__device__ __forceinline__ uint32_t item_partition(const uint64_t *__restrict__ off, uint32_t P,
+                                                   uint64_t total, uint64_t item) {
+  uint32_t lo = (uint32_t)((item * (uint64_t)P) / total);
+  if (lo >= P) lo = P - 1;
+  uint32_t hi;
+  if (off[lo] <= item) {
+    uint32_t step = 1;
+    hi = lo + 1;
+    while (hi < P && off[hi] <= item) {
+      lo = hi;
+      step <<= 1;
+      hi = lo + step < P ? lo + step : P;
+    }
+  } else {
+    uint32_t step = 1;
+    hi = lo;
+    for (;;) {  // off[hi] > item; off[0] = 0 <= item ends the walk
+      lo = hi > step ? hi - step : 0;
+      if (off[lo] <= item) break;
+      hi = lo;
+      step <<= 1;
+    }
+  }
+  while (hi - lo > 1) {  // off[lo] <= item < off[hi]
+    const uint32_t mid = (lo + hi) >> 1;
+    if (off[mid] <= item) lo = mid; else hi = mid;
+  }
+  return lo;
+}
+
+enum : int { kAggGeneric = 0, kAggCountXor = 1, kAggCountProduct = 2 };
+
+// Table slot of key k: multiply-shift of the fmix32 bits above the partition
+// bits onto [0, cap).
+__device__ __forceinline__ uint32_t table_slot(int32_t k, int bits, uint32_t cap) {
+  return (uint32_t)(((uint64_t)(gbjd::fmix32((uint32_t)k) >> bits) * cap) >> (32 - bits));
+}
+
+template <int kAgg>
+__device__ __forceinline__ void join_match(const gbj::AggSpec &spec, gbjd::Acc &acc, int64_t &a_cnt,
+                                           int64_t &a_sum, int32_t k, int32_t bv, int32_t pv) {
+  if (kAgg == kAggCountXor) {
+    a_cnt += 1;
+    a_sum += (int64_t)bv ^ (int64_t)pv;
+  } else if (kAgg == kAggCountProduct) {
+    a_cnt += 1;
+    a_sum += (int64_t)bv * (int64_t)pv;
+  } else {
+    acc.update(spec, k, bv, pv, bv, pv);
+  }
+}
+
+// Persistent partition join.  Dynamic shared memory holds, for the current
+// build chunk of m tuples and cap = 2m rounded up to 64 slots, either
+//   keys[cap] + values[cap]            (every partition but one), or
+//   pairs[kRMax] + index[cap] (16-bit) (the partition INT32_MIN maps to).
+template <int kRMax, int kThreads, int kAgg>
+__global__ void __launch_bounds__(kThreads, 1)
     k_radix_join(const int2 *__restrict__ R, const uint64_t *__restrict__ ro,
                  const int2 *__restrict__ S, const uint64_t *__restrict__ so,
                  const uint64_t *__restrict__ item_off, uint32_t P, int bits, uint64_t w,
-                 gbj::AggSpec spec, int64_t *out, unsigned long long *item_ctr) {
+                 uint32_t sentinel_part, gbj::AggSpec spec, int64_t *out,
+                 unsigned long long *item_ctr) {
+  static_assert(2 * kRMax + 64 <= 65535, "16-bit index entries");
+  constexpr uint32_t kCapMax = 2 * kRMax + 64;
   extern __shared__ __align__(16) unsigned char smem[];
-  int32_t *rk = reinterpret_cast<int32_t *>(smem);
-  int32_t *rv = rk + kRMax;
-  unsigned short *tab = reinterpret_cast<unsigned short *>(rv + kRMax);
+  int32_t *tkey = reinterpret_cast<int32_t *>(smem);
+  int32_t *tval = tkey + kCapMax;
+  int2 *rp = reinterpret_cast<int2 *>(smem);
+  unsigned short *tab = reinterpret_cast<unsigned short *>(rp + kRMax);
   __shared__ int64_t red[32 * GBJ_MAX_AGGS];
   __shared__ unsigned long long s_item;
+  __shared__ uint32_t s_part;
   __shared__ int s_dup;
   gbjd::Acc acc;
   acc.init(spec);
+  int64_t a_cnt = 0, a_sum = 0;
   const uint64_t total = item_off[P];
+  if (threadIdx.x == 0) {
+    s_item = atomicAdd(item_ctr, 1ull);
+    s_part = s_item < total ? item_partition(item_off, P, total, s_item) : 0;
+  }
+  __syncthreads();
   for (;;) {
-    if (threadIdx.x == 0) {
-      s_item = atomicAdd(item_ctr, 1ull);
-      s_dup = 0;
-    }
-    __syncthreads();
     const uint64_t item = s_item;
+    const uint32_t p = s_part;
     if (item >= total) break;
-    uint32_t lo = 0, hi = P;  // item_off[lo] <= item < item_off[hi]
-    while (hi - lo > 1) {
-      const uint32_t mid = (lo + hi) >> 1;
-      if (item_off[mid] <= item) lo = mid; else hi = mid;
-    }
-    const uint32_t p = lo;
     const uint64_t r0 = ro[p], r1 = ro[p + 1], s0 = so[p], s1 = so[p + 1];
     const uint64_t nrc = (r1 - r0 + kRMax - 1) / kRMax;
     const uint64_t local = item - item_off[p];
@@ -184,33 +332,68 @@ __global__ void __launch_bounds__(kThreads)
     const uint64_t sb = s0 + (local / nrc) * w;
     const uint64_t se = sb + w < s1 ? sb + w : s1;
     const int m = (int)(re - rb);
-    int cap = 64;
-    while (cap < 2 * m) cap <<= 1;
-    const uint32_t cmask = cap - 1;
-    uint32_t *tab32 = reinterpret_cast<uint32_t *>(tab);
-    for (int i = threadIdx.x; i < cap / 2; i += kThreads) tab32[i] = 0;
-    for (int i = threadIdx.x; i < m; i += kThreads) {
-      const int2 t = R[rb + i];
-      rk[i] = t.x;
-      rv[i] = t.y;
-    }
-    __syncthreads();
-    for (int i = threadIdx.x; i < m; i += kThreads) {
-      const int32_t k = rk[i];
-      uint32_t h = (gbjd::fmix32((uint32_t)k) >> bits) & cmask;
+    const uint32_t cap = (uint32_t)((2 * m + 63) & ~63);
+    const bool fast = p != sentinel_part;
+    if (threadIdx.x == 0) s_dup = 0;
+    if (fast) {
+      // ---- keys + values table ----
+      int4 *tk4 = reinterpret_cast<int4 *>(tkey);
+      for (uint32_t i = threadIdx.x; i < cap / 4; i += kThreads)
+        tk4[i] = make_int4(kEmpty, kEmpty, kEmpty, kEmpty);
+      __syncthreads();
       bool dup = false;
-      for (int step = 0; step < cap; ++step) {
-        const unsigned short old = atomicCAS(&tab[h], (unsigned short)0, (unsigned short)(i + 1));
-        if (old == 0) break;
-        dup |= (rk[old - 1] == k);
-        h = (h + 1) & cmask;
+      auto insert = [&](int2 t) {
+        uint32_t h = table_slot(t.x, bits, cap);
+        for (uint32_t step = 0; step < cap; ++step) {
+          const int32_t old = atomicCAS(&tkey[h], kEmpty, t.x);
+          if (old == kEmpty) {
+            tval[h] = t.y;
+            return;
+          }
+          dup |= (old == t.x);
+          if (++h == cap) h = 0;
+        }
+      };
+      for (uint64_t i0 = rb + threadIdx.x; i0 < re; i0 += 4 * kThreads) {
+        int2 t[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+          const uint64_t i = i0 + (uint64_t)u * kThreads;
+          if (i < re) t[u] = __ldcs(R + i);
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u)
+          if (i0 + (uint64_t)u * kThreads < re) insert(t[u]);
+      }
+      if (dup) s_dup = 1;
+    } else {
+      // ---- pairs + 16-bit index table (INT32_MIN keys allowed) ----
+      uint32_t *tab32 = reinterpret_cast<uint32_t *>(tab);
+      for (uint32_t i = threadIdx.x; i < cap / 2; i += kThreads) tab32[i] = 0;
+      for (int i = threadIdx.x; i < m; i += kThreads) rp[i] = R[rb + i];
+      __syncthreads();
+      bool dup = false;
+      for (int i = threadIdx.x; i < m; i += kThreads) {
+        const int32_t k = rp[i].x;
+        uint32_t h = table_slot(k, bits, cap);
+        for (uint32_t step = 0; step < cap; ++step) {
+          const unsigned short old = atomicCAS(&tab[h], (unsigned short)0, (unsigned short)(i + 1));
+          if (old == 0) break;
+          dup |= (rp[old - 1].x == k);
+          if (++h == cap) h = 0;
+        }
       }
       if (dup) s_dup = 1;
     }
     __syncthreads();
     const bool unique = s_dup == 0;
-    // probe: 4 independent tuples per thread per round for memory-level
-    // parallelism on the streamed probe chunk
+    // next item: fetched now, consumed after the closing barrier
+    if (threadIdx.x == 0) {
+      const unsigned long long nx = atomicAdd(item_ctr, 1ull);
+      s_item = nx;
+      s_part = nx < total ? item_partition(item_off, P, total, nx) : 0;
+    }
+    // probe chunk: 4 tuples per thread per round, loads issued together
     for (uint64_t j0 = sb + threadIdx.x; j0 < se; j0 += 4 * kThreads) {
       int2 t[4];
 #pragma unroll
@@ -222,59 +405,156 @@ __global__ void __launch_bounds__(kThreads)
       for (int u = 0; u < 4; ++u) {
         if (j0 + (uint64_t)u * kThreads >= se) continue;
         const int32_t k = t[u].x;
-        uint32_t h = (gbjd::fmix32((uint32_t)k) >> bits) & cmask;
-        for (int step = 0; step < cap; ++step) {
-          const unsigned short idx = tab[h];
-          if (idx == 0) break;
-          if (rk[idx - 1] == k) {
-            const int64_t bv = rv[idx - 1];
-            acc.update(spec, k, bv, t[u].y, bv, t[u].y);
-            if (unique) break;
+        const uint32_t h = table_slot(k, bits, cap);
+        if (fast) {
+          // four keys per 16-byte load; slots before the first empty one
+          // (from the probe start) are candidates
+          uint32_t g0 = h & ~3u, o = h & 3u;
+          for (uint32_t step = 0; step < cap; step += 4) {
+            const int4 kk = *reinterpret_cast<const int4 *>(tkey + g0);
+            const uint32_t valid = (0xfu << o) & 0xfu;
+            const uint32_t em = valid & ((kk.x == kEmpty) | ((kk.y == kEmpty) << 1) |
+                                         ((kk.z == kEmpty) << 2) | ((kk.w == kEmpty) << 3));
+            const uint32_t before = em ? (em & (0u - em)) - 1u : 0xfu;
+            uint32_t hits = valid & before &
+                            ((kk.x == k) | ((kk.y == k) << 1) | ((kk.z == k) << 2) | ((kk.w == k) << 3));
+            bool stop = em != 0;
+            while (hits) {
+              const uint32_t i = __ffs(hits) - 1;
+              join_match<kAgg>(spec, acc, a_cnt, a_sum, k, tval[g0 + i], t[u].y);
+              if (unique) {
+                stop = true;
+                break;
+              }
+              hits &= hits - 1;
+            }
+            if (stop) break;
+            o = 0;
+            g0 += 4;
+            if (g0 >= cap) g0 = 0;
           }
-          h = (h + 1) & cmask;
+        } else {
+          uint32_t hh = h;
+          for (uint32_t step = 0; step < cap; ++step) {
+            const unsigned short idx = tab[hh];
+            if (idx == 0) break;
+            const int2 bt = rp[idx - 1];
+            if (bt.x == k) {
+              join_match<kAgg>(spec, acc, a_cnt, a_sum, k, bt.y, t[u].y);
+              if (unique) break;
+            }
+            if (++hh == cap) hh = 0;
+          }
         }
       }
     }
     __syncthreads();
   }
+  if (kAgg != kAggGeneric) {
+    acc.v[0] = a_cnt;
+    acc.v[1] = a_sum;
+  }
   gbjd::block_flush(spec, acc, red, out);
 }
 
-struct JoinCfg {
-  int rmax;
-  int threads;
-};
+template <int kRMax>
+constexpr size_t join_smem() {
+  return (size_t)2 * (2 * kRMax + 64) * sizeof(int32_t);  // >= pairs + 16-bit index
+}
 
-template <int kRMax, int kThreads>
+template <int kRMax, int kThreads, int kAgg>
 int launch_join(gbj_ctx *ctx, const int2 *R, const uint64_t *ro, const int2 *S,
                 const uint64_t *so, const uint64_t *item_off, uint32_t P, int bits,
-                uint64_t w, const AggSpec &spec, int64_t *out, unsigned long long *ctr,
-                cudaStream_t s) {
-  const size_t smem = (size_t)kRMax * 8 + (size_t)kRMax * 2 * 2;
-  auto kern = k_radix_join<kRMax, kThreads>;
+                uint64_t w, uint32_t sentinel_part, const AggSpec &spec, int64_t *out,
+                unsigned long long *ctr, cudaStream_t s) {
+  const size_t smem = join_smem<kRMax>();
+  auto kern = k_radix_join<kRMax, kThreads, kAgg>;
   GBJ_CHECK_CUDA(ctx, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                            (int)smem));
   int per_sm = 0;
   GBJ_CHECK_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kThreads, smem));
-  if (per_sm < 1) per_sm = 1;
-  kern<<<ctx->sm_count * per_sm, kThreads, smem, s>>>(R, ro, S, so, item_off, P, bits, w, spec,
-                                                     out, ctr);
+  if (per_sm < 1) return set_error(ctx, GBJ_ERR_CUDA, "k_radix_join: no resident block fits");
+  kern<<<ctx->sm_count * per_sm, kThreads, smem, s>>>(R, ro, S, so, item_off, P, bits, w,
+                                                     sentinel_part, spec, out, ctr);
   return after_launch(ctx, "k_radix_join", s);
 }
 
-int part_grid(gbj_ctx *ctx, uint64_t n, uint64_t *seg) {
-  // One CTA per SM (the shared histogram / cursors take up to 128 KB);
-  // segments are multiples of 4 tuples for the int4 loads.
-  uint64_t G = (uint64_t)ctx->sm_count;
-  if (n < (1u << 16)) G = 1;
-  else if (n < (1u << 22)) G = std::max<uint64_t>(1, std::min<uint64_t>(G, n >> 14));
-  uint64_t sg = (n + G - 1) / G;
-  sg = (sg + 3) / 4 * 4;
-  if (sg == 0) sg = 4;
-  G = (n + sg - 1) / sg;
-  if (G == 0) G = 1;
-  *seg = sg;
-  return (int)G;
+template <int kDigit, bool kPairsIn, bool kAoSOut>
+int launch_tile_pass(gbj_ctx *ctx, const int32_t *keys, const int32_t *vals, const int2 *pin,
+                     uint64_t n, int dshift, uint32_t dmask, const uint64_t *bucket_off,
+                     const uint64_t *tile_off, uint32_t nb, uint32_t *cursor, int2 *op, int32_t *ok,
+                     int32_t *ov, cudaStream_t s) {
+  auto kern = k_tile_pass<kDigit, kPairsIn, kAoSOut>;
+  const size_t smem = sizeof(TileSmem);
+  GBJ_CHECK_CUDA(ctx, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  int per_sm = 0;
+  GBJ_CHECK_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kTileThreads, smem));
+  if (per_sm < 1) per_sm = 1;
+  const uint64_t tiles_hint = (n + kTile - 1) / kTile + nb;
+  const uint64_t grid = std::max<uint64_t>(1, std::min<uint64_t>((uint64_t)ctx->sm_count * per_sm, tiles_hint));
+  kern<<<(unsigned)grid, kTileThreads, smem, s>>>(keys, vals, pin, n, dshift, dmask, bucket_off,
+                                                  tile_off, nb, cursor, op, ok, ov);
+  return after_launch(ctx, "k_tile_pass", s);
+}
+
+template <int kDigit>
+int partition_impl(gbj_ctx *ctx, const int32_t *keys, const int32_t *vals, uint64_t n, int shift,
+                   int bits, int2 *out_pairs, int32_t *out_keys, int32_t *out_vals,
+                   uint64_t *offsets, cudaStream_t s) {
+  const uint32_t P = 1u << bits, pmask = P - 1;
+  Scratch scratch(ctx, s);
+  uint32_t *hist, *cursor2;
+  uint64_t *off;
+  GBJ_TRY(scratch.get(P + 1, &hist));
+  GBJ_TRY(scratch.get(P + 1, &cursor2));
+  GBJ_TRY(scratch.get(P + 1, &off));
+  GBJ_CHECK_CUDA(ctx, cudaMemsetAsync(hist, 0, sizeof(uint32_t) * P, s));
+  {
+    const size_t smem = (size_t)P * sizeof(uint32_t);
+    GBJ_CHECK_CUDA(ctx, cudaFuncSetAttribute(k_pid_hist<kDigit>,
+                                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    const uint64_t grid = std::max<uint64_t>(1, std::min<uint64_t>(ctx->sm_count, (n + 16383) / 16384));
+    k_pid_hist<kDigit><<<(unsigned)grid, 1024, smem, s>>>(keys, n, shift, pmask, hist);
+    GBJ_TRY(after_launch(ctx, "k_pid_hist", s));
+  }
+  GBJ_TRY(scan_u32_to_u64(ctx, hist, off, P, s));
+  if (bits <= 8) {
+    k_cursors<<<(P + 255) / 256, 256, 0, s>>>(off, P, 0, nullptr, cursor2, nullptr);
+    GBJ_TRY(after_launch(ctx, "k_cursors", s));
+    if (out_pairs)
+      GBJ_TRY((launch_tile_pass<kDigit, false, true>(ctx, keys, vals, nullptr, n, shift, pmask, nullptr,
+                                                     nullptr, 1, cursor2, out_pairs, nullptr, nullptr, s)));
+    else
+      GBJ_TRY((launch_tile_pass<kDigit, false, false>(ctx, keys, vals, nullptr, n, shift, pmask, nullptr,
+                                                      nullptr, 1, cursor2, nullptr, out_keys, out_vals, s)));
+  } else {
+    const int bits2 = bits / 2, bits1 = bits - bits2;
+    const uint32_t B1 = 1u << bits1;
+    uint32_t *cursor1;
+    uint64_t *bucket_off, *tiles;
+    int2 *tmp;
+    GBJ_TRY(scratch.get(B1 + 1, &cursor1));
+    GBJ_TRY(scratch.get(B1 + 1, &bucket_off));
+    GBJ_TRY(scratch.get(B1 + 1, &tiles));
+    GBJ_TRY(scratch.get(n + 1, &tmp));
+    k_cursors<<<(P + 255) / 256, 256, 0, s>>>(off, P, bits2, cursor1, cursor2, bucket_off);
+    GBJ_TRY(after_launch(ctx, "k_cursors", s));
+    GBJ_TRY((launch_tile_pass<kDigit, false, true>(ctx, keys, vals, nullptr, n, shift + bits2, B1 - 1,
+                                                   nullptr, nullptr, 1, cursor1, tmp, nullptr, nullptr, s)));
+    k_bucket_tiles<<<(B1 + 255) / 256, 256, 0, s>>>(bucket_off, B1, tiles);
+    GBJ_TRY(after_launch(ctx, "k_bucket_tiles", s));
+    GBJ_TRY(scan_u64(ctx, tiles, tiles, B1, s));
+    const uint32_t m2 = (1u << bits2) - 1;
+    if (out_pairs)
+      GBJ_TRY((launch_tile_pass<kDigit, true, true>(ctx, nullptr, nullptr, tmp, n, shift, m2, bucket_off,
+                                                    tiles, B1, cursor2, out_pairs, nullptr, nullptr, s)));
+    else
+      GBJ_TRY((launch_tile_pass<kDigit, true, false>(ctx, nullptr, nullptr, tmp, n, shift, m2, bucket_off,
+                                                     tiles, B1, cursor2, nullptr, out_keys, out_vals, s)));
+  }
+  if (offsets) GBJ_CHECK_CUDA(ctx, cudaMemcpyAsync(offsets, off, sizeof(uint64_t) * (P + 1),
+                                                   cudaMemcpyDeviceToDevice, s));
+  return GBJ_OK;
 }
 
 }  // namespace
@@ -284,60 +564,11 @@ namespace gbj {
 int partition_tuples(gbj_ctx *ctx, const int32_t *keys, const int32_t *vals, uint64_t n,
                      int digit, int shift, int bits, int2 *out_pairs, int32_t *out_keys,
                      int32_t *out_vals, uint64_t *offsets, cudaStream_t s) {
-  const uint32_t P = 1u << bits, pmask = P - 1;
-  Scratch scratch(ctx, s);
-  // int4 loads need 16-byte aligned inputs; realign odd callers once.
-  if ((uintptr_t)keys % 16 || (vals && (uintptr_t)vals % 16)) {
-    int32_t *k2, *v2 = nullptr;
-    GBJ_TRY(scratch.get(n, &k2));
-    k_copy_i32<<<ctx->sm_count * 4, 256, 0, s>>>(keys, k2, n);
-    GBJ_TRY(after_launch(ctx, "k_copy_i32", s));
-    if (vals) {
-      GBJ_TRY(scratch.get(n, &v2));
-      k_copy_i32<<<ctx->sm_count * 4, 256, 0, s>>>(vals, v2, n);
-      GBJ_TRY(after_launch(ctx, "k_copy_i32", s));
-    }
-    keys = k2;
-    vals = v2;
-  }
-  uint64_t seg;
-  const int G = part_grid(ctx, n, &seg);
-  uint32_t *hist;
-  uint64_t *base;
-  GBJ_TRY(scratch.get((uint64_t)P * G, &hist));
-  GBJ_TRY(scratch.get((uint64_t)P * G + 1, &base));
-  const size_t smem = (size_t)P * sizeof(uint32_t);
-  if (digit == GBJ_DIGIT_HASH) {
-    GBJ_CHECK_CUDA(ctx, cudaFuncSetAttribute(k_part_count<GBJ_DIGIT_HASH>,
-                                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    k_part_count<GBJ_DIGIT_HASH><<<G, kPartThreads, smem, s>>>(keys, n, shift, pmask, seg, hist);
-  } else {
-    GBJ_CHECK_CUDA(ctx, cudaFuncSetAttribute(k_part_count<GBJ_DIGIT_KEY>,
-                                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    k_part_count<GBJ_DIGIT_KEY><<<G, kPartThreads, smem, s>>>(keys, n, shift, pmask, seg, hist);
-  }
-  GBJ_TRY(after_launch(ctx, "k_part_count", s));
-  GBJ_TRY(scan_u32_to_u64(ctx, hist, base, (uint64_t)P * G, s));
-#define GBJ_SCATTER(D, A)                                                                     \
-  do {                                                                                        \
-    GBJ_CHECK_CUDA(ctx, cudaFuncSetAttribute(k_part_scatter<D, A>,                            \
-                                             cudaFuncAttributeMaxDynamicSharedMemorySize,     \
-                                             (int)smem));                                     \
-    k_part_scatter<D, A><<<G, kPartThreads, smem, s>>>(keys, vals, n, shift, pmask, seg, base, \
-                                                       out_pairs, out_keys, out_vals);       \
-  } while (0)
-  if (digit == GBJ_DIGIT_HASH) {
-    if (out_pairs) GBJ_SCATTER(GBJ_DIGIT_HASH, true); else GBJ_SCATTER(GBJ_DIGIT_HASH, false);
-  } else {
-    if (out_pairs) GBJ_SCATTER(GBJ_DIGIT_KEY, true); else GBJ_SCATTER(GBJ_DIGIT_KEY, false);
-  }
-#undef GBJ_SCATTER
-  GBJ_TRY(after_launch(ctx, "k_part_scatter", s));
-  if (offsets) {
-    k_part_offsets<<<(P + 256) / 256, 256, 0, s>>>(base, P, G, n, offsets);
-    GBJ_TRY(after_launch(ctx, "k_part_offsets", s));
-  }
-  return GBJ_OK;
+  if (digit == GBJ_DIGIT_HASH)
+    return partition_impl<GBJ_DIGIT_HASH>(ctx, keys, vals, n, shift, bits, out_pairs, out_keys,
+                                          out_vals, offsets, s);
+  return partition_impl<GBJ_DIGIT_KEY>(ctx, keys, vals, n, shift, bits, out_pairs, out_keys,
+                                       out_vals, offsets, s);
 }
 
 }  // namespace gbj
@@ -401,23 +632,29 @@ int gbj_radix_join_agg(gbj_ctx *ctx, const int32_t *d_build_keys,
   GBJ_TRY(init_agg_out(ctx, spec, d_out, s));
   if (n_build == 0 || n_probe == 0) return GBJ_OK;
 
-  // ---- plan (autotuned defaults; explicit params override) ----
-  constexpr int kRMax = 8192;
+  // ---- plan: fewest radix bits whose largest expected build partition
+  //      (mean + 5 sd) fits the on-chip table; explicit params override ----
+  constexpr int kRMax = 9216;
   int bits = 1;
-  while (bits < kMaxPartBits && (n_build >> bits) > (uint64_t)kRMax / 2) ++bits;
+  while (bits < kMaxPartBits) {
+    const double mean = (double)n_build / (double)(1u << bits);
+    if (mean + 5.0 * std::sqrt(mean) <= (double)kRMax) break;
+    ++bits;
+  }
   if (params && params->log_parts > 0) bits = std::min(params->log_parts, kMaxPartBits);
   if (params && params->bits > 0) bits = std::min(params->bits, kMaxPartBits);
-  if (params && params->passes > 1)
-    return set_error(ctx, GBJ_ERR_UNSUPPORTED, "radix_join: only single-pass partitioning");
+  if (params && params->passes > 2)
+    return set_error(ctx, GBJ_ERR_UNSUPPORTED, "radix_join: at most two partitioning passes");
   const uint32_t P = 1u << bits;
-  const uint64_t w = 1u << 16;  // probe tuples per work item
+  const uint64_t w = 1u << 17;  // probe tuples per work item
+  const uint32_t sentinel_part = gbjd::fmix32((uint32_t)INT32_MIN) & (P - 1);
 
   Scratch scratch(ctx, s);
   int2 *R, *S;
   uint64_t *ro, *so, *items;
   unsigned long long *ctr;
-  GBJ_TRY(scratch.get(n_build, &R));
-  GBJ_TRY(scratch.get(n_probe, &S));
+  GBJ_TRY(scratch.get(n_build + 2, &R));
+  GBJ_TRY(scratch.get(n_probe + 2, &S));
   GBJ_TRY(scratch.get(P + 1, &ro));
   GBJ_TRY(scratch.get(P + 1, &so));
   GBJ_TRY(scratch.get(P + 1, &items));
@@ -430,7 +667,15 @@ int gbj_radix_join_agg(gbj_ctx *ctx, const int32_t *d_build_keys,
   GBJ_TRY(after_launch(ctx, "k_join_items", s));
   GBJ_TRY(scan_u64(ctx, items, items, P, s));
   GBJ_CHECK_CUDA(ctx, cudaMemsetAsync(ctr, 0, sizeof(unsigned long long), s));
-  return launch_join<kRMax, 512>(ctx, R, ro, S, so, items, P, bits, w, spec, d_out, ctr, s);
+  const bool two = spec.n == 2 && spec.op[0] == GBJ_AGG_COUNT && spec.op[1] == GBJ_AGG_SUM;
+  if (two && spec.operand[1] == GBJ_VAL_ROWID_XOR)
+    return launch_join<kRMax, 1024, kAggCountXor>(ctx, R, ro, S, so, items, P, bits, w, sentinel_part,
+                                                  spec, d_out, ctr, s);
+  if (two && spec.operand[1] == GBJ_VAL_PRODUCT)
+    return launch_join<kRMax, 1024, kAggCountProduct>(ctx, R, ro, S, so, items, P, bits, w,
+                                                      sentinel_part, spec, d_out, ctr, s);
+  return launch_join<kRMax, 1024, kAggGeneric>(ctx, R, ro, S, so, items, P, bits, w, sentinel_part,
+                                               spec, d_out, ctr, s);
 }
 
 }  // extern "C"
