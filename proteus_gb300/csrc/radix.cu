@@ -40,8 +40,9 @@ using namespace gbj;
 
 namespace {
 
-constexpr int kTile = 4096;          // tuples per tile of a partition pass
-constexpr int kTileThreads = 1024;   // 4 tuples per thread
+constexpr int kTile = 2048;          // tuples per tile of a partition pass
+constexpr int kTileThreads = 512;    // 4 tuples per thread, 4 CTAs per SM
+constexpr int kTileWarps = kTileThreads / 32;
 constexpr int kMaxDigits = 256;      // <= 8 digit bits per pass
 constexpr int32_t kEmpty = INT32_MIN;
 
@@ -77,7 +78,7 @@ __global__ void __launch_bounds__(1024)
 }
 
 struct TileSmem {
-  uint32_t whist[32][kMaxDigits];  // per-warp digit counts, then run offsets
+  uint32_t whist[kTileWarps][kMaxDigits];  // per-warp digit counts, then run offsets
   int2 sorted[kTile];
   uint16_t sdig[kTile];
   uint32_t dstart[kMaxDigits];
@@ -91,7 +92,7 @@ struct TileSmem {
 // digit = (f(key) >> dshift) & dmask; the output cursor of (bucket b,
 // digit d) is cursor[b * (dmask + 1) + d].
 template <int kDigit, bool kPairsIn, bool kAoSOut>
-__global__ void __launch_bounds__(kTileThreads, 2)
+__global__ void __launch_bounds__(kTileThreads, 4)
     k_tile_pass(const int32_t *__restrict__ keys, const int32_t *__restrict__ vals,
                 const int2 *__restrict__ pin, uint64_t n, int dshift, uint32_t dmask,
                 const uint64_t *__restrict__ bucket_off, const uint64_t *__restrict__ tile_off,
@@ -145,7 +146,8 @@ __global__ void __launch_bounds__(kTileThreads, 2)
     // per digit: prefix over warps (in place) and the tile total
     uint32_t tot = 0;
     if ((uint32_t)tid < ndig) {
-      for (int w = 0; w < 32; ++w) {
+#pragma unroll
+      for (int w = 0; w < kTileWarps; ++w) {
         const uint32_t c = S.whist[w][tid];
         S.whist[w][tid] = tot;
         tot += c;
@@ -307,15 +309,20 @@ __global__ void __launch_bounds__(kThreads, 1)
   int32_t *tval = tkey + kCapMax;
   int2 *rp = reinterpret_cast<int2 *>(smem);
   unsigned short *tab = reinterpret_cast<unsigned short *>(rp + kRMax);
+  // unresolved probes of one round: {key, probe value, next group, -}
+  int4 *queue = reinterpret_cast<int4 *>(tval + kCapMax);
   __shared__ int64_t red[32 * GBJ_MAX_AGGS];
   __shared__ unsigned long long s_item;
   __shared__ uint32_t s_part;
   __shared__ int s_dup;
+  __shared__ uint32_t s_qn[2];
   gbjd::Acc acc;
   acc.init(spec);
   int64_t a_cnt = 0, a_sum = 0;
+  uint32_t round = 0;
   const uint64_t total = item_off[P];
   if (threadIdx.x == 0) {
+    s_qn[0] = s_qn[1] = 0;
     s_item = atomicAdd(item_ctr, 1ull);
     s_part = s_item < total ? item_partition(item_off, P, total, s_item) : 0;
   }
@@ -354,15 +361,16 @@ __global__ void __launch_bounds__(kThreads, 1)
           if (++h == cap) h = 0;
         }
       };
-      for (uint64_t i0 = rb + threadIdx.x; i0 < re; i0 += 4 * kThreads) {
-        int2 t[4];
+      // the whole chunk's loads in flight at once (m <= 9216 = 9 per thread)
+      for (uint64_t i0 = rb + threadIdx.x; i0 < re; i0 += 8 * kThreads) {
+        int2 t[8];
 #pragma unroll
-        for (int u = 0; u < 4; ++u) {
+        for (int u = 0; u < 8; ++u) {
           const uint64_t i = i0 + (uint64_t)u * kThreads;
           if (i < re) t[u] = __ldcs(R + i);
         }
 #pragma unroll
-        for (int u = 0; u < 4; ++u)
+        for (int u = 0; u < 8; ++u)
           if (i0 + (uint64_t)u * kThreads < re) insert(t[u]);
       }
       if (dup) s_dup = 1;
@@ -393,48 +401,81 @@ __global__ void __launch_bounds__(kThreads, 1)
       s_item = nx;
       s_part = nx < total ? item_partition(item_off, P, total, nx) : 0;
     }
-    // probe chunk: 4 tuples per thread per round, loads issued together
-    for (uint64_t j0 = sb + threadIdx.x; j0 < se; j0 += 4 * kThreads) {
-      int2 t[4];
+    if (fast) {
+      // One 4-slot group from the probe start: the candidates are the slots
+      // before the first empty one.  Returns true when the probe is done.
+      auto group = [&](int32_t k, int32_t v, uint32_t g0, uint32_t o) -> bool {
+        const int4 kk = *reinterpret_cast<const int4 *>(tkey + g0);
+        const uint32_t valid = (0xfu << o) & 0xfu;
+        const uint32_t em = valid & ((kk.x == kEmpty) | ((kk.y == kEmpty) << 1) |
+                                     ((kk.z == kEmpty) << 2) | ((kk.w == kEmpty) << 3));
+        const uint32_t before = em ? (em & (0u - em)) - 1u : 0xfu;
+        uint32_t hits = valid & before &
+                        ((kk.x == k) | ((kk.y == k) << 1) | ((kk.z == k) << 2) | ((kk.w == k) << 3));
+        while (hits) {
+          join_match<kAgg>(spec, acc, a_cnt, a_sum, k, tval[g0 + __ffs(hits) - 1], v);
+          if (unique) return true;
+          hits &= hits - 1;
+        }
+        return em != 0;
+      };
+      // Probe rounds of 4 tuples per thread: every probe checks its first
+      // group; the few that must continue go to a shared queue that all
+      // lanes then drain together, so no warp idles behind one long walk.
+      // The next round's tuples are loaded while this round is probed.
+      int2 nxt[4];
 #pragma unroll
       for (int u = 0; u < 4; ++u) {
-        const uint64_t j = j0 + (uint64_t)u * kThreads;
-        t[u] = j < se ? __ldcs(S + j) : make_int2(0, 0);
+        const uint64_t j = sb + threadIdx.x + (uint64_t)u * kThreads;
+        nxt[u] = j < se ? __ldcs(S + j) : make_int2(0, 0);
       }
+      for (uint64_t j0 = sb; j0 < se; j0 += 4 * kThreads, ++round) {
+        const int par = round & 1;
+        int2 t[4];
 #pragma unroll
-      for (int u = 0; u < 4; ++u) {
-        if (j0 + (uint64_t)u * kThreads >= se) continue;
-        const int32_t k = t[u].x;
-        const uint32_t h = table_slot(k, bits, cap);
-        if (fast) {
-          // four keys per 16-byte load; slots before the first empty one
-          // (from the probe start) are candidates
-          uint32_t g0 = h & ~3u, o = h & 3u;
-          for (uint32_t step = 0; step < cap; step += 4) {
-            const int4 kk = *reinterpret_cast<const int4 *>(tkey + g0);
-            const uint32_t valid = (0xfu << o) & 0xfu;
-            const uint32_t em = valid & ((kk.x == kEmpty) | ((kk.y == kEmpty) << 1) |
-                                         ((kk.z == kEmpty) << 2) | ((kk.w == kEmpty) << 3));
-            const uint32_t before = em ? (em & (0u - em)) - 1u : 0xfu;
-            uint32_t hits = valid & before &
-                            ((kk.x == k) | ((kk.y == k) << 1) | ((kk.z == k) << 2) | ((kk.w == k) << 3));
-            bool stop = em != 0;
-            while (hits) {
-              const uint32_t i = __ffs(hits) - 1;
-              join_match<kAgg>(spec, acc, a_cnt, a_sum, k, tval[g0 + i], t[u].y);
-              if (unique) {
-                stop = true;
-                break;
-              }
-              hits &= hits - 1;
-            }
-            if (stop) break;
-            o = 0;
+        for (int u = 0; u < 4; ++u) {
+          t[u] = nxt[u];
+          const uint64_t j = j0 + 4 * kThreads + threadIdx.x + (uint64_t)u * kThreads;
+          nxt[u] = j < se ? __ldcs(S + j) : make_int2(0, 0);
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+          if (j0 + threadIdx.x + (uint64_t)u * kThreads >= se) continue;
+          const uint32_t h = table_slot(t[u].x, bits, cap);
+          if (!group(t[u].x, t[u].y, h & ~3u, h & 3u)) {
+            uint32_t g1 = (h & ~3u) + 4;
+            if (g1 >= cap) g1 = 0;
+            queue[atomicAdd(&s_qn[par], 1u)] = make_int4(t[u].x, t[u].y, (int)g1, 0);
+          }
+        }
+        __syncthreads();
+        const uint32_t nq = s_qn[par];
+        if (threadIdx.x == 0) s_qn[par ^ 1] = 0;
+        for (uint32_t i = threadIdx.x; i < nq; i += kThreads) {
+          const int4 e = queue[i];
+          uint32_t g0 = (uint32_t)e.z;
+          for (uint32_t step = 4; step < cap; step += 4) {
+            if (group(e.x, e.y, g0, 0)) break;
             g0 += 4;
             if (g0 >= cap) g0 = 0;
           }
-        } else {
-          uint32_t hh = h;
+        }
+        __syncthreads();
+      }
+    } else {
+      // index table: plain linear probing, one slot per step
+      for (uint64_t j0 = sb + threadIdx.x; j0 < se; j0 += 4 * kThreads) {
+        int2 t[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+          const uint64_t j = j0 + (uint64_t)u * kThreads;
+          t[u] = j < se ? __ldcs(S + j) : make_int2(0, 0);
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+          if (j0 + (uint64_t)u * kThreads >= se) continue;
+          const int32_t k = t[u].x;
+          uint32_t hh = table_slot(k, bits, cap);
           for (uint32_t step = 0; step < cap; ++step) {
             const unsigned short idx = tab[hh];
             if (idx == 0) break;
@@ -457,9 +498,11 @@ __global__ void __launch_bounds__(kThreads, 1)
   gbjd::block_flush(spec, acc, red, out);
 }
 
-template <int kRMax>
+// keys + values table (>= pairs + 16-bit index) and the probe queue of one
+// round (4 probes per thread).
+template <int kRMax, int kThreads>
 constexpr size_t join_smem() {
-  return (size_t)2 * (2 * kRMax + 64) * sizeof(int32_t);  // >= pairs + 16-bit index
+  return (size_t)2 * (2 * kRMax + 64) * sizeof(int32_t) + (size_t)4 * kThreads * sizeof(int4);
 }
 
 template <int kRMax, int kThreads, int kAgg>
@@ -467,7 +510,7 @@ int launch_join(gbj_ctx *ctx, const int2 *R, const uint64_t *ro, const int2 *S,
                 const uint64_t *so, const uint64_t *item_off, uint32_t P, int bits,
                 uint64_t w, uint32_t sentinel_part, const AggSpec &spec, int64_t *out,
                 unsigned long long *ctr, cudaStream_t s) {
-  const size_t smem = join_smem<kRMax>();
+  const size_t smem = join_smem<kRMax, kThreads>();
   auto kern = k_radix_join<kRMax, kThreads, kAgg>;
   GBJ_CHECK_CUDA(ctx, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                            (int)smem));
