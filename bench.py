@@ -1,17 +1,25 @@
-"""Benchmark: radix-partitioned hash join, R = 2^27 unique keys, S = 2^29
-keys (50% hits, hit keys Zipf theta in {0, 0.5, 1.0}), output match count and
-int64 SUM(R.rowid XOR S.rowid).  One step = the three joins (one per theta)
-over resident device columns.
+"""Benchmark of the GB300 relational hot path.
+
+Default workload (the one the driver runs): radix-partitioned hash join,
+R = 2^27 unique keys, S = 2^29 keys (50% hits, hit keys Zipf theta in
+{0, 0.5, 1.0}), output match count and int64 SUM(R.rowid XOR S.rowid).  One
+step = the three joins (one per theta) over resident device columns.
+
+Other workloads (same JSON contract):
+  --workload plain    R = 2^20 permuted keys, S = 2^24 uniform keys,
+                      COUNT and int64 SUM(R.payload * S.payload)
+  --workload groupby  2^29 rows, --card C groups (--theta 0 uniform or Zipf),
+                      COUNT / int64 SUM / MIN / MAX per key
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
 
-Prints ONE JSON line (rank 0).  `value` is probe tuples per second over the
-device-timed steps (inputs resident in HBM); `e2e` repeats the steps with the
-probe and build key columns copied host->device from pinned memory and the
-results copied back inside the timed region.  `--impl reference` times the
-CPU restatement of the reference's join (the oracle port, all host threads)
-on a bounded sample of the same workload.  N > 1 runs independent replicas
-(one per GPU): the join does not shard across GPUs here.
+Prints ONE JSON line (rank 0).  `value` is tuples per second over the
+device-timed steps (inputs resident in HBM); `e2e` repeats the steps with
+the inputs copied host->device from pinned memory and the results copied
+back inside the timed region.  `--impl reference` times the CPU restatement
+of the reference's algorithm (the oracle port, all host threads) on a
+bounded sample of the same workload.  N > 1 runs independent replicas (one
+per GPU): these joins and aggregations do not shard across GPUs here.
 """
 from __future__ import annotations
 
@@ -27,14 +35,7 @@ import time
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
-LOG_R, LOG_S = 27, 29
-THETAS = (0.0, 0.5, 1.0)
-HIT_RATE = 0.5
 SEED = 20260
-METRIC = "probe Gtuples/s"
-UNIT = "Gtuples/s"
-WORKLOAD = "radix-partitioned hash join R=2^27 unique int32 keys, S=2^29 int32 keys " \
-           "(50% hits, Zipf theta 0/0.5/1.0), COUNT + SUM(rowid xor)"
 
 
 def parse():
@@ -43,12 +44,15 @@ def parse():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--log-r", type=int, default=LOG_R)
-    ap.add_argument("--log-s", type=int, default=LOG_S)
+    ap.add_argument("--workload", default="radix", choices=["radix", "plain", "groupby"])
+    ap.add_argument("--log-r", type=int, default=None, help="log2 build rows (joins)")
+    ap.add_argument("--log-s", type=int, default=None, help="log2 probe / input rows")
+    ap.add_argument("--card", type=int, default=1 << 16, help="group-by cardinality")
+    ap.add_argument("--theta", type=float, default=0.0, help="group-by Zipf exponent")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--cpu-sample-log", type=int, default=26,
-                    help="log2 probe rows per theta in the CPU baseline sample")
+                    help="log2 probe / input rows per join in the CPU baseline sample")
     return ap.parse_args()
 
 
@@ -57,15 +61,272 @@ def dist_env():
             int(os.environ.get("WORLD_SIZE", 1)))
 
 
-def gen_inputs(log_r, log_s):
-    from proteus_gb300 import engine
+# ------------------------------------------------------------- workloads
+class RadixJoin:
+    metric, unit = "probe Gtuples/s", "Gtuples/s"
+    THETAS = (0.0, 0.5, 1.0)
 
-    rk, _ = engine.gen_build_side(SEED, 1 << log_r, payload=False)
-    sks = [engine.gen_probe_zipf(SEED + i, 1 << log_s, 1 << log_r, th, HIT_RATE)[0]
-           for i, th in enumerate(THETAS)]
-    return rk, sks
+    def __init__(self, args):
+        self.lr = args.log_r or 27
+        self.ls = args.log_s or 29
+        self.nr, self.ns = 1 << self.lr, 1 << self.ls
+
+    def describe(self):
+        return {"workload": f"radix-partitioned hash join R=2^{self.lr} unique int32 keys, "
+                            f"S=2^{self.ls} int32 keys (50% hits, Zipf theta 0/0.5/1.0), "
+                            f"COUNT + SUM(rowid xor)",
+                "n_build": self.nr, "n_probe": self.ns, "thetas": list(self.THETAS),
+                "hit_rate": 0.5, "l2": "inputs larger than L2 (2 GiB probe keys per join)"}
+
+    def generate(self):
+        from proteus_gb300 import engine
+
+        self.rk, _ = engine.gen_build_side(SEED, self.nr, payload=False)
+        self.sks = [engine.gen_probe_zipf(SEED + i, self.ns, self.nr, th, 0.5)[0]
+                    for i, th in enumerate(self.THETAS)]
+
+    def device(self, ctx):
+        import torch
+
+        from proteus_gb300 import abi
+
+        self.ctx = ctx
+        self.aggs = [(abi.AGG_COUNT, abi.VAL_ONE), (abi.AGG_SUM, abi.VAL_ROWID_XOR)]
+        self.d_r = torch.from_numpy(self.rk).cuda()
+        self.d_s = [torch.from_numpy(s).cuda() for s in self.sks]
+        self.outs = [torch.empty(2, dtype=torch.int64, device="cuda") for _ in self.THETAS]
+
+    def step(self):
+        for ds, o in zip(self.d_s, self.outs):
+            self.ctx.radix_join_agg(self.d_r, None, ds, None, self.aggs, out=o)
+
+    def results(self):
+        return [o.cpu().tolist() for o in self.outs]
+
+    def pin(self):
+        import torch
+
+        self.h_r = torch.from_numpy(self.rk).pin_memory()
+        self.h_s = [torch.from_numpy(s).pin_memory() for s in self.sks]
+        self.h_out = torch.empty((len(self.THETAS), 2), dtype=torch.int64).pin_memory()
+
+    def e2e_step(self):
+        self.d_r.copy_(self.h_r, non_blocking=True)
+        for i, (hs, ds, o) in enumerate(zip(self.h_s, self.d_s, self.outs)):
+            ds.copy_(hs, non_blocking=True)
+            self.ctx.radix_join_agg(self.d_r, None, ds, None, self.aggs, out=o)
+            self.h_out[i].copy_(o, non_blocking=True)
+
+    def e2e_results(self):
+        return self.h_out.tolist()
+
+    def h2d_bytes(self):
+        return 4 * (self.nr + len(self.THETAS) * self.ns)
+
+    def d2h_bytes(self):
+        return 16 * len(self.THETAS)
+
+    def units_per_step(self):
+        return len(self.THETAS) * self.ns
+
+    def kernel_bytes(self, name):
+        """Algorithmic HBM bytes of all launches of `name` in one step."""
+        t = len(self.THETAS) * (self.nr + self.ns)
+        return {"k_pid_hist": 4 * t,            # key read
+                "k_tile_pass": 28 * t,          # pass 1: key read + pair write (12 B),
+                                                # pass 2: pair read + pair write (16 B)
+                "k_radix_join": 8 * t}.get(name)  # partitioned pairs read once
+
+    def extra(self, ms, steps, peak):
+        comp = 4 * (self.nr + self.ns) * len(self.THETAS) * steps
+        return {"job_hbm_gbs_compulsory": round(comp / (ms / 1e3) / 1e9, 1),
+                "job_frac_compulsory": round(comp / (ms / 1e3) / 1e9 / peak, 4),
+                "build_plus_probe_gtuples_s": round(len(self.THETAS) * (self.nr + self.ns) * steps
+                                                    / (ms / 1e3) / 1e9, 3)}
+
+    def cpu(self, threads, sample_log):
+        from oracle import oracle as O
+
+        ns = 1 << min(sample_log, self.ls)
+        aggs = [(0, 0), (1, 6)]
+        t0 = time.perf_counter()
+        for sk in self.sks:
+            O.radix_join_agg(self.rk, None, sk[:ns], None, aggs, threads=threads)
+        dt = time.perf_counter() - t0
+        return len(self.THETAS) * ns, dt, (f"full R (2^{self.lr}), first {ns} rows of each S "
+                                           f"(theta 0/0.5/1.0); oracle C port of the reference's "
+                                           f"partitioned chained-hash join, {threads} threads")
 
 
+class PlainJoin:
+    metric, unit = "probe Gtuples/s", "Gtuples/s"
+
+    def __init__(self, args):
+        self.lr = args.log_r or 20
+        self.ls = args.log_s or 24
+        self.nr, self.ns = 1 << self.lr, 1 << self.ls
+
+    def describe(self):
+        return {"workload": f"plain hash join R=2^{self.lr} (permuted keys, payload U[0,1000)), "
+                            f"S=2^{self.ls} (keys U{{1..2^{self.lr}}}), COUNT + SUM(R.p*S.p)",
+                "n_build": self.nr, "n_probe": self.ns,
+                "l2": "probe columns (128 MiB) larger than L2"}
+
+    def generate(self):
+        from proteus_gb300 import engine
+
+        self.rk, self.rp = engine.gen_build_side(SEED, self.nr)
+        self.sk, self.sp = engine.gen_probe_uniform(SEED, self.ns, self.nr)
+
+    def device(self, ctx):
+        import torch
+
+        from proteus_gb300 import abi
+
+        self.ctx = ctx
+        self.aggs = [(abi.AGG_COUNT, abi.VAL_ONE), (abi.AGG_SUM, abi.VAL_PRODUCT)]
+        self.d = [torch.from_numpy(a).cuda() for a in (self.rk, self.rp, self.sk, self.sp)]
+        self.out = torch.empty(2, dtype=torch.int64, device="cuda")
+
+    def step(self):
+        t = self.ctx.join_build(self.d[0], self.d[1])
+        self.ctx.join_probe_agg(t, self.d[2], self.d[3], self.aggs, out=self.out)
+        t.destroy()
+
+    def results(self):
+        return self.out.cpu().tolist()
+
+    def pin(self):
+        import torch
+
+        self.h = [torch.from_numpy(a).pin_memory() for a in (self.rk, self.rp, self.sk, self.sp)]
+        self.h_out = torch.empty(2, dtype=torch.int64).pin_memory()
+
+    def e2e_step(self):
+        for h, d in zip(self.h, self.d):
+            d.copy_(h, non_blocking=True)
+        self.step()
+        self.h_out.copy_(self.out, non_blocking=True)
+
+    def e2e_results(self):
+        return self.h_out.tolist()
+
+    def h2d_bytes(self):
+        return 8 * (self.nr + self.ns)
+
+    def d2h_bytes(self):
+        return 16
+
+    def units_per_step(self):
+        return self.ns
+
+    def kernel_bytes(self, name):
+        return {"k_join_probe_agg": 8 * self.ns,   # probe key + payload
+                "k_join_build": 12 * self.nr}.get(name)  # key read + slot write
+
+    def extra(self, ms, steps, peak):
+        comp = 8 * (self.nr + self.ns) * steps
+        return {"job_hbm_gbs_compulsory": round(comp / (ms / 1e3) / 1e9, 1),
+                "job_frac_compulsory": round(comp / (ms / 1e3) / 1e9 / peak, 4)}
+
+    def cpu(self, threads, sample_log):
+        from oracle import oracle as O
+
+        t0 = time.perf_counter()
+        O.join_agg(self.rk, self.rp, self.sk, self.sp, [(0, 0), (1, 3)], threads=threads)
+        dt = time.perf_counter() - t0
+        return self.ns, dt, (f"full workload; oracle C port of HashJoinChained "
+                             f"(multi-worker build, {threads} threads)")
+
+
+class GroupBy:
+    metric, unit = "group-by Gtuples/s", "Gtuples/s"
+
+    def __init__(self, args):
+        self.ls = args.log_s or 29
+        self.n = 1 << self.ls
+        self.card, self.theta = args.card, args.theta
+
+    def describe(self):
+        return {"workload": f"hash group-by 2^{self.ls} rows, {self.card} groups "
+                            f"({'Zipf %.1f' % self.theta if self.theta else 'uniform'}), "
+                            f"int32 value U[-2^20,2^20): COUNT, SUM int64, MIN, MAX",
+                "rows": self.n, "cardinality": self.card, "theta": self.theta,
+                "l2": "inputs (4 GiB) larger than L2"}
+
+    def generate(self):
+        from proteus_gb300 import engine
+
+        self.k, self.v = engine.gen_groupby(SEED, self.n, self.card, self.theta)
+
+    def device(self, ctx):
+        import torch
+
+        self.ctx = ctx
+        self.dk, self.dv = torch.from_numpy(self.k).cuda(), torch.from_numpy(self.v).cuda()
+        self.cap = self.card + 16
+        self.res = None
+
+    def step(self):
+        self.res = self.ctx.groupby(self.dk, self.dv, self.cap, expected_groups=self.card)
+
+    def results(self):
+        return int(self.res[5].cpu()[0])
+
+    def pin(self):
+        import torch
+
+        self.hk = torch.from_numpy(self.k).pin_memory()
+        self.hv = torch.from_numpy(self.v).pin_memory()
+        self.h_out = [torch.empty(self.cap, dtype=t).pin_memory() for t in
+                      (torch.int32, torch.int64, torch.int64, torch.int32, torch.int32)]
+        self.h_n = torch.empty(1, dtype=torch.int64).pin_memory()
+
+    def e2e_step(self):
+        self.dk.copy_(self.hk, non_blocking=True)
+        self.dv.copy_(self.hv, non_blocking=True)
+        self.step()
+        for h, d in zip(self.h_out, self.res[:5]):
+            h.copy_(d, non_blocking=True)
+        self.h_n.copy_(self.res[5], non_blocking=True)
+
+    def e2e_results(self):
+        return int(self.h_n[0])
+
+    def h2d_bytes(self):
+        return 8 * self.n
+
+    def d2h_bytes(self):
+        return 28 * self.cap + 8
+
+    def units_per_step(self):
+        return self.n
+
+    def kernel_bytes(self, name):
+        return {"k_groupby": 8 * self.n,       # (key, value) per row, raw or partitioned
+                "k_pid_hist": 4 * self.n,      # key read
+                "k_tile_pass": 16 * self.n}.get(name)  # per pass: pair read + pair write
+
+    def extra(self, ms, steps, peak):
+        comp = 8 * self.n * steps
+        return {"job_hbm_gbs_compulsory": round(comp / (ms / 1e3) / 1e9, 1),
+                "job_frac_compulsory": round(comp / (ms / 1e3) / 1e9 / peak, 4)}
+
+    def cpu(self, threads, sample_log):
+        from oracle import oracle as O
+
+        n = 1 << min(sample_log + 1, self.ls)
+        t0 = time.perf_counter()
+        O.groupby(self.k[:n], self.v[:n], threads=threads)
+        dt = time.perf_counter() - t0
+        return n, dt, (f"first {n} rows; oracle C port of HashGroupByChained "
+                       f"(hash-partitioned per thread), {threads} threads")
+
+
+WORKLOADS = {"radix": RadixJoin, "plain": PlainJoin, "groupby": GroupBy}
+
+
+# ------------------------------------------------------------- helpers
 class ClockSampler:
     """nvidia-smi clocks / throttle reasons sampled during the timed region."""
 
@@ -125,19 +386,9 @@ def hbm_peak():
         return 6800.0, "fallback"
 
 
-def kernel_bytes(name, n_r, n_s):
-    """Algorithmic HBM bytes of one join's launches of `name` (all launches
-    of that kernel in one join together), per the kernel's definition."""
-    tuples = n_r + n_s
-    return {"k_pid_hist": 4 * tuples,          # key read
-            "k_tile_pass": 28 * tuples,        # pass 1: key read + pair write (12 B),
-                                               # pass 2: pair read + pair write (16 B)
-            "k_radix_join": 8 * tuples}.get(name)  # partitioned pairs read once
-
-
-def traffic_from_profiles(kernel):
+def traffic_from_profiles(workload, kernel):
     """Per-launch DRAM bytes of `kernel` from the committed ncu summary."""
-    path = os.path.join(ROOT, "profiles", "radix_join_traffic.json")
+    path = os.path.join(ROOT, "profiles", f"{workload}_traffic.json")
     try:
         with open(path) as f:
             d = json.load(f)
@@ -146,21 +397,7 @@ def traffic_from_profiles(kernel):
         return None
 
 
-def cpu_baseline(rk, sks, sample_log, threads):
-    from oracle import oracle as O
-    from proteus_gb300 import abi
-
-    aggs = [(abi.AGG_COUNT, abi.VAL_ONE), (abi.AGG_SUM, abi.VAL_ROWID_XOR)]
-    ns = 1 << sample_log
-    t0 = time.perf_counter()
-    tuples = 0
-    for sk in sks:
-        O.radix_join_agg(rk, None, sk[:ns], None, aggs, threads=threads)
-        tuples += ns
-    dt = time.perf_counter() - t0
-    return tuples / dt / 1e9, dt
-
-
+# ------------------------------------------------------------- arms
 def run_reference(args):
     rank, _, world = dist_env()
     if rank != 0:
@@ -168,29 +405,26 @@ def run_reference(args):
     from oracle import oracle as O
 
     O.build()
+    wl = WORKLOADS[args.workload](args)
+    wl.generate()
     threads = os.cpu_count() or 1
-    rk, sks = gen_inputs(args.log_r, args.log_s)
-    sample = min(args.cpu_sample_log, args.log_s)
     for _ in range(args.warmup):
-        cpu_baseline(rk, sks, sample, threads)
-    times, vals = [], []
+        wl.cpu(threads, args.cpu_sample_log)
+    units, secs, sample = 0, 0.0, ""
     for _ in range(args.steps):
-        v, dt = cpu_baseline(rk, sks, sample, threads)
-        vals.append(v)
-        times.append(dt)
-    value = (len(THETAS) << sample) * args.steps / sum(times) / 1e9
+        u, dt, sample = wl.cpu(threads, args.cpu_sample_log)
+        units += u
+        secs += dt
+    value = units / secs / 1e9
     line = {
-        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * sum(times) / args.steps,
-        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32",
-        "data": "synthetic (seeded generator)",
-        "config": {"workload": WORKLOAD, "n_build": 1 << args.log_r, "n_probe": 1 << args.log_s,
-                   "sample_probe_rows_per_theta": 1 << sample},
-        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
-                         "sample": f"full R (2^{args.log_r}), first 2^{sample} rows of each S "
-                                   f"(theta 0/0.5/1.0); oracle C port of the reference's "
-                                   f"partitioned chained-hash join, {threads} threads"},
-        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "impl": "reference", "metric": wl.metric, "value": value, "unit": wl.unit,
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1e3 * secs / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "int32", "data": "synthetic (seeded generator)",
+        "config": wl.describe(),
+        "cpu_baseline": {"value": value, "unit": wl.unit, "cores": threads, "kind": "port",
+                         "sample": sample},
+        "e2e": {"value": value, "unit": wl.unit, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
 
@@ -204,30 +438,30 @@ def run_gpu(args):
         import torch.distributed as dist
 
         dist.init_process_group("nccl")
-    from proteus_gb300 import abi, engine
+    from proteus_gb300 import engine
 
-    n_r, n_s = 1 << args.log_r, 1 << args.log_s
-    rk, sks = gen_inputs(args.log_r, args.log_s)
+    wl = WORKLOADS[args.workload](args)
+    wl.generate()
     stream = torch.cuda.current_stream()
-    d_r = torch.from_numpy(rk).cuda()
-    d_s = [torch.from_numpy(s).cuda() for s in sks]
     ctx = engine.Context(local_rank, pool_bytes=24 << 30)
-    aggs = [(abi.AGG_COUNT, abi.VAL_ONE), (abi.AGG_SUM, abi.VAL_ROWID_XOR)]
-    outs = [torch.empty(2, dtype=torch.int64, device="cuda") for _ in THETAS]
-
-    def step():
-        for ds, o in zip(d_s, outs):
-            ctx.radix_join_agg(d_r, None, ds, None, aggs, out=o)
+    wl.device(ctx)
 
     for _ in range(args.warmup):
-        step()
+        wl.step()
     ctx.sync()
-    results = [o.cpu().tolist() for o in outs]
+    results = wl.results()
 
     def barrier():
         if world > 1:
             torch.distributed.barrier()
         torch.cuda.synchronize()
+
+    def max_over_ranks(ms):
+        if world > 1:
+            t = torch.tensor([ms], device="cuda")
+            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+            ms = float(t.item())
+        return ms
 
     # ---- device-timed steps (inputs resident) ----
     clocks = ClockSampler(local_rank)
@@ -238,101 +472,69 @@ def run_gpu(args):
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e0.record(stream)
     for _ in range(args.steps):
-        step()
+        wl.step()
     e1.record(stream)
     barrier()
-    ms = e0.elapsed_time(e1)
+    ms = max_over_ranks(e0.elapsed_time(e1))
     launches = ctx.launches() - launches0
     prof = ctx.profile_dump()
     ctx.profile(False)
     clk = clocks.stop()
     ctx.sync()
-    if world > 1:
-        t = torch.tensor([ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
-    value = world * len(THETAS) * n_s * args.steps / (ms / 1e3) / 1e9
+    value = world * wl.units_per_step() * args.steps / (ms / 1e3) / 1e9
 
     # ---- roofline of the dominant kernel ----
-    dom = max(prof.items(), key=lambda kv: kv[1][1])
-    dom_name, (dom_launches, dom_ms) = dom
-    joins = len(THETAS) * args.steps
-    per_join = kernel_bytes(dom_name, n_r, n_s)
     peak, peak_kind = hbm_peak()
+    dom_name, (dom_launches, dom_ms) = max(prof.items(), key=lambda kv: kv[1][1])
+    per_step = wl.kernel_bytes(dom_name)
     roof = None
-    if per_join is not None:
-        achieved = per_join * joins / (dom_ms / 1e3) / 1e9
-        per_launch_bytes = per_join * joins / dom_launches
-        traffic = traffic_from_profiles(dom_name)
+    if per_step is not None:
+        achieved = per_step * args.steps / (dom_ms / 1e3) / 1e9
         roof = {"bound": "hbm", "kernel": dom_name, "achieved": round(achieved, 1),
                 "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 4),
-                "peak_source": peak_kind, "traffic": traffic,
-                "algorithmic_bytes_per_launch": per_launch_bytes,
+                "peak_source": peak_kind, "traffic": traffic_from_profiles(args.workload, dom_name),
+                "algorithmic_bytes_per_launch": per_step * args.steps / dom_launches,
                 "avg_launch_ms": dom_ms / dom_launches}
-    kernels = {k: {"launches": v[0], "ms_total": round(v[1], 3),
-                   "share": round(v[1] / sum(x[1] for x in prof.values()), 4)}
+    total = sum(x[1] for x in prof.values())
+    kernels = {k: {"launches": v[0], "ms_total": round(v[1], 3), "share": round(v[1] / total, 4)}
                for k, v in sorted(prof.items(), key=lambda kv: -kv[1][1])}
-    compulsory = 4 * (n_r + n_s)  # key bytes of one join
 
     # ---- end to end through the API with host buffers ----
     e2e = None
     if not args.no_e2e:
-        h_r = torch.from_numpy(rk).pin_memory()
-        h_s = [torch.from_numpy(s).pin_memory() for s in sks]
-        h_out = torch.empty((len(THETAS), 2), dtype=torch.int64).pin_memory()
-
-        def e2e_step():
-            d_r.copy_(h_r, non_blocking=True)
-            for i, (hs, ds, o) in enumerate(zip(h_s, d_s, outs)):
-                ds.copy_(hs, non_blocking=True)
-                ctx.radix_join_agg(d_r, None, ds, None, aggs, out=o)
-                h_out[i].copy_(o, non_blocking=True)
-
+        wl.pin()
         for _ in range(max(1, args.warmup)):
-            e2e_step()
+            wl.e2e_step()
         barrier()
         f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         f0.record(stream)
         for _ in range(args.steps):
-            e2e_step()
+            wl.e2e_step()
         f1.record(stream)
         barrier()
-        ems = f0.elapsed_time(f1)
-        if world > 1:
-            t = torch.tensor([ems], device="cuda")
-            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-            ems = float(t.item())
-        assert h_out.tolist() == results, "e2e results differ from resident results"
-        e2e = {"value": world * len(THETAS) * n_s * args.steps / (ems / 1e3) / 1e9, "unit": UNIT,
-               "h2d_bytes_per_step": 4 * (n_r + len(THETAS) * n_s),
-               "d2h_bytes_per_step": 16 * len(THETAS), "ms_per_step": ems / args.steps}
+        ems = max_over_ranks(f0.elapsed_time(f1))
+        assert wl.e2e_results() == results, "e2e results differ from resident results"
+        e2e = {"value": world * wl.units_per_step() * args.steps / (ems / 1e3) / 1e9,
+               "unit": wl.unit, "h2d_bytes_per_step": wl.h2d_bytes(),
+               "d2h_bytes_per_step": wl.d2h_bytes(), "ms_per_step": ems / args.steps}
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
         threads = os.cpu_count() or 1
-        sample = min(args.cpu_sample_log, args.log_s)
-        v, dt = cpu_baseline(rk, sks, sample, threads)
-        cpu = {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
-               "sample": f"full R (2^{args.log_r}), first 2^{sample} rows of each S "
-                         f"(theta 0/0.5/1.0), {dt:.1f} s; oracle C port of the reference's "
-                         f"partitioned chained-hash join, {threads} threads"}
+        u, dt, sample = wl.cpu(threads, args.cpu_sample_log)
+        cpu = {"value": u / dt / 1e9, "unit": wl.unit, "cores": threads, "kind": "port",
+               "sample": f"{sample}; {dt:.1f} s"}
 
     if rank == 0:
+        cfg = wl.describe()
+        cfg["parallelism"] = f"replicas x{world}"
         line = {
-            "metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": world,
+            "metric": wl.metric, "value": round(value, 3), "unit": wl.unit, "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32",
-            "data": "synthetic (seeded generator)",
-            "config": {"workload": WORKLOAD, "n_build": n_r, "n_probe": n_s,
-                       "thetas": list(THETAS), "hit_rate": HIT_RATE,
-                       "parallelism": f"replicas x{world}",
-                       "l2": "inputs larger than L2 (2 GiB probe keys per join)"},
+            "data": "synthetic (seeded generator)", "config": cfg,
             "e2e": e2e, "roofline": roof, "cpu_baseline": cpu, "clocks": clk,
-            "gpu_launches": launches,
-            "job_hbm_gbs_compulsory": round(compulsory * joins / (ms / 1e3) / 1e9, 1),
-            "job_frac_compulsory": round(compulsory * joins / (ms / 1e3) / 1e9 / peak, 4),
-            "build_plus_probe_gtuples_s": round(world * len(THETAS) * (n_r + n_s) * args.steps
-                                                / (ms / 1e3) / 1e9, 3),
+            "gpu_launches": launches, **wl.extra(ms, args.steps, peak),
             "kernels": kernels, "results": results,
         }
         print(json.dumps(line), flush=True)

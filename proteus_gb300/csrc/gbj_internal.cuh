@@ -188,18 +188,27 @@ struct Acc {
 #pragma unroll
     for (int j = 0; j < GBJ_MAX_AGGS; ++j) v[j] = j < s.n ? agg_identity(s.op[j]) : 0;
   }
+  // Branch-free: operand and op are selected with predicated moves, so a
+  // match costs a few instructions per aggregate and no jump tables.
   __device__ __forceinline__ void update(const gbj::AggSpec &s, int32_t key,
                                          int64_t bval, int64_t pval,
                                          int64_t brow, int64_t prow) {
+    const int64_t prod = bval * pval, xr = brow ^ prow;
 #pragma unroll
     for (int j = 0; j < GBJ_MAX_AGGS; ++j) {
       if (j < s.n) {
-        int64_t x = operand_value(s.operand[j], key, bval, pval, brow, prow);
-        int op = s.op[j];
-        if (op == GBJ_AGG_COUNT) v[j] += 1;
-        else if (op == GBJ_AGG_SUM) v[j] += x;
-        else if (op == GBJ_AGG_MIN) v[j] = x < v[j] ? x : v[j];
-        else v[j] = x > v[j] ? x : v[j];
+        const int o = s.operand[j];
+        int64_t x = o == GBJ_VAL_BUILD ? bval : 1;
+        x = o == GBJ_VAL_PROBE ? pval : x;
+        x = o == GBJ_VAL_PRODUCT ? prod : x;
+        x = o == GBJ_VAL_BUILD_ROWID ? brow : x;
+        x = o == GBJ_VAL_PROBE_ROWID ? prow : x;
+        x = o == GBJ_VAL_ROWID_XOR ? xr : x;
+        x = o == GBJ_VAL_BUILD_KEY ? (int64_t)key : x;
+        const int op = s.op[j];
+        const int64_t add = v[j] + (op == GBJ_AGG_COUNT ? 1 : x);
+        const int64_t mm = op == GBJ_AGG_MIN ? (x < v[j] ? x : v[j]) : (x > v[j] ? x : v[j]);
+        v[j] = op <= GBJ_AGG_SUM ? add : mm;
       }
     }
   }

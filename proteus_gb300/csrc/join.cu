@@ -58,10 +58,13 @@ __global__ void __launch_bounds__(kThreads)
   }
 }
 
+enum : int { kAggGeneric = 0, kAggCountXor = 1, kAggCountProduct = 2 };
+
 // Probe with fused aggregate.  Four probe keys per thread: their first slot
 // loads are issued together so each thread keeps several L2 requests in
-// flight; chains past the first slot are walked afterwards.
-template <bool kVec>
+// flight; chains past the first slot are walked afterwards.  kAgg selects
+// a specialised accumulator for the two aggregate lists the workloads use.
+template <bool kVec, int kAgg>
 __global__ void __launch_bounds__(kThreads)
     k_join_probe_agg(const int32_t *__restrict__ keys,
                      const int32_t *__restrict__ pay, uint64_t n,
@@ -72,17 +75,29 @@ __global__ void __launch_bounds__(kThreads)
   __shared__ int64_t red[32 * GBJ_MAX_AGGS];
   gbjd::Acc acc;
   acc.init(spec);
+  int64_t a_cnt = 0, a_sum = 0;
   const bool unique = meta[0] == 0;
   const uint64_t nq = n / 4;
   const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  auto match = [&](int32_t k, int64_t pv, uint64_t prow, uint64_t e) {
+    const uint32_t r = slot_row(e);
+    if (kAgg == kAggCountXor) {
+      a_cnt += 1;
+      a_sum += (int64_t)r ^ (int64_t)prow;
+    } else if (kAgg == kAggCountProduct) {
+      a_cnt += 1;
+      a_sum += (int64_t)__ldg(&bpay[r]) * pv;
+    } else {
+      const int64_t bv = bpay ? __ldg(&bpay[r]) : 0;
+      acc.update(spec, k, bv, pv, r, prow);
+    }
+  };
   auto probe_one = [&](int32_t k, int64_t pv, uint64_t prow, uint64_t h,
                        uint64_t e) {
     for (uint64_t step = 0; step <= mask; ++step) {
       if (e == 0) break;
       if (slot_key(e) == k) {
-        const uint32_t r = slot_row(e);
-        const int64_t bv = bpay ? __ldg(&bpay[r]) : 0;
-        acc.update(spec, k, bv, pv, r, prow);
+        match(k, pv, prow, e);
         if (unique) break;
       }
       h = (h + 1) & mask;
@@ -118,6 +133,10 @@ __global__ void __launch_bounds__(kThreads)
       const uint64_t h = gbjd::fmix32((uint32_t)k) & mask;
       probe_one(k, pay ? pay[i] : 0, i, h, __ldg(&slots[h]));
     }
+  }
+  if (kAgg != kAggGeneric) {
+    acc.v[0] = a_cnt;
+    acc.v[1] = a_sum;
   }
   gbjd::block_flush(spec, acc, red, out);
 }
@@ -250,6 +269,33 @@ int grid_for(gbj_ctx *ctx, uint64_t work, int threads, int per_sm = 4) {
   return grid_for_sms(ctx->sm_count, work, threads, per_sm);
 }
 
+// Picks the probe kernel: int4 loads when both probe columns are 16-byte
+// aligned, and a specialised accumulator for COUNT + SUM(product / xor).
+void launch_probe(int sm_count, const int32_t *keys, const int32_t *pay, uint64_t n,
+                  const uint64_t *slots, uint64_t mask, const int32_t *bpay,
+                  const uint32_t *meta, const gbj::AggSpec &spec, int64_t *out,
+                  cudaStream_t s) {
+  const bool vec = ((uintptr_t)keys % 16 == 0) && (!pay || (uintptr_t)pay % 16 == 0);
+  const bool two = spec.n == 2 && spec.op[0] == GBJ_AGG_COUNT && spec.op[1] == GBJ_AGG_SUM;
+  const int agg = two && spec.operand[1] == GBJ_VAL_ROWID_XOR ? kAggCountXor
+                  : two && spec.operand[1] == GBJ_VAL_PRODUCT ? kAggCountProduct
+                                                              : kAggGeneric;
+  const int gv = grid_for_sms(sm_count, (n + 3) / 4, kThreads);
+  const int gs = grid_for_sms(sm_count, n, kThreads);
+#define GBJ_PROBE(V, A) \
+  k_join_probe_agg<V, A><<<V ? gv : gs, kThreads, 0, s>>>(keys, pay, n, slots, mask, bpay, meta, spec, out)
+  if (vec) {
+    if (agg == kAggCountXor) GBJ_PROBE(true, kAggCountXor);
+    else if (agg == kAggCountProduct) GBJ_PROBE(true, kAggCountProduct);
+    else GBJ_PROBE(true, kAggGeneric);
+  } else {
+    if (agg == kAggCountXor) GBJ_PROBE(false, kAggCountXor);
+    else if (agg == kAggCountProduct) GBJ_PROBE(false, kAggCountProduct);
+    else GBJ_PROBE(false, kAggGeneric);
+  }
+#undef GBJ_PROBE
+}
+
 // ------------------------------------------------ allocation-free variant
 // Hash table of gbj_join_agg_noalloc: a fixed array in the module's device
 // memory, so that entry point never allocates.  Slots for build sides of up
@@ -365,15 +411,8 @@ int gbj_join_probe_agg(gbj_ctx *ctx, const gbj_table *t, const int32_t *d_keys,
   GBJ_TRY(init_agg_out(ctx, spec, d_out, s));
   if (n == 0) return GBJ_OK;
   const uint32_t *meta = (const uint32_t *)(t->slots + t->mask + 1);
-  const bool vec = ((uintptr_t)d_keys % 16 == 0) &&
-                   (!d_payload || (uintptr_t)d_payload % 16 == 0);
-  if (vec) {
-    k_join_probe_agg<true><<<grid_for(ctx, (n + 3) / 4, kThreads), kThreads, 0, s>>>(
-        d_keys, d_payload, n, t->slots, t->mask, t->payload, meta, spec, d_out);
-  } else {
-    k_join_probe_agg<false><<<grid_for(ctx, n, kThreads), kThreads, 0, s>>>(
-        d_keys, d_payload, n, t->slots, t->mask, t->payload, meta, spec, d_out);
-  }
+  launch_probe(ctx->sm_count, d_keys, d_payload, n, t->slots, t->mask, t->payload, meta, spec,
+               d_out, s);
   return after_launch(ctx, "k_join_probe_agg", s);
 }
 
@@ -515,16 +554,9 @@ int gbj_join_agg_noalloc(const int32_t *d_build_keys, const int32_t *d_build_pay
   if (n_build)
     k_join_build<<<grid_for_sms(d.sm_count, n_build, kThreads), kThreads, 0, s>>>(
         d_build_keys, n_build, table, slots - 1, meta, status);
-  if (n_probe) {
-    const bool vec = ((uintptr_t)d_probe_keys % 16 == 0) &&
-                     (!d_probe_payload || (uintptr_t)d_probe_payload % 16 == 0);
-    if (vec)
-      k_join_probe_agg<true><<<grid_for_sms(d.sm_count, (n_probe + 3) / 4, kThreads), kThreads, 0, s>>>(
-          d_probe_keys, d_probe_payload, n_probe, table, slots - 1, d_build_payload, meta, spec, d_out);
-    else
-      k_join_probe_agg<false><<<grid_for_sms(d.sm_count, n_probe, kThreads), kThreads, 0, s>>>(
-          d_probe_keys, d_probe_payload, n_probe, table, slots - 1, d_build_payload, meta, spec, d_out);
-  }
+  if (n_probe)
+    launch_probe(d.sm_count, d_probe_keys, d_probe_payload, n_probe, table, slots - 1,
+                 d_build_payload, meta, spec, d_out, s);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return noalloc_fail(GBJ_ERR_CUDA, cudaGetErrorString(e));
   return GBJ_OK;
