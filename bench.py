@@ -44,7 +44,7 @@ def parse():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--workload", default="radix", choices=["radix", "plain", "groupby"])
+    ap.add_argument("--workload", default="radix", choices=["radix", "plain", "groupby", "star"])
     ap.add_argument("--log-r", type=int, default=None, help="log2 build rows (joins)")
     ap.add_argument("--log-s", type=int, default=None, help="log2 probe / input rows")
     ap.add_argument("--card", type=int, default=1 << 16, help="group-by cardinality")
@@ -323,7 +323,139 @@ class GroupBy:
                        f"(hash-partitioned per thread), {threads} threads")
 
 
-WORKLOADS = {"radix": RadixJoin, "plain": PlainJoin, "groupby": GroupBy}
+class StarBatch:
+    """64 star-join query variants over a 2^28-row fact table, all in one
+    graph replay sharing the fact scan (one step = one batch)."""
+    metric, unit, scale = "star-join queries/s", "queries/s", 1.0
+
+    def __init__(self, args):
+        self.lf = args.log_s or 28
+        self.nq = 64
+
+    def describe(self):
+        return {"workload": f"batched star join: fact 2^{self.lf} rows (4 int32 FKs into dims of "
+                            f"2^21, 2557, 2^18, 2^16 rows, quantity, price), {self.nq} seeded "
+                            f"query variants (3 joins, 1/5-1/50 predicates per dimension, group-by "
+                            f"2 dimension attributes, SUM int64 price*quantity) in one launch "
+                            f"sequence replayed from a CUDA graph",
+                "fact_rows": 1 << self.lf, "queries_per_batch": self.nq,
+                "l2": "fact columns (6 GiB) larger than L2"}
+
+    def generate(self):
+        from proteus_gb300 import star
+
+        self.data = star.gen_star(SEED, n_fact=1 << self.lf)
+        self.queries = star.gen_queries(SEED, self.nq, self.data.dims)
+
+    def device(self, ctx):
+        from proteus_gb300 import star
+
+        self.ctx = ctx
+        self.plan = star.StarPlan(ctx, self.data)
+        self.out = self.plan.new_output(self.nq)
+
+    def step(self):
+        self.plan.run(self.queries, self.out, use_graph=True)
+
+    def _digest(self, cnt, sm, n):
+        return int(n.sum()) * 1000003 + int(cnt.sum()) * 7 + int(sm.sum() % 1000000007)
+
+    def results(self):
+        return self._digest(self.out["count"].cpu().numpy() * (self._valid_mask()),
+                            self.out["sum"].cpu().numpy() * (self._valid_mask()),
+                            self.out["n"].cpu().numpy())
+
+    def _valid_mask(self):
+        import numpy as np
+
+        n = self.out["n"].cpu().numpy()
+        cap = self.out["cap"]
+        m = np.zeros(self.nq * cap, dtype=np.int64)
+        for q in range(self.nq):
+            m[q * cap:q * cap + int(n[q])] = 1
+        return m
+
+    def pin(self):
+        import torch
+
+        self.h_fk = [torch.from_numpy(c).pin_memory() for c in self.data.fk]
+        self.h_qty = torch.from_numpy(self.data.quantity).pin_memory()
+        self.h_price = torch.from_numpy(self.data.price).pin_memory()
+        self.h_out = {k: torch.empty_like(self.out[k], device="cpu").pin_memory()
+                      for k in ("a", "b", "count", "sum", "n")}
+
+    def e2e_step(self):
+        for d, h in zip(self.plan.dev_fk, self.h_fk):
+            d.copy_(h, non_blocking=True)
+        self.plan.dev_qty.copy_(self.h_qty, non_blocking=True)
+        self.plan.dev_price.copy_(self.h_price, non_blocking=True)
+        self.step()
+        for k, h in self.h_out.items():
+            h.copy_(self.out[k], non_blocking=True)
+
+    def e2e_results(self):
+        import numpy as np
+
+        n = self.h_out["n"].numpy()
+        cap = self.out["cap"]
+        m = np.zeros(self.nq * cap, dtype=np.int64)
+        for q in range(self.nq):
+            m[q * cap:q * cap + int(n[q])] = 1
+        return self._digest(self.h_out["count"].numpy() * m, self.h_out["sum"].numpy() * m, n)
+
+    def h2d_bytes(self):
+        return 24 * (1 << self.lf)
+
+    def d2h_bytes(self):
+        return sum(t.numel() * t.element_size() for t in self.h_out.values())
+
+    def units_per_step(self):
+        return self.nq
+
+    def kernel_bytes(self, name):
+        fact = 24 * (1 << self.lf)  # 4 FKs + quantity + price, read once per batch
+        return {"star_graph": fact, "k_star_fact": fact}.get(name)
+
+    def extra(self, ms, steps, peak):
+        import torch
+
+        # the plain form: one query per launch sequence (each scans the fact)
+        outs = self.plan.new_output(1)
+        for q in self.queries[:2]:
+            self.plan.run([q], outs, use_graph=False)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for q in self.queries:
+            self.plan.run([q], outs, use_graph=False)
+        e1.record()
+        torch.cuda.synchronize()
+        plain_ms = e0.elapsed_time(e1)
+        batched_qps = self.nq * steps / (ms / 1e3)
+        plain_qps = self.nq / (plain_ms / 1e3)
+        comp = 24 * (1 << self.lf) * steps
+        return {"fact_gtuples_per_s": round((1 << self.lf) * steps / (ms / 1e3) / 1e9, 2),
+                "job_hbm_gbs_compulsory": round(comp / (ms / 1e3) / 1e9, 1),
+                "job_frac_compulsory": round(comp / (ms / 1e3) / 1e9 / peak, 4),
+                "plain_one_query_per_launch_qps": round(plain_qps, 1),
+                "batched_over_plain": round(batched_qps / plain_qps, 2)}
+
+    def cpu(self, threads, sample_log):
+        from oracle import oracle as O
+
+        rows = 1 << min(sample_log + 2, self.lf)
+        nq = 8
+        t0 = time.perf_counter()
+        for q in self.queries[:nq]:
+            O.star_query(self.data, q, threads=threads, rows=rows)
+        dt = time.perf_counter() - t0
+        equiv = nq * rows / (1 << self.lf)  # full-size queries the sample amounts to
+        return equiv, dt, (f"{nq} queries over the first {rows} fact rows (counted as {equiv:.4f} "
+                           f"full-size queries); oracle C port of select -> HashJoinChained x3 -> "
+                           f"HashGroupByChained, one query at a time, {threads} threads")
+
+
+WORKLOADS = {"radix": RadixJoin, "plain": PlainJoin, "groupby": GroupBy, "star": StarBatch}
 
 
 # ------------------------------------------------------------- helpers
@@ -415,7 +547,7 @@ def run_reference(args):
         u, dt, sample = wl.cpu(threads, args.cpu_sample_log)
         units += u
         secs += dt
-    value = units / secs / 1e9
+    value = units / secs / getattr(wl, "scale", 1e9)
     line = {
         "impl": "reference", "metric": wl.metric, "value": value, "unit": wl.unit,
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
@@ -481,7 +613,8 @@ def run_gpu(args):
     ctx.profile(False)
     clk = clocks.stop()
     ctx.sync()
-    value = world * wl.units_per_step() * args.steps / (ms / 1e3) / 1e9
+    scale = getattr(wl, "scale", 1e9)
+    value = world * wl.units_per_step() * args.steps / (ms / 1e3) / scale
 
     # ---- roofline of the dominant kernel ----
     peak, peak_kind = hbm_peak()
@@ -514,7 +647,7 @@ def run_gpu(args):
         barrier()
         ems = max_over_ranks(f0.elapsed_time(f1))
         assert wl.e2e_results() == results, "e2e results differ from resident results"
-        e2e = {"value": world * wl.units_per_step() * args.steps / (ems / 1e3) / 1e9,
+        e2e = {"value": world * wl.units_per_step() * args.steps / (ems / 1e3) / scale,
                "unit": wl.unit, "h2d_bytes_per_step": wl.h2d_bytes(),
                "d2h_bytes_per_step": wl.d2h_bytes(), "ms_per_step": ems / args.steps}
 
@@ -522,7 +655,7 @@ def run_gpu(args):
     if rank == 0 and world == 1 and not args.no_cpu:
         threads = os.cpu_count() or 1
         u, dt, sample = wl.cpu(threads, args.cpu_sample_log)
-        cpu = {"value": u / dt / 1e9, "unit": wl.unit, "cores": threads, "kind": "port",
+        cpu = {"value": u / dt / scale, "unit": wl.unit, "cores": threads, "kind": "port",
                "sample": f"{sample}; {dt:.1f} s"}
 
     if rank == 0:

@@ -243,6 +243,88 @@ int gbj_select_range(gbj_ctx *ctx, const int32_t *d_col, uint64_t n,
                      int32_t lo, int32_t hi, int32_t *d_rows_out,
                      uint64_t *d_count, void *stream);
 
+/* ------------------------------------------------ batched star join */
+/* Up to GBJ_STAR_MAX_QUERIES star-join queries over one fact table in one
+ * pass.  Each query computes what a reference plan of
+ *   select(dim predicate) -> hashjoin-chained(build dim.PK, probe fact.FK)
+ *   for each joined dimension -> groupby(dimA.attr, dimB.attr;
+ *   COUNT, SUM(int64 price * quantity))
+ * computes with the operators of core/olap/lib/operators/select.cpp:26-37,
+ * hash-join-chained.cpp:262-566 and hash-group-by-chained.cpp:267-853; the
+ * reference runs such plans one query at a time (its SSB plans,
+ * tests/inputs/plans/gpu-ssb/ *.json, have this shape).  Here every query of
+ * a batch shares one read of the fact columns.
+ *
+ * Dimension row i has primary key key_base + i (dense keys, as the
+ * reference's SSB dimensions have); a fact foreign key outside
+ * [key_base, key_base + n) matches nothing.  Group keys must come from
+ * joined dimensions and their declared [attr_min, attr_max] domains must
+ * multiply to at most GBJ_STAR_MAX_GROUPS groups; a value outside its
+ * declared domain is reported as GBJ_ERR_INVALID at gbj_sync.
+ *
+ * Results of query q: rows [q * group_cap, q * group_cap + d_n_groups[q])
+ * of the output columns, one per group with at least one row, sorted by
+ * (key_a, key_b). */
+#define GBJ_STAR_MAX_DIMS 4
+#define GBJ_STAR_MAX_ATTRS 4
+#define GBJ_STAR_MAX_QUERIES 64
+#define GBJ_STAR_MAX_GROUPS 4096
+
+typedef enum gbj_attr_type { GBJ_ATTR_I32 = 0, GBJ_ATTR_I8 = 1 } gbj_attr_type;
+
+typedef struct gbj_star_dim {
+  uint64_t n;                              /* rows (< 2^31)               */
+  int32_t key_base;                        /* primary key of row 0        */
+  int32_t n_attrs;
+  const void *d_attr[GBJ_STAR_MAX_ATTRS];  /* int32 or int8 columns       */
+  int32_t attr_type[GBJ_STAR_MAX_ATTRS];   /* gbj_attr_type               */
+  int32_t attr_min[GBJ_STAR_MAX_ATTRS];    /* value domain (group keys)   */
+  int32_t attr_max[GBJ_STAR_MAX_ATTRS];
+} gbj_star_dim;
+
+typedef struct gbj_star_fact {
+  uint64_t n;
+  int32_t n_dims;                          /* 1..GBJ_STAR_MAX_DIMS        */
+  const int32_t *d_fk[GBJ_STAR_MAX_DIMS];  /* fk column d -> dimension d  */
+  const int32_t *d_quantity;
+  const int32_t *d_price;
+} gbj_star_fact;
+
+typedef struct gbj_star_query {
+  int32_t join_mask;                       /* bit d: join dimension d     */
+  int32_t pred_attr[GBJ_STAR_MAX_DIMS];    /* attribute filtered, -1 none */
+  int32_t pred_lo[GBJ_STAR_MAX_DIMS];      /* lo <= attr <= hi            */
+  int32_t pred_hi[GBJ_STAR_MAX_DIMS];
+  int32_t group_dim[2];                    /* group key a, b: dimension   */
+  int32_t group_attr[2];                   /*   and attribute             */
+} gbj_star_query;
+
+typedef struct gbj_star_out {
+  int32_t *d_key_a;       /* [n_queries * group_cap] each                 */
+  int32_t *d_key_b;
+  int64_t *d_count;
+  int64_t *d_sum;         /* SUM((int64)price * quantity)                 */
+  uint64_t *d_n_groups;   /* [n_queries]                                  */
+  uint64_t group_cap;
+} gbj_star_out;
+
+/* A plan holds a schema's per-batch device state (dimension masks, group
+ * tables, the descriptor buffers) and the CUDA graphs of a batch.  The
+ * columns stay caller-owned and must outlive the plan. */
+typedef struct gbj_star_plan gbj_star_plan;
+
+int gbj_star_plan_create(gbj_ctx *ctx, const gbj_star_fact *fact,
+                         const gbj_star_dim *dims, gbj_star_plan **out);
+/* Runs n_queries (1..GBJ_STAR_MAX_QUERIES) queries on `stream`.  use_graph:
+ * the batch's copies and three kernels are captured into a CUDA graph on
+ * first use and replayed afterwards (two graphs alternate so the host can
+ * prepare the next batch while one runs).  Runs of one plan must be ordered
+ * (one stream, or synchronised): they share the plan's device state. */
+int gbj_star_run(gbj_star_plan *plan, const gbj_star_query *queries,
+                 int32_t n_queries, const gbj_star_out *out,
+                 int32_t use_graph, void *stream);
+void gbj_star_plan_destroy(gbj_star_plan *plan);
+
 /* --------------------------------------- allocation-free join + aggregate */
 /* This entry point has no counterpart in the reference.  It is for callers
  * that may not allocate device memory at the moment they call: a host engine
@@ -291,6 +373,10 @@ int gbj_gen_probe_zipf(uint64_t seed, uint64_t n, uint64_t n_build,
 int gbj_gen_groupby(uint64_t seed, uint64_t n, uint64_t cardinality,
                     double theta, int32_t *h_keys, int32_t *h_values,
                     int threads);
+/* out[i] = lo + a uniform draw from {0 .. hi - lo} of column stream
+ * `stream` (independent streams for independent columns). */
+int gbj_gen_uniform_i32(uint64_t seed, uint64_t stream, uint64_t n,
+                        int32_t lo, int32_t hi, int32_t *h_out, int threads);
 uint64_t gbj_gen_rand(uint64_t seed, uint64_t stream, uint64_t i);
 uint64_t gbj_gen_perm(uint64_t seed, uint64_t stream, uint64_t n, uint64_t i);
 uint64_t gbj_gen_zipf(uint64_t seed, uint64_t stream, uint64_t n, double theta,

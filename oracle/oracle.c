@@ -797,3 +797,232 @@ void orc_reduce(const int32_t *col, const int32_t *rows, uint64_t n,
   }
   for (int j = 0; j < n_aggs; ++j) out[j] = a.v[j];
 }
+
+/* ------------------------------------------------------------ star join */
+/* One star-join query as a chain of the reference's operators: Select on
+ * each joined dimension (select.cpp:26-37); HashJoinChained with the
+ * qualifying dimension rows as build side keyed by their primary key and
+ * the fact's foreign key as probe key (hash-join-chained.cpp:262-566, via
+ * orc_join_build); HashGroupByChained on the two group attributes with
+ * COUNT and SUM((int64)price * quantity) (hash-group-by-chained.cpp:
+ * 267-853; the int64 product is the plan's CastExpression,
+ * expressions.hpp:1162).  Fact rows are split over threads, each with its
+ * own group table; the tables are merged and sorted by (a, b). */
+
+static int32_t star_attr(const orc_star_dim *d, int a, uint64_t i) {
+  return d->attr_type[a] == 1 ? (int32_t)((const int8_t *)d->attr[a])[i]
+                              : ((const int32_t *)d->attr[a])[i];
+}
+
+typedef struct {
+  int32_t a, b, next;
+  int64_t cnt, sum;
+} star_group;
+
+typedef struct {
+  int32_t *head;
+  star_group *e;
+  uint64_t n, cap;
+  int hb;
+} star_gtable;
+
+/* combineHashes (core/olap/lib/util/functions.cpp:397-400): boost-style
+ * hash_combine of the two key hashes.  Placement only. */
+static uint64_t star_pair_hash(int32_t a, int32_t b) {
+  uint64_t h = orc_hash_int32(a);
+  h ^= orc_hash_int32(b) + 0x9e3779b9ULL + (h << 6) + (h >> 2);
+  return h;
+}
+
+static int star_gt_init(star_gtable *g) {
+  g->hb = 12;
+  g->head = (int32_t *)malloc(sizeof(int32_t) << g->hb);
+  g->cap = 1024;
+  g->e = (star_group *)malloc(sizeof(star_group) * g->cap);
+  g->n = 0;
+  if (!g->head || !g->e) return -1;
+  memset(g->head, 0xff, sizeof(int32_t) << g->hb);
+  return 0;
+}
+
+static void star_gt_free(star_gtable *g) {
+  free(g->head);
+  free(g->e);
+}
+
+static int star_gt_update(star_gtable *g, int32_t a, int32_t b, int64_t cnt, int64_t sum) {
+  if (g->n >= (2ULL << g->hb) && g->hb < 24) {
+    int hb = g->hb + 1;
+    int32_t *head = (int32_t *)malloc(sizeof(int32_t) << hb);
+    if (!head) return -1;
+    memset(head, 0xff, sizeof(int32_t) << hb);
+    for (uint64_t i = 0; i < g->n; ++i) {
+      uint64_t h = star_pair_hash(g->e[i].a, g->e[i].b) & ((1ULL << hb) - 1);
+      g->e[i].next = head[h];
+      head[h] = (int32_t)i;
+    }
+    free(g->head);
+    g->head = head;
+    g->hb = hb;
+  }
+  uint64_t h = star_pair_hash(a, b) & ((1ULL << g->hb) - 1);
+  for (int32_t cur = g->head[h]; cur != -1; cur = g->e[cur].next) {
+    star_group *x = &g->e[cur];
+    if (x->a == a && x->b == b) {
+      x->cnt += cnt;
+      x->sum += sum;
+      return 0;
+    }
+  }
+  if (g->n == g->cap) {
+    g->cap *= 2;
+    star_group *e = (star_group *)realloc(g->e, sizeof(star_group) * g->cap);
+    if (!e) return -1;
+    g->e = e;
+  }
+  star_group *x = &g->e[g->n];
+  x->a = a;
+  x->b = b;
+  x->cnt = cnt;
+  x->sum = sum;
+  x->next = g->head[h];
+  g->head[h] = (int32_t)g->n;
+  g->n++;
+  return 0;
+}
+
+static int star_cmp(const void *p, const void *q) {
+  const star_group *x = (const star_group *)p, *y = (const star_group *)q;
+  if (x->a != y->a) return (x->a > y->a) - (x->a < y->a);
+  return (x->b > y->b) - (x->b < y->b);
+}
+
+typedef struct {
+  const int32_t *const *fk;
+  const int32_t *qty, *price;
+  const orc_star_dim *dims;
+  const orc_star_q *q;
+  const orc_chained_table *ht; /* per dimension, joined ones only */
+  int32_t n_dims;
+  uint64_t lo, hi;
+  star_gtable g;
+  int rc;
+} star_arg;
+
+static void *star_worker(void *p) {
+  star_arg *s = (star_arg *)p;
+  const orc_star_q *q = s->q;
+  for (uint64_t i = s->lo; i < s->hi && !s->rc; ++i) {
+    int64_t row[4] = {-1, -1, -1, -1};
+    int ok = 1;
+    for (int d = 0; d < s->n_dims && ok; ++d) {
+      if (!((q->join_mask >> d) & 1)) continue;
+      const orc_chained_table *t = &s->ht[d];
+      const int32_t k = s->fk[d][i];
+      int64_t hit = -1;
+      /* probe: walk head[h] chain, eq(key) (hash-join-chained.cpp:321-566) */
+      for (int32_t cur = t->head[bucket_of(k, t->hash_bits)]; cur != -1; cur = t->next[cur])
+        if (t->key[cur] == k) {
+          hit = t->payload[cur];
+          break; /* primary keys: at most one match */
+        }
+      if (hit < 0) ok = 0;
+      row[d] = hit;
+    }
+    if (!ok) continue;
+    const int32_t a = star_attr(&s->dims[q->group_dim[0]], q->group_attr[0], (uint64_t)row[q->group_dim[0]]);
+    const int32_t b = star_attr(&s->dims[q->group_dim[1]], q->group_attr[1], (uint64_t)row[q->group_dim[1]]);
+    if (star_gt_update(&s->g, a, b, 1, (int64_t)s->price[i] * (int64_t)s->qty[i])) s->rc = -1;
+  }
+  return 0;
+}
+
+int64_t orc_star_query(const int32_t *const *fk, int32_t n_dims, const int32_t *qty,
+                       const int32_t *price, uint64_t n_fact, const orc_star_dim *dims,
+                       const orc_star_q *q, int threads, int32_t *out_a, int32_t *out_b,
+                       int64_t *out_count, int64_t *out_sum, uint64_t cap) {
+  if (!dims || !q || n_dims < 1 || n_dims > 4 || (n_fact && (!fk || !qty || !price))) return -1;
+  for (int k = 0; k < 2; ++k)
+    if (q->group_dim[k] < 0 || q->group_dim[k] >= n_dims || !((q->join_mask >> q->group_dim[k]) & 1))
+      return -1;
+  if (threads < 1) threads = 1;
+  if (n_fact < 65536) threads = 1;
+  orc_chained_table ht[4];
+  int32_t *bkeys[4] = {0, 0, 0, 0}, *brows[4] = {0, 0, 0, 0};
+  memset(ht, 0, sizeof(ht));
+  int64_t rc = 0;
+  for (int d = 0; d < n_dims && !rc; ++d) {
+    if (!((q->join_mask >> d) & 1)) continue;
+    const orc_star_dim *dd = &dims[d];
+    bkeys[d] = (int32_t *)malloc(sizeof(int32_t) * (dd->n ? dd->n : 1));
+    brows[d] = (int32_t *)malloc(sizeof(int32_t) * (dd->n ? dd->n : 1));
+    if (!bkeys[d] || !brows[d]) {
+      rc = -1;
+      break;
+    }
+    uint64_t m = 0;
+    const int pa = q->pred_attr[d];
+    for (uint64_t r = 0; r < dd->n; ++r) {
+      if (pa >= 0) {
+        const int32_t v = star_attr(dd, pa, r);
+        if (v < q->pred_lo[d] || v > q->pred_hi[d]) continue; /* Select */
+      }
+      bkeys[d][m] = dd->key_base + (int32_t)r;
+      brows[d][m] = (int32_t)r;
+      ++m;
+    }
+    if (orc_join_build(bkeys[d], brows[d], m, 0, &ht[d])) rc = -1;
+  }
+  star_arg *args = (star_arg *)calloc((size_t)threads, sizeof(star_arg));
+  pthread_t *th = (pthread_t *)calloc((size_t)threads, sizeof(pthread_t));
+  if (!args || !th) rc = -1;
+  for (int t = 0; t < threads && !rc; ++t) {
+    args[t].fk = fk;
+    args[t].qty = qty;
+    args[t].price = price;
+    args[t].dims = dims;
+    args[t].q = q;
+    args[t].ht = ht;
+    args[t].n_dims = n_dims;
+    args[t].lo = n_fact * (uint64_t)t / (uint64_t)threads;
+    args[t].hi = n_fact * (uint64_t)(t + 1) / (uint64_t)threads;
+    if (star_gt_init(&args[t].g)) rc = -1;
+  }
+  if (!rc) {
+    for (int t = 1; t < threads; ++t) pthread_create(&th[t], 0, star_worker, &args[t]);
+    star_worker(&args[0]);
+    for (int t = 1; t < threads; ++t) pthread_join(th[t], 0);
+    for (int t = 0; t < threads; ++t)
+      if (args[t].rc) rc = -1;
+  }
+  if (!rc) {
+    star_gtable *g = &args[0].g;
+    for (int t = 1; t < threads && !rc; ++t)
+      for (uint64_t i = 0; i < args[t].g.n; ++i)
+        if (star_gt_update(g, args[t].g.e[i].a, args[t].g.e[i].b, args[t].g.e[i].cnt, args[t].g.e[i].sum)) {
+          rc = -1;
+          break;
+        }
+    if (!rc) {
+      qsort(g->e, g->n, sizeof(star_group), star_cmp);
+      for (uint64_t i = 0; i < g->n && i < cap; ++i) {
+        if (out_a) out_a[i] = g->e[i].a;
+        if (out_b) out_b[i] = g->e[i].b;
+        if (out_count) out_count[i] = g->e[i].cnt;
+        if (out_sum) out_sum[i] = g->e[i].sum;
+      }
+      rc = (int64_t)g->n;
+    }
+  }
+  if (args)
+    for (int t = 0; t < threads; ++t)
+      if (args[t].g.head) star_gt_free(&args[t].g);
+  free(args);
+  free(th);
+  for (int d = 0; d < 4; ++d) {
+    if (ht[d].head) orc_join_free(&ht[d]);
+    free(bkeys[d]);
+    free(brows[d]);
+  }
+  return rc;
+}

@@ -109,6 +109,38 @@ void orc_reduce(const int32_t *col, const int32_t *rows, uint64_t n,
                 const int32_t *ops, const int32_t *operands, int32_t n_aggs,
                 int64_t *out);
 
+
+/* ---- star-join query: Select -> HashJoinChained per joined dimension ->
+ *      HashGroupByChained on two dimension attributes (compositions of the
+ *      functions above; see oracle.c) ---- */
+typedef struct orc_star_dim {
+  uint64_t n;
+  int32_t key_base; /* primary key of row 0; row i has key_base + i */
+  int32_t n_attrs;
+  const void *attr[4];
+  int32_t attr_type[4]; /* 0 int32, 1 int8 */
+  int32_t attr_min[4];  /* unused by the oracle (same layout as gbjoin.h) */
+  int32_t attr_max[4];
+} orc_star_dim;
+
+typedef struct orc_star_q {
+  int32_t join_mask;
+  int32_t pred_attr[4]; /* -1: no predicate */
+  int32_t pred_lo[4];
+  int32_t pred_hi[4];
+  int32_t group_dim[2];
+  int32_t group_attr[2];
+} orc_star_q;
+
+/* Groups (a, b, COUNT, SUM((int64)price * quantity)) sorted by (a, b);
+ * returns the group count (only the first cap are written) or -1. */
+int64_t orc_star_query(const int32_t *const *fk, int32_t n_dims,
+                       const int32_t *qty, const int32_t *price,
+                       uint64_t n_fact, const orc_star_dim *dims,
+                       const orc_star_q *q, int threads, int32_t *out_a,
+                       int32_t *out_b, int64_t *out_count, int64_t *out_sum,
+                       uint64_t cap);
+
 #ifdef __cplusplus
 }
 #endif

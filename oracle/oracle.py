@@ -68,6 +68,8 @@ def lib():
         L.orc_groupby.argtypes = [vp, vp, u64, i32, C.c_int, vp, vp, vp, vp, vp, u64]
         L.orc_reduce.restype = None
         L.orc_reduce.argtypes = [vp, vp, u64, vp, vp, i32, vp]
+        L.orc_star_query.restype = i64
+        L.orc_star_query.argtypes = [vp, i32, vp, vp, u64, vp, vp, C.c_int, vp, vp, vp, vp, u64]
         _lib = L
     return _lib
 
@@ -194,6 +196,49 @@ def reduce(col, aggs, rows=None):
     n = len(rows) if rows is not None else len(col)
     L.orc_reduce(_p(col), _p(rows), n, _p(ops), _p(opd), len(aggs), _p(out))
     return [int(x) for x in out]
+
+
+class StarDim(C.Structure):
+    _fields_ = [("n", u64), ("key_base", i32), ("n_attrs", i32), ("attr", vp * 4),
+                ("attr_type", i32 * 4), ("attr_min", i32 * 4), ("attr_max", i32 * 4)]
+
+
+class StarQ(C.Structure):
+    _fields_ = [("join_mask", i32), ("pred_attr", i32 * 4), ("pred_lo", i32 * 4),
+                ("pred_hi", i32 * 4), ("group_dim", i32 * 2), ("group_attr", i32 * 2)]
+
+
+def star_query(data, query, threads=1, rows=None):
+    """One star query (a proteus_gb300.star.Query) over a StarData, on the
+    fact rows [0, rows) (all when None) -> (a, b, count, sum) sorted by (a, b)."""
+    L = lib()
+    nd = len(data.dims)
+    n = data.n_fact if rows is None else int(rows)
+    fk = [np.ascontiguousarray(c[:n], dtype=np.int32) for c in data.fk]
+    qty = np.ascontiguousarray(data.quantity[:n], dtype=np.int32)
+    price = np.ascontiguousarray(data.price[:n], dtype=np.int32)
+    fk_ptrs = (vp * 4)(*[c.ctypes.data for c in fk])
+    dims = (StarDim * 4)()
+    for d, dim in enumerate(data.dims):
+        dims[d].n, dims[d].key_base, dims[d].n_attrs = dim.n, 1, len(dim.attrs)
+        for a, col in enumerate(dim.attrs):
+            dims[d].attr[a] = col.ctypes.data
+            dims[d].attr_type[a] = 1 if col.dtype == np.int8 else 0
+    q = StarQ()
+    q.join_mask = query.join_mask
+    for d in range(4):
+        q.pred_attr[d], q.pred_lo[d], q.pred_hi[d] = query.pred_attr[d], query.pred_lo[d], query.pred_hi[d]
+    for k in range(2):
+        q.group_dim[k], q.group_attr[k] = query.group_dim[k], query.group_attr[k]
+    cap = 4096
+    a = np.empty(cap, dtype=np.int32)
+    b = np.empty(cap, dtype=np.int32)
+    c = np.empty(cap, dtype=np.int64)
+    s = np.empty(cap, dtype=np.int64)
+    ng = L.orc_star_query(fk_ptrs, nd, _p(qty), _p(price), n, dims, C.byref(q), threads, _p(a), _p(b),
+                          _p(c), _p(s), cap)
+    assert 0 <= ng <= cap, ng
+    return a[:ng], b[:ng], c[:ng], s[:ng]
 
 
 def ref_rj_stepwise(rkeys, skeys):

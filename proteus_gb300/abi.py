@@ -39,6 +39,33 @@ class GroupbyParams(C.Structure):
                 ("max_input_size", C.c_uint64), ("expected_groups", C.c_uint64)]
 
 
+STAR_MAX_DIMS, STAR_MAX_ATTRS, STAR_MAX_QUERIES, STAR_MAX_GROUPS = 4, 4, 64, 4096
+ATTR_I32, ATTR_I8 = 0, 1
+
+
+class StarDim(C.Structure):
+    _fields_ = [("n", C.c_uint64), ("key_base", C.c_int32), ("n_attrs", C.c_int32),
+                ("d_attr", C.c_void_p * STAR_MAX_ATTRS), ("attr_type", C.c_int32 * STAR_MAX_ATTRS),
+                ("attr_min", C.c_int32 * STAR_MAX_ATTRS), ("attr_max", C.c_int32 * STAR_MAX_ATTRS)]
+
+
+class StarFact(C.Structure):
+    _fields_ = [("n", C.c_uint64), ("n_dims", C.c_int32),
+                ("d_fk", C.c_void_p * STAR_MAX_DIMS), ("d_quantity", C.c_void_p),
+                ("d_price", C.c_void_p)]
+
+
+class StarQuery(C.Structure):
+    _fields_ = [("join_mask", C.c_int32), ("pred_attr", C.c_int32 * STAR_MAX_DIMS),
+                ("pred_lo", C.c_int32 * STAR_MAX_DIMS), ("pred_hi", C.c_int32 * STAR_MAX_DIMS),
+                ("group_dim", C.c_int32 * 2), ("group_attr", C.c_int32 * 2)]
+
+
+class StarOut(C.Structure):
+    _fields_ = [("d_key_a", C.c_void_p), ("d_key_b", C.c_void_p), ("d_count", C.c_void_p),
+                ("d_sum", C.c_void_p), ("d_n_groups", C.c_void_p), ("group_cap", C.c_uint64)]
+
+
 vp, u64, i32, i64, dbl = C.c_void_p, C.c_uint64, C.c_int32, C.c_int64, C.c_double
 P = C.POINTER
 
@@ -74,6 +101,10 @@ SIGNATURES = {
     "gbj_gen_probe_uniform": (C.c_int, [u64, u64, u64, vp, vp, C.c_int]),
     "gbj_gen_probe_zipf": (C.c_int, [u64, u64, u64, dbl, dbl, vp, vp, C.c_int]),
     "gbj_gen_groupby": (C.c_int, [u64, u64, u64, dbl, vp, vp, C.c_int]),
+    "gbj_star_plan_create": (C.c_int, [vp, P(StarFact), P(StarDim), P(vp)]),
+    "gbj_star_run": (C.c_int, [vp, P(StarQuery), i32, P(StarOut), i32, vp]),
+    "gbj_star_plan_destroy": (None, [vp]),
+    "gbj_gen_uniform_i32": (C.c_int, [u64, u64, u64, i32, i32, vp, C.c_int]),
     "gbj_gen_rand": (u64, [u64, u64, u64]),
     "gbj_gen_perm": (u64, [u64, u64, u64, u64]),
     "gbj_gen_zipf": (u64, [u64, u64, u64, dbl, u64]),

@@ -315,4 +315,16 @@ int gbj_gen_groupby(uint64_t seed, uint64_t n, uint64_t cardinality,
   return GBJ_OK;
 }
 
+// out[i] = lo + uniform{0 .. hi - lo}, from column stream `stream`.
+int gbj_gen_uniform_i32(uint64_t seed, uint64_t stream, uint64_t n, int32_t lo, int32_t hi,
+                        int32_t *out, int threads) {
+  if (hi < lo || (n && !out)) return GBJ_ERR_INVALID;
+  const uint64_t key = stream_key(seed, stream);
+  const uint64_t range = (uint64_t)((int64_t)hi - lo) + 1;
+  parallel_rows(n, threads, [&](uint64_t a, uint64_t b) {
+    for (uint64_t i = a; i < b; ++i) out[i] = (int32_t)((int64_t)lo + (int64_t)below(draw(key, i), range));
+  });
+  return GBJ_OK;
+}
+
 }  // extern "C"

@@ -1,0 +1,132 @@
+"""Batched star join (gbj_star_*) on the GPU vs the oracle's per-query
+restatement, through the C ABI."""
+import numpy as np
+import pytest
+
+from gpu_util import cpu_threads
+from proteus_gb300 import abi, star
+
+pytestmark = pytest.mark.gpu
+
+SMALL_DIMS = (1 << 14, 2557, 1 << 12, 1 << 10)
+
+
+@pytest.fixture(scope="module")
+def data():
+    return star.gen_star(21, n_fact=(1 << 20) + 3, dim_rows=SMALL_DIMS)
+
+
+@pytest.fixture(scope="module")
+def plan(ctx, data):
+    p = star.StarPlan(ctx, data)
+    yield p
+    p.close()
+
+
+@pytest.fixture(scope="module")
+def expected(data, oracle):
+    qs = star.gen_queries(21, 64, data.dims)
+    return qs, [oracle.star_query(data, q, threads=cpu_threads()) for q in qs]
+
+
+def check(got, exp):
+    for i, (g, e) in enumerate(zip(got, exp)):
+        assert len(g[0]) == len(e[0]), i
+        for x, y in zip(g, e):
+            assert (x == y).all(), i
+
+
+@pytest.mark.parametrize("use_graph", [False, True])
+def test_star_batch_parity(ctx, plan, expected, use_graph):
+    qs, exp = expected
+    out = plan.run(qs, use_graph=use_graph)
+    ctx.sync()
+    check(star.StarPlan.results(out, len(qs)), exp)
+
+
+def test_star_graph_replays_alternate(ctx, plan, expected):
+    """Four replays (two graphs alternating) with different query subsets."""
+    qs, exp = expected
+    subsets = [list(range(0, 64, 2)), list(range(1, 64, 3)), list(range(64)), [5]]
+    outs = [plan.run([qs[i] for i in s], use_graph=True) for s in subsets]
+    ctx.sync()
+    for s, out in zip(subsets, outs):
+        check(star.StarPlan.results(out, len(s)), [exp[i] for i in s])
+
+
+def test_star_alone_equals_in_batch(ctx, plan, expected):
+    qs, exp = expected
+    for i in (0, 17, 63):
+        out = plan.run([qs[i]], use_graph=False)
+        ctx.sync()
+        check(star.StarPlan.results(out, 1), [exp[i]])
+
+
+def test_star_unaligned_columns_scalar_path(ctx, data, oracle):
+    """Fact columns that are not 16-byte aligned take the scalar load path."""
+    import torch
+
+    fk = [torch.from_numpy(c).cuda()[1:] for c in data.fk]
+    qty = torch.from_numpy(data.quantity).cuda()[1:]
+    price = torch.from_numpy(data.price).cuda()[1:]
+    shifted = star.StarData(data.dims, [c[1:] for c in data.fk], data.quantity[1:], data.price[1:])
+    p = star.StarPlan(ctx, data, fact_tensors=(fk, qty, price))
+    qs = star.gen_queries(4, 8, data.dims)
+    out = p.run(qs, use_graph=False)
+    ctx.sync()
+    exp = [oracle.star_query(shifted, q, threads=cpu_threads()) for q in qs]
+    check(star.StarPlan.results(out, len(qs)), exp)
+    p.close()
+
+
+def test_star_foreign_keys_outside_dimension(ctx, oracle):
+    d = star.gen_star(9, n_fact=1 << 18, dim_rows=SMALL_DIMS)
+    d.fk[0][::7] = 0
+    d.fk[1][::11] = SMALL_DIMS[1] + 3
+    d.fk[2][::13] = -5
+    p = star.StarPlan(ctx, d)
+    qs = star.gen_queries(9, 64, d.dims)
+    out = p.run(qs)
+    ctx.sync()
+    check(star.StarPlan.results(out, len(qs)), [oracle.star_query(d, q, threads=cpu_threads()) for q in qs])
+    p.close()
+
+
+def test_star_invalid_requests(ctx, plan, data):
+    good = star.gen_queries(1, 1, data.dims)[0]
+    bad = []
+    q = star.gen_queries(1, 1, data.dims)[0]
+    q.join_mask = 0
+    bad.append(q)
+    q = star.gen_queries(1, 1, data.dims)[0]
+    q.join_mask = 1 << 5
+    bad.append(q)
+    q = star.gen_queries(1, 1, data.dims)[0]
+    q.join_mask = 0b0001
+    q.group_dim = [0, 2]  # dimension 2 is not joined
+    bad.append(q)
+    q = star.Query(join_mask=0b0101, group_dim=[0, 2], group_attr=[2, 2])  # 250 x 1000 groups
+    bad.append(q)
+    for q in bad:
+        with pytest.raises(abi.GbjError) as e:
+            plan.run([q])
+        assert e.value.code == abi.ERR_INVALID
+    with pytest.raises(abi.GbjError):
+        plan.run([good] * 65)
+    out = plan.run([good])  # the plan still works
+    ctx.sync()
+    assert int(out["n"][0]) > 0
+
+
+def test_star_full_size(ctx, oracle):
+    """2^28-row fact, full dimensions, 64 queries in one graph replay; eight
+    of them checked against the oracle on the full fact table."""
+    d = star.gen_star(2026, n_fact=star.FULL_FACT_ROWS)
+    p = star.StarPlan(ctx, d)
+    qs = star.gen_queries(2026, 64, d.dims)
+    out = p.run(qs, use_graph=True)
+    ctx.sync()
+    got = star.StarPlan.results(out, len(qs))
+    for i in range(0, 64, 8):
+        check([got[i]], [oracle.star_query(d, qs[i], threads=cpu_threads())])
+    p.close()
