@@ -325,6 +325,92 @@ int gbj_star_run(gbj_star_plan *plan, const gbj_star_query *queries,
                  int32_t use_graph, void *stream);
 void gbj_star_plan_destroy(gbj_star_plan *plan);
 
+/* ------------------------------------------------------- query serving */
+/* A request loop for join + group-by queries over resident device columns:
+ *   SELECT b.group, COUNT(*), SUM((int64)p.value)
+ *   FROM build b JOIN probe p ON b.key = p.key GROUP BY b.group
+ * with HashJoinChained semantics (every build row inserted, duplicates
+ * allowed; core/olap/lib/operators/hash-join-chained.cpp:262-566) feeding
+ * HashGroupByChained (hash-group-by-chained.cpp:267-853).
+ *
+ * It stands in for the reference's per-query execution path: operators that
+ * allocate their tables through MemoryManager / buffer_manager at open() and
+ * free them at close() (core/olap/lib/operators/gpu/
+ * gpu-hash-join-chained.cpp:31-73, core/platform/lib/memory/
+ * memory-manager.cpp), one query after another with a stream sync per GPU
+ * operator.  Here the tables of admitted queries come from the context's
+ * resident pool within an HBM budget; queries that arrive while others run
+ * are admitted as soon as an in-flight slot and budget are free, and each
+ * admitted group runs as one batch: five persistent kernels (clear, build,
+ * probe + group-by, emit, finish) over the work items of all its queries,
+ * captured once per slot as a CUDA graph and replayed.  Slots run on their
+ * own streams, so batches overlap on the device.
+ *
+ * max_batch = 1, max_inflight = 1, use_graph = 0 is the plain form: one query
+ * per launch sequence, each waited for before the next starts.
+ *
+ * Output groups come out in no particular order; *out_n_groups is written
+ * when the query completes.  Output pointers may be device memory or mapped
+ * pinned host memory. */
+#define GBJ_SERVE_MAX_BATCH 64
+
+typedef struct gbj_serve_query {
+  const int32_t *d_build_keys;
+  const int32_t *d_build_group;  /* group key of each build row        */
+  uint64_t n_build;
+  const int32_t *d_probe_keys;
+  const int32_t *d_probe_vals;
+  uint64_t n_probe;
+  uint64_t expected_groups;      /* upper bound of distinct groups     */
+  int32_t *out_group;
+  int64_t *out_count;
+  int64_t *out_sum;
+  uint64_t *out_n_groups;
+  uint64_t out_capacity;
+} gbj_serve_query;
+
+typedef struct gbj_server_params {
+  uint64_t hbm_budget;   /* pool bytes queries in flight may hold (0 = pool) */
+  int32_t max_batch;     /* queries per batch, 1..GBJ_SERVE_MAX_BATCH        */
+  int32_t max_inflight;  /* batches in flight (streams), 1..8                */
+  int32_t use_graph;     /* replay each slot's batch from a CUDA graph       */
+  int32_t large_slots;   /* slots reserved for large queries (0 = one class) */
+  uint64_t small_rows;   /* a query with n_build + n_probe above this is
+                            large (0 = 2^22); large queries queue apart,
+                            run on low-priority streams with one work item
+                            per CTA, so small batches on the high-priority
+                            slots take SMs as the large batch's CTAs retire */
+} gbj_server_params;
+
+typedef struct gbj_server gbj_server;
+
+int gbj_server_create(gbj_ctx *ctx, const gbj_server_params *params,
+                      gbj_server **out);
+/* Queues a query (non-blocking; the columns and outputs must stay valid
+ * until it completes).  A query whose tables exceed the whole budget is
+ * completed at once with GBJ_ERR_BUDGET. */
+int gbj_server_submit(gbj_server *srv, const gbj_serve_query *q,
+                      uint64_t *ticket);
+/* Queues n queries under one lock (so the request loop sees them together);
+ * tickets[i] gets query i's ticket.  All or none are queued. */
+int gbj_server_submit_batch(gbj_server *srv, const gbj_serve_query *qs,
+                            uint64_t n, uint64_t *tickets);
+/* Waits up to timeout_s (< 0: forever) for a query; *status gets its
+ * result status.  Returns GBJ_ERR_TIMEOUT if it is still running. */
+int gbj_server_wait(gbj_server *srv, uint64_t ticket, double timeout_s,
+                    int32_t *status);
+/* Host-clock seconds (since the server started) at which the query was
+ * submitted, launched and seen complete; -1 for a stage not reached. */
+int gbj_server_times(gbj_server *srv, uint64_t ticket, double *submitted,
+                     double *launched, double *completed);
+/* Waits for every submitted query. */
+int gbj_server_drain(gbj_server *srv);
+/* Totals: queries completed, batches launched, peak budget bytes held. */
+int gbj_server_stats(gbj_server *srv, uint64_t *completed, uint64_t *batches,
+                     uint64_t *peak_bytes);
+/* Drains, stops the request loop and frees the server. */
+int gbj_server_destroy(gbj_server *srv);
+
 /* --------------------------------------- allocation-free join + aggregate */
 /* This entry point has no counterpart in the reference.  It is for callers
  * that may not allocate device memory at the moment they call: a host engine
@@ -377,6 +463,15 @@ int gbj_gen_groupby(uint64_t seed, uint64_t n, uint64_t cardinality,
  * `stream` (independent streams for independent columns). */
 int gbj_gen_uniform_i32(uint64_t seed, uint64_t stream, uint64_t n,
                         int32_t lo, int32_t hi, int32_t *h_out, int threads);
+/* One served join + group-by query (gbj_serve_query inputs): build keys a
+ * seeded permutation of 1..n_build, build groups `cardinality` distinct
+ * int32 values, probe keys hitting a uniform build key with probability
+ * match_rate (else a key above every build key), probe values U[0, 1000). */
+int gbj_gen_serve_query(uint64_t seed, uint64_t n_build, uint64_t n_probe,
+                        double match_rate, uint64_t cardinality,
+                        int32_t *h_build_keys, int32_t *h_build_group,
+                        int32_t *h_probe_keys, int32_t *h_probe_vals,
+                        int threads);
 uint64_t gbj_gen_rand(uint64_t seed, uint64_t stream, uint64_t i);
 uint64_t gbj_gen_perm(uint64_t seed, uint64_t stream, uint64_t n, uint64_t i);
 uint64_t gbj_gen_zipf(uint64_t seed, uint64_t stream, uint64_t n, double theta,

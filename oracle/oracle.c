@@ -1026,3 +1026,91 @@ int64_t orc_star_query(const int32_t *const *fk, int32_t n_dims, const int32_t *
   }
   return rc;
 }
+
+/* ------------------------------------------------- join -> group-by */
+/* HashJoinChained (build keys with the group column as payload; every
+ * build row inserted; a probe emits one binding per matching build row,
+ * hash-join-chained.cpp:262-566) feeding HashGroupByChained on the build
+ * row's group with COUNT and SUM/MIN/MAX of the probe value
+ * (hash-group-by-chained.cpp:267-633).  Probe rows are split over threads,
+ * each with its own group table; merged and sorted by group key. */
+typedef struct {
+  const orc_chained_table *t;
+  const int32_t *pk, *pv;
+  uint64_t lo, hi;
+  orc_gtable g;
+  int rc;
+} jg_arg;
+
+static void *jg_worker(void *p) {
+  jg_arg *a = (jg_arg *)p;
+  const orc_chained_table *t = a->t;
+  for (uint64_t i = a->lo; i < a->hi && !a->rc; ++i) {
+    const int32_t k = a->pk[i];
+    for (int32_t cur = t->head[bucket_of(k, t->hash_bits)]; cur != -1; cur = t->next[cur])
+      if (t->key[cur] == k && gtable_update(&a->g, t->payload[cur], 1, a->pv[i], a->pv[i], a->pv[i]))
+        a->rc = -1;
+  }
+  return 0;
+}
+
+int64_t orc_join_groupby(const int32_t *bk, const int32_t *bg, uint64_t nb, const int32_t *pk,
+                         const int32_t *pv, uint64_t np, int threads, int32_t *out_keys,
+                         int64_t *out_count, int64_t *out_sum, int32_t *out_min, int32_t *out_max,
+                         uint64_t cap) {
+  if ((nb && (!bk || !bg)) || (np && (!pk || !pv))) return -1;
+  if (threads < 1) threads = 1;
+  if (np < 65536) threads = 1;
+  orc_chained_table t;
+  memset(&t, 0, sizeof(t));
+  if (orc_join_build(bk, bg, nb, 0, &t)) return -1;
+  jg_arg *args = (jg_arg *)calloc((size_t)threads, sizeof(jg_arg));
+  pthread_t *th = (pthread_t *)calloc((size_t)threads, sizeof(pthread_t));
+  int64_t rc = (args && th) ? 0 : -1;
+  for (int i = 0; i < threads && !rc; ++i) {
+    args[i].t = &t;
+    args[i].pk = pk;
+    args[i].pv = pv;
+    args[i].lo = np * (uint64_t)i / (uint64_t)threads;
+    args[i].hi = np * (uint64_t)(i + 1) / (uint64_t)threads;
+    if (gtable_init(&args[i].g, 10, 1024)) rc = -1;
+  }
+  if (!rc) {
+    for (int i = 1; i < threads; ++i) pthread_create(&th[i], 0, jg_worker, &args[i]);
+    jg_worker(&args[0]);
+    for (int i = 1; i < threads; ++i) pthread_join(th[i], 0);
+    for (int i = 0; i < threads; ++i)
+      if (args[i].rc) rc = -1;
+  }
+  if (!rc) {
+    orc_gtable *g = &args[0].g;
+    for (int i = 1; i < threads && !rc; ++i)
+      for (uint64_t j = 0; j < args[i].g.n; ++j) {
+        const orc_group *x = &args[i].g.e[j];
+        if (gtable_update(g, x->key, x->cnt, x->sum, x->mn, x->mx)) {
+          rc = -1;
+          break;
+        }
+      }
+    if (!rc) {
+      qsort(g->e, g->n, sizeof(orc_group), cmp_group);
+      for (uint64_t j = 0; j < g->n && j < cap; ++j) {
+        if (out_keys) out_keys[j] = g->e[j].key;
+        if (out_count) out_count[j] = g->e[j].cnt;
+        if (out_sum) out_sum[j] = g->e[j].sum;
+        if (out_min) out_min[j] = g->e[j].mn;
+        if (out_max) out_max[j] = g->e[j].mx;
+      }
+      rc = (int64_t)g->n;
+    }
+  }
+  if (args)
+    for (int i = 0; i < threads; ++i) {
+      free(args[i].g.head);
+      free(args[i].g.e);
+    }
+  free(args);
+  free(th);
+  orc_join_free(&t);
+  return rc;
+}

@@ -141,6 +141,17 @@ int64_t orc_star_query(const int32_t *const *fk, int32_t n_dims,
                        int32_t *out_b, int64_t *out_count, int64_t *out_sum,
                        uint64_t cap);
 
+
+/* HashJoinChained (build payload = group column) feeding HashGroupByChained
+ * on the matched build row's group: COUNT and SUM/MIN/MAX of the probe
+ * value per group, sorted by group key.  Returns the group count (only the
+ * first cap are written) or -1. */
+int64_t orc_join_groupby(const int32_t *bk, const int32_t *bg, uint64_t nb,
+                         const int32_t *pk, const int32_t *pv, uint64_t np,
+                         int threads, int32_t *out_keys, int64_t *out_count,
+                         int64_t *out_sum, int32_t *out_min, int32_t *out_max,
+                         uint64_t cap);
+
 #ifdef __cplusplus
 }
 #endif

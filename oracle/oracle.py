@@ -68,6 +68,8 @@ def lib():
         L.orc_groupby.argtypes = [vp, vp, u64, i32, C.c_int, vp, vp, vp, vp, vp, u64]
         L.orc_reduce.restype = None
         L.orc_reduce.argtypes = [vp, vp, u64, vp, vp, i32, vp]
+        L.orc_join_groupby.restype = i64
+        L.orc_join_groupby.argtypes = [vp, vp, u64, vp, vp, u64, C.c_int, vp, vp, vp, vp, vp, u64]
         L.orc_star_query.restype = i64
         L.orc_star_query.argtypes = [vp, i32, vp, vp, u64, vp, vp, C.c_int, vp, vp, vp, vp, u64]
         _lib = L
@@ -196,6 +198,23 @@ def reduce(col, aggs, rows=None):
     n = len(rows) if rows is not None else len(col)
     L.orc_reduce(_p(col), _p(rows), n, _p(ops), _p(opd), len(aggs), _p(out))
     return [int(x) for x in out]
+
+
+def join_groupby(bk, bg, pk, pv, threads=1):
+    """Join on build keys, group by the matched build row's group:
+    -> (group, count, sum, min, max) sorted by group."""
+    L = lib()
+    bk, bg, pk, pv = _i32(bk), _i32(bg), _i32(pk), _i32(pv)
+    ng = L.orc_join_groupby(_p(bk), _p(bg), len(bk), _p(pk), _p(pv), len(pk), threads, None, None,
+                            None, None, None, 0)
+    assert ng >= 0
+    m = max(ng, 1)
+    out = (np.empty(m, np.int32), np.empty(m, np.int64), np.empty(m, np.int64), np.empty(m, np.int32),
+           np.empty(m, np.int32))
+    ng2 = L.orc_join_groupby(_p(bk), _p(bg), len(bk), _p(pk), _p(pv), len(pk), threads,
+                             *[_p(a) for a in out], ng)
+    assert ng2 == ng
+    return tuple(a[:ng] for a in out)
 
 
 class StarDim(C.Structure):

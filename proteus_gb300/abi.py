@@ -66,6 +66,21 @@ class StarOut(C.Structure):
                 ("d_sum", C.c_void_p), ("d_n_groups", C.c_void_p), ("group_cap", C.c_uint64)]
 
 
+SERVE_MAX_BATCH = 64
+
+
+class ServeQuery(C.Structure):
+    _fields_ = [("d_build_keys", C.c_void_p), ("d_build_group", C.c_void_p), ("n_build", C.c_uint64),
+                ("d_probe_keys", C.c_void_p), ("d_probe_vals", C.c_void_p), ("n_probe", C.c_uint64),
+                ("expected_groups", C.c_uint64), ("out_group", C.c_void_p), ("out_count", C.c_void_p),
+                ("out_sum", C.c_void_p), ("out_n_groups", C.c_void_p), ("out_capacity", C.c_uint64)]
+
+
+class ServerParams(C.Structure):
+    _fields_ = [("hbm_budget", C.c_uint64), ("max_batch", C.c_int32), ("max_inflight", C.c_int32),
+                ("use_graph", C.c_int32), ("large_slots", C.c_int32), ("small_rows", C.c_uint64)]
+
+
 vp, u64, i32, i64, dbl = C.c_void_p, C.c_uint64, C.c_int32, C.c_int64, C.c_double
 P = C.POINTER
 
@@ -104,6 +119,15 @@ SIGNATURES = {
     "gbj_star_plan_create": (C.c_int, [vp, P(StarFact), P(StarDim), P(vp)]),
     "gbj_star_run": (C.c_int, [vp, P(StarQuery), i32, P(StarOut), i32, vp]),
     "gbj_star_plan_destroy": (None, [vp]),
+    "gbj_server_create": (C.c_int, [vp, P(ServerParams), P(vp)]),
+    "gbj_server_submit": (C.c_int, [vp, P(ServeQuery), P(u64)]),
+    "gbj_server_submit_batch": (C.c_int, [vp, P(ServeQuery), u64, P(u64)]),
+    "gbj_server_wait": (C.c_int, [vp, u64, dbl, P(i32)]),
+    "gbj_server_times": (C.c_int, [vp, u64, P(dbl), P(dbl), P(dbl)]),
+    "gbj_server_drain": (C.c_int, [vp]),
+    "gbj_server_stats": (C.c_int, [vp, P(u64), P(u64), P(u64)]),
+    "gbj_server_destroy": (C.c_int, [vp]),
+    "gbj_gen_serve_query": (C.c_int, [u64, u64, u64, dbl, u64, vp, vp, vp, vp, C.c_int]),
     "gbj_gen_uniform_i32": (C.c_int, [u64, u64, u64, i32, i32, vp, C.c_int]),
     "gbj_gen_rand": (u64, [u64, u64, u64]),
     "gbj_gen_perm": (u64, [u64, u64, u64, u64]),

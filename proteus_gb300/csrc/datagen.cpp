@@ -198,6 +198,11 @@ enum Stream : uint64_t {
   kGVal = 10,
   kGPerm = 11,
   kGZipf = 12,
+  kQKey = 13,
+  kQGroup = 14,
+  kQHit = 15,
+  kQProbe = 16,
+  kQVal = 17,
 };
 
 template <typename F>
@@ -323,6 +328,38 @@ int gbj_gen_uniform_i32(uint64_t seed, uint64_t stream, uint64_t n, int32_t lo, 
   const uint64_t range = (uint64_t)((int64_t)hi - lo) + 1;
   parallel_rows(n, threads, [&](uint64_t a, uint64_t b) {
     for (uint64_t i = a; i < b; ++i) out[i] = (int32_t)((int64_t)lo + (int64_t)below(draw(key, i), range));
+  });
+  return GBJ_OK;
+}
+
+// One served join + group-by query: build keys = a seeded permutation of
+// 1..n_build, build group uniform over [0, cardinality) spread over int32 by
+// perm32; probe key = a uniform build key with probability match_rate, else
+// a key above every build key; probe value U[0, 1000).
+int gbj_gen_serve_query(uint64_t seed, uint64_t n_build, uint64_t n_probe, double match_rate,
+                        uint64_t cardinality, int32_t *bk, int32_t *bg, int32_t *pk, int32_t *pv,
+                        int threads) {
+  if (n_build >= (1ULL << 30) || cardinality == 0 || match_rate < 0.0 || match_rate > 1.0)
+    return GBJ_ERR_INVALID;
+  Perm perm(n_build, stream_key(seed, kQKey));
+  const uint64_t kgrp = stream_key(seed, kQGroup), khit = stream_key(seed, kQHit);
+  const uint64_t kprobe = stream_key(seed, kQProbe), kval = stream_key(seed, kQVal);
+  const uint64_t kgperm = stream_key(seed, kGPerm);
+  parallel_rows(n_build, threads, [&](uint64_t lo, uint64_t hi) {
+    for (uint64_t i = lo; i < hi; ++i) {
+      if (bk) bk[i] = (int32_t)(1 + perm(i));
+      if (bg) bg[i] = (int32_t)perm32((uint32_t)below(draw(kgrp, i), cardinality), kgperm);
+    }
+  });
+  parallel_rows(n_probe, threads, [&](uint64_t lo, uint64_t hi) {
+    for (uint64_t j = lo; j < hi; ++j) {
+      if (pk) {
+        const bool hit = n_build && unit(draw(khit, j)) < match_rate;
+        const uint64_t r = draw(kprobe, j);
+        pk[j] = hit ? (int32_t)(1 + below(r, n_build)) : (int32_t)(n_build + 1 + below(r, 1ULL << 30));
+      }
+      if (pv) pv[j] = (int32_t)below(draw(kval, j), 1000);
+    }
   });
   return GBJ_OK;
 }
