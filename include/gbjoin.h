@@ -411,6 +411,37 @@ int gbj_server_stats(gbj_server *srv, uint64_t *completed, uint64_t *batches,
 /* Drains, stops the request loop and frees the server. */
 int gbj_server_destroy(gbj_server *srv);
 
+/* ------------------------------------------------------------ plan façade */
+/* Executes a JSON plan in the reference's plan format (operator names and
+ * fields of core/olap/lib/plan/plan-parser.cpp; expressions of
+ * core/olap/lib/plan/expression-parser.cpp) over int32 device columns named
+ * in a catalog (relation name = the scan plugin's "name", attribute = the
+ * projection's "attrName").  Supported operators: scan, select,
+ * hashjoin-chained, partitioned-hashjoin-chained, join, groupby /
+ * hashgroupby-chained (one int32 key) and reduce (the last two at the root);
+ * expressions recordProjection, int, int64, bool, cast, eq, lt, le, gt, ge,
+ * and, multiply; accumulators sum, max, min.  Anything else gives
+ * GBJ_ERR_UNSUPPORTED with a message naming it.  Sizing fields (hash_bits,
+ * maxBuildInputSize, maxInputSize) are capacity hints.  Execution is
+ * synchronous; results are int64 host columns (group-by rows sorted by key).
+ * The catalog holds pointers only: columns stay caller-owned. */
+typedef struct gbj_catalog gbj_catalog;
+typedef struct gbj_result gbj_result;
+
+int gbj_catalog_create(gbj_ctx *ctx, gbj_catalog **out);
+int gbj_catalog_add_column(gbj_catalog *cat, const char *rel,
+                           const char *attr, const int32_t *d_col, uint64_t n);
+int gbj_catalog_destroy(gbj_catalog *cat);
+/* Parses and checks a plan (operator names, required fields) without a GPU;
+ * on failure err gets the message. */
+int gbj_plan_validate(const char *plan_json, char *err, uint64_t err_len);
+int gbj_plan_execute(gbj_catalog *cat, const char *plan_json,
+                     gbj_result **out);
+int gbj_result_shape(const gbj_result *r, int32_t *n_cols, uint64_t *n_rows);
+const char *gbj_result_name(const gbj_result *r, int32_t col);
+int gbj_result_column(const gbj_result *r, int32_t col, int64_t *h_out);
+void gbj_result_destroy(gbj_result *r);
+
 /* --------------------------------------- allocation-free join + aggregate */
 /* This entry point has no counterpart in the reference.  It is for callers
  * that may not allocate device memory at the moment they call: a host engine

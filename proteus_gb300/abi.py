@@ -127,6 +127,15 @@ SIGNATURES = {
     "gbj_server_drain": (C.c_int, [vp]),
     "gbj_server_stats": (C.c_int, [vp, P(u64), P(u64), P(u64)]),
     "gbj_server_destroy": (C.c_int, [vp]),
+    "gbj_catalog_create": (C.c_int, [vp, P(vp)]),
+    "gbj_catalog_add_column": (C.c_int, [vp, C.c_char_p, C.c_char_p, vp, u64]),
+    "gbj_catalog_destroy": (C.c_int, [vp]),
+    "gbj_plan_validate": (C.c_int, [C.c_char_p, C.c_char_p, u64]),
+    "gbj_plan_execute": (C.c_int, [vp, C.c_char_p, P(vp)]),
+    "gbj_result_shape": (C.c_int, [vp, P(i32), P(u64)]),
+    "gbj_result_name": (C.c_char_p, [vp, i32]),
+    "gbj_result_column": (C.c_int, [vp, i32, vp]),
+    "gbj_result_destroy": (None, [vp]),
     "gbj_gen_serve_query": (C.c_int, [u64, u64, u64, dbl, u64, vp, vp, vp, vp, C.c_int]),
     "gbj_gen_uniform_i32": (C.c_int, [u64, u64, u64, i32, i32, vp, C.c_int]),
     "gbj_gen_rand": (u64, [u64, u64, u64]),

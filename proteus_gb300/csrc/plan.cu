@@ -1,0 +1,800 @@
+// Plan façade: executes the reference's JSON plans (the operator names and
+// fields of core/olap/lib/plan/plan-parser.cpp) on resident device columns
+// by lowering each operator onto the C ABI.
+//
+// Operators: scan (plugin.name + projections, plan-parser.cpp scan cases),
+// select (p), hashjoin-chained (build_input, probe_input, build_k, probe_k,
+// hash_bits, maxBuildInputSize; plan-parser.cpp:977-1006),
+// partitioned-hashjoin-chained (:851-976) and join (radix; p{eq},
+// leftInput, rightInput; :1007-1139), groupby / hashgroupby-chained (input,
+// k, e[{e, m, packet, offset}], hash_bits, maxInputSize; :479-530) and
+// reduce (e, accumulator, p; :248-286).  Expressions (expression-parser.cpp):
+// recordProjection, argument, int, int64, bool, cast, eq, lt, le, gt, ge,
+// and, multiply.  Accumulators: sum, max, min.  Anything else is rejected
+// with GBJ_ERR_UNSUPPORTED and a message naming it.
+//
+// Lowering: reduce over a join whose output expressions read at most one
+// build column and one probe column runs as one fused probe + aggregate
+// (gbj_join_probe_agg for hashjoin-chained, gbj_radix_join_agg for the
+// partitioned / radix joins), as the reference's generated pipeline fuses
+// them; other joins materialise (build row, probe row) pairs and gather the
+// columns their parents read.  Sizing fields are capacity hints.
+#include <algorithm>
+#include <cstdlib>
+#include <cstring>
+#include <map>
+#include <memory>
+#include <set>
+#include <string>
+#include <vector>
+
+#include "gbj_internal.cuh"
+
+using namespace gbj;
+
+namespace {
+
+// ------------------------------------------------------------------- JSON
+struct JVal {
+  enum Type { Null, Bool, Num, Str, Arr, Obj } t = Null;
+  bool b = false;
+  double num = 0;
+  int64_t i = 0;
+  bool is_int = false;
+  std::string s;
+  std::vector<JVal> a;
+  std::vector<std::pair<std::string, JVal>> o;
+  const JVal *get(const char *k) const {
+    if (t != Obj) return nullptr;
+    for (const auto &kv : o)
+      if (kv.first == k) return &kv.second;
+    return nullptr;
+  }
+};
+
+struct PlanError {
+  int code;
+  std::string msg;
+};
+
+[[noreturn]] void fail(int code, const std::string &msg) { throw PlanError{code, msg}; }
+
+class JsonParser {
+ public:
+  explicit JsonParser(const char *p) : p_(p) {}
+  JVal parse() {
+    JVal v = value();
+    ws();
+    if (*p_) fail(GBJ_ERR_INVALID, "plan: trailing characters after JSON value");
+    return v;
+  }
+
+ private:
+  const char *p_;
+  int depth_ = 0;
+  void ws() {
+    while (*p_ == ' ' || *p_ == '\t' || *p_ == '\n' || *p_ == '\r') ++p_;
+  }
+  JVal value() {
+    if (++depth_ > 256) fail(GBJ_ERR_INVALID, "plan: JSON nested too deeply");
+    ws();
+    JVal v;
+    const char c = *p_;
+    if (c == '{') {
+      v.t = JVal::Obj;
+      ++p_;
+      ws();
+      if (*p_ == '}') {
+        ++p_;
+      } else {
+        for (;;) {
+          ws();
+          if (*p_ != '"') fail(GBJ_ERR_INVALID, "plan: expected a string key");
+          std::string k = str();
+          ws();
+          if (*p_ != ':') fail(GBJ_ERR_INVALID, "plan: expected ':'");
+          ++p_;
+          v.o.emplace_back(std::move(k), value());
+          ws();
+          if (*p_ == ',') { ++p_; continue; }
+          if (*p_ == '}') { ++p_; break; }
+          fail(GBJ_ERR_INVALID, "plan: expected ',' or '}'");
+        }
+      }
+    } else if (c == '[') {
+      v.t = JVal::Arr;
+      ++p_;
+      ws();
+      if (*p_ == ']') {
+        ++p_;
+      } else {
+        for (;;) {
+          v.a.push_back(value());
+          ws();
+          if (*p_ == ',') { ++p_; continue; }
+          if (*p_ == ']') { ++p_; break; }
+          fail(GBJ_ERR_INVALID, "plan: expected ',' or ']'");
+        }
+      }
+    } else if (c == '"') {
+      v.t = JVal::Str;
+      v.s = str();
+    } else if (!strncmp(p_, "true", 4)) {
+      v.t = JVal::Bool, v.b = true, p_ += 4;
+    } else if (!strncmp(p_, "false", 5)) {
+      v.t = JVal::Bool, v.b = false, p_ += 5;
+    } else if (!strncmp(p_, "null", 4)) {
+      p_ += 4;
+    } else if (c == '-' || (c >= '0' && c <= '9')) {
+      v.t = JVal::Num;
+      const char *st = p_;
+      if (*p_ == '-') ++p_;
+      while (*p_ >= '0' && *p_ <= '9') ++p_;
+      v.is_int = !(*p_ == '.' || *p_ == 'e' || *p_ == 'E');
+      if (v.is_int) {
+        v.i = strtoll(st, nullptr, 10);
+        v.num = (double)v.i;
+      } else {
+        char *end = nullptr;
+        v.num = strtod(st, &end);
+        p_ = end;
+        v.i = (int64_t)v.num;
+      }
+    } else {
+      fail(GBJ_ERR_INVALID, "plan: malformed JSON");
+    }
+    --depth_;
+    return v;
+  }
+  std::string str() {
+    std::string out;
+    ++p_;  // opening quote
+    while (*p_ && *p_ != '"') {
+      if (*p_ == '\\') {
+        ++p_;
+        switch (*p_) {
+          case 'n': out += '\n'; break;
+          case 't': out += '\t'; break;
+          case 'r': out += '\r'; break;
+          case 'b': out += '\b'; break;
+          case 'f': out += '\f'; break;
+          case 'u':  // names here are ASCII: a \uXXXX escape becomes '?'
+            out += '?';
+            for (int k = 0; k < 4 && p_[1]; ++k) ++p_;
+            break;
+          default: out += *p_;
+        }
+        if (*p_) ++p_;
+      } else {
+        out += *p_++;
+      }
+    }
+    if (*p_ != '"') fail(GBJ_ERR_INVALID, "plan: unterminated string");
+    ++p_;
+    return out;
+  }
+};
+
+const JVal &need(const JVal &v, const char *k, const char *op) {
+  const JVal *x = v.get(k);
+  if (!x) fail(GBJ_ERR_INVALID, std::string("plan: operator '") + op + "' needs field '" + k + "'");
+  return *x;
+}
+
+std::string op_name(const JVal &v) {
+  const JVal *o = v.get("operator");
+  if (!o || o->t != JVal::Str) fail(GBJ_ERR_INVALID, "plan: node without an \"operator\" string");
+  return o->s;
+}
+
+std::string expr_name(const JVal &e) {
+  const JVal *x = e.get("expression");
+  if (!x || x->t != JVal::Str) fail(GBJ_ERR_INVALID, "plan: expression without an \"expression\" string");
+  return x->s;
+}
+
+// Strips cast wrappers (int64 accumulation is how the library aggregates).
+const JVal &uncast(const JVal &e) {
+  const JVal *x = &e;
+  while (expr_name(*x) == "cast") x = &need(*x, "e", "cast");
+  return *x;
+}
+
+// (relName, attrName) of a recordProjection.
+std::pair<std::string, std::string> projection(const JVal &e) {
+  const JVal &x = uncast(e);
+  if (expr_name(x) != "recordProjection")
+    fail(GBJ_ERR_UNSUPPORTED, "plan: expected a column (recordProjection), got '" + expr_name(x) + "'");
+  const JVal &a = need(x, "attribute", "recordProjection");
+  const JVal *rel = a.get("relName"), *attr = a.get("attrName");
+  if (!attr || attr->t != JVal::Str) fail(GBJ_ERR_INVALID, "plan: attribute without attrName");
+  return {rel && rel->t == JVal::Str ? rel->s : std::string(), attr->s};
+}
+
+bool is_const(const JVal &e, int64_t *v) {
+  const JVal &x = uncast(e);
+  const std::string n = expr_name(x);
+  if (n != "int" && n != "int64") return false;
+  const JVal *c = x.get("v");
+  if (!c || c->t != JVal::Num) fail(GBJ_ERR_INVALID, "plan: constant without \"v\"");
+  *v = c->i;
+  return true;
+}
+
+int monoid(const std::string &m) {
+  if (m == "sum") return GBJ_AGG_SUM;
+  if (m == "max") return GBJ_AGG_MAX;
+  if (m == "min") return GBJ_AGG_MIN;
+  fail(GBJ_ERR_UNSUPPORTED, "plan: accumulator '" + m + "' is not supported (sum, max, min are)");
+}
+
+// Walks a plan checking operator names and required fields (no GPU work).
+void validate(const JVal &v) {
+  const std::string op = op_name(v);
+  if (op == "scan") {
+    const JVal &pl = need(v, "plugin", "scan");
+    need(pl, "name", "scan plugin");
+  } else if (op == "select") {
+    need(v, "p", "select");
+    validate(need(v, "input", "select"));
+  } else if (op == "hashjoin-chained" || op == "partitioned-hashjoin-chained") {
+    need(v, "build_k", op.c_str());
+    need(v, "probe_k", op.c_str());
+    validate(need(v, "build_input", op.c_str()));
+    validate(need(v, "probe_input", op.c_str()));
+  } else if (op == "join") {
+    need(v, "p", "join");
+    validate(need(v, "leftInput", "join"));
+    validate(need(v, "rightInput", "join"));
+  } else if (op == "groupby" || op == "hashgroupby-chained") {
+    need(v, "k", op.c_str());
+    const JVal &e = need(v, "e", op.c_str());
+    for (const JVal &x : e.a) {
+      need(x, "e", op.c_str());
+      monoid(need(x, "m", op.c_str()).s);
+    }
+    validate(need(v, "input", op.c_str()));
+  } else if (op == "reduce") {
+    const JVal &acc = need(v, "accumulator", "reduce");
+    for (const JVal &a : acc.a) monoid(a.s);
+    need(v, "e", "reduce");
+    validate(need(v, "input", "reduce"));
+  } else {
+    fail(GBJ_ERR_UNSUPPORTED, "plan: operator '" + op +
+                                  "' is not supported (scan, select, hashjoin-chained, "
+                                  "partitioned-hashjoin-chained, join, groupby, hashgroupby-chained, reduce are)");
+  }
+}
+
+}  // namespace
+
+// ------------------------------------------------------------- catalog
+struct gbj_catalog {
+  gbj_ctx *ctx = nullptr;
+  struct Col {
+    const int32_t *d;
+    uint64_t n;
+  };
+  std::map<std::pair<std::string, std::string>, Col> cols;
+  std::map<std::string, std::vector<std::string>> rel_attrs;
+};
+
+struct gbj_result {
+  std::vector<std::string> names;
+  std::vector<std::vector<int64_t>> cols;
+  uint64_t rows = 0;
+};
+
+namespace {
+
+// A relation during execution: int32 device columns of equal length.
+struct Rel {
+  uint64_t n = 0;
+  struct C {
+    std::string rel, attr;
+    const int32_t *d;
+  };
+  std::vector<C> cols;
+  const C *find(const std::pair<std::string, std::string> &ra) const {
+    for (const C &c : cols)
+      if (c.attr == ra.second && (ra.first.empty() || c.rel.empty() || c.rel == ra.first)) return &c;
+    return nullptr;
+  }
+};
+
+class Exec {
+ public:
+  Exec(gbj_catalog *cat) : cat_(cat), ctx_(cat->ctx) {}
+  ~Exec() {
+    for (void *p : allocs_) gbj_pool_free(ctx_, p);
+  }
+
+  gbj_result *run(const JVal &root) {
+    auto res = std::make_unique<gbj_result>();
+    const std::string op = op_name(root);
+    if (op == "reduce") {
+      reduce(root, res.get());
+    } else if (op == "groupby" || op == "hashgroupby-chained") {
+      groupby(root, res.get());
+    } else {
+      const Rel r = rel(root);
+      res->rows = r.n;
+      for (const auto &c : r.cols) {
+        res->names.push_back(c.rel.empty() ? c.attr : c.rel + "." + c.attr);
+        res->cols.push_back(to_host32(c.d, r.n));
+      }
+    }
+    return res.release();
+  }
+
+ private:
+  gbj_catalog *cat_;
+  gbj_ctx *ctx_;
+  std::vector<void *> allocs_;
+
+  void ck(int rc, const char *what) {
+    if (rc != GBJ_OK) fail(rc, std::string(what) + ": " + gbj_last_error(ctx_));
+  }
+  template <typename T>
+  T *alloc(uint64_t n) {
+    void *p = nullptr;
+    ck(gbj_pool_alloc(ctx_, std::max<uint64_t>(n, 1) * sizeof(T), &p), "pool");
+    allocs_.push_back(p);
+    return static_cast<T *>(p);
+  }
+  void sync() { ck(gbj_sync(ctx_, nullptr), "sync"); }
+  template <typename T>
+  T read1(const T *d) {
+    T v{};
+    sync();
+    if (cudaMemcpy(&v, d, sizeof(T), cudaMemcpyDeviceToHost) != cudaSuccess) fail(GBJ_ERR_CUDA, "plan: copy");
+    return v;
+  }
+  std::vector<int64_t> to_host32(const int32_t *d, uint64_t n) {
+    std::vector<int32_t> h(n);
+    sync();
+    if (n && cudaMemcpy(h.data(), d, n * 4, cudaMemcpyDeviceToHost) != cudaSuccess) fail(GBJ_ERR_CUDA, "plan: copy");
+    return std::vector<int64_t>(h.begin(), h.end());
+  }
+  std::vector<int64_t> to_host64(const int64_t *d, uint64_t n) {
+    std::vector<int64_t> h(n);
+    sync();
+    if (n && cudaMemcpy(h.data(), d, n * 8, cudaMemcpyDeviceToHost) != cudaSuccess) fail(GBJ_ERR_CUDA, "plan: copy");
+    return h;
+  }
+
+  const int32_t *column(const Rel &r, const JVal &e) {
+    const auto ra = projection(e);
+    const Rel::C *c = r.find(ra);
+    if (!c) fail(GBJ_ERR_INVALID, "plan: column " + ra.first + "." + ra.second + " is not in the operator's input");
+    return c->d;
+  }
+
+  Rel rel(const JVal &v) {
+    const std::string op = op_name(v);
+    if (op == "scan") return scan(v);
+    if (op == "select") return select(v);
+    if (op == "hashjoin-chained" || op == "partitioned-hashjoin-chained" || op == "join") return join(v);
+    if (op == "groupby" || op == "hashgroupby-chained" || op == "reduce")
+      fail(GBJ_ERR_UNSUPPORTED, "plan: '" + op + "' is supported only as the plan's root");
+    validate(v);  // raises the unsupported-operator error
+    fail(GBJ_ERR_UNSUPPORTED, "plan: operator '" + op + "'");
+  }
+
+  Rel scan(const JVal &v) {
+    const JVal &pl = need(v, "plugin", "scan");
+    const std::string name = need(pl, "name", "scan plugin").s;
+    auto it = cat_->rel_attrs.find(name);
+    if (it == cat_->rel_attrs.end()) fail(GBJ_ERR_INVALID, "plan: relation '" + name + "' is not in the catalog");
+    std::vector<std::string> attrs = it->second;
+    if (const JVal *pr = pl.get("projections")) {
+      attrs.clear();
+      for (const JVal &a : pr->a) {
+        const JVal *an = a.get("attrName");
+        if (!an) fail(GBJ_ERR_INVALID, "plan: projection without attrName");
+        attrs.push_back(an->s);
+      }
+    }
+    Rel r;
+    bool first = true;
+    for (const std::string &a : attrs) {
+      auto c = cat_->cols.find({name, a});
+      if (c == cat_->cols.end()) fail(GBJ_ERR_INVALID, "plan: column " + name + "." + a + " is not in the catalog");
+      if (!first && c->second.n != r.n) fail(GBJ_ERR_INVALID, "plan: columns of " + name + " differ in length");
+      r.n = c->second.n;
+      first = false;
+      r.cols.push_back({name, a, c->second.d});
+    }
+    if (first) r.n = 0;
+    return r;
+  }
+
+  // Conjunction of column-vs-constant comparisons -> per-column [lo, hi].
+  void ranges(const JVal &p, std::vector<std::tuple<std::pair<std::string, std::string>, int32_t, int32_t>> &out) {
+    const JVal &x = uncast(p);
+    const std::string n = expr_name(x);
+    if (n == "bool") {
+      const JVal *b = x.get("v");
+      if (b && b->t == JVal::Bool && b->b) return;
+      out.push_back({{"", ""}, 1, 0});  // always false: empty range
+      return;
+    }
+    if (n == "and") {
+      ranges(need(x, "left", "and"), out);
+      ranges(need(x, "right", "and"), out);
+      return;
+    }
+    if (n != "eq" && n != "lt" && n != "le" && n != "gt" && n != "ge")
+      fail(GBJ_ERR_UNSUPPORTED, "plan: predicate '" + n + "' is not supported (eq, lt, le, gt, ge, and are)");
+    const JVal &l = need(x, "left", n.c_str()), &r = need(x, "right", n.c_str());
+    int64_t c = 0;
+    std::string cmp = n;
+    const JVal *col = &l;
+    if (is_const(l, &c)) {  // constant on the left: mirror the comparison
+      col = &r;
+      cmp = n == "lt" ? "gt" : n == "le" ? "ge" : n == "gt" ? "lt" : n == "ge" ? "le" : n;
+    } else if (!is_const(r, &c)) {
+      fail(GBJ_ERR_UNSUPPORTED, "plan: predicates compare a column with a constant");
+    }
+    int64_t lo = INT32_MIN, hi = INT32_MAX;
+    if (cmp == "eq") lo = hi = c;
+    if (cmp == "lt") hi = c - 1;
+    if (cmp == "le") hi = c;
+    if (cmp == "gt") lo = c + 1;
+    if (cmp == "ge") lo = c;
+    if (lo > INT32_MAX || hi < INT32_MIN || lo > hi) {
+      out.push_back({{"", ""}, 1, 0});
+      return;
+    }
+    out.push_back({projection(*col), (int32_t)std::max<int64_t>(lo, INT32_MIN),
+                   (int32_t)std::min<int64_t>(hi, INT32_MAX)});
+  }
+
+  // Rows of `r` kept by `rows` (positions), every column gathered.
+  Rel gather(const Rel &r, const int32_t *rows, uint64_t n) {
+    Rel o;
+    o.n = n;
+    for (const auto &c : r.cols) {
+      int32_t *d = alloc<int32_t>(n);
+      if (n) ck(gbj_gather(ctx_, c.d, rows, n, d, nullptr), "gather");
+      o.cols.push_back({c.rel, c.attr, d});
+    }
+    return o;
+  }
+
+  Rel select(const JVal &v) {
+    Rel in = rel(need(v, "input", "select"));
+    std::vector<std::tuple<std::pair<std::string, std::string>, int32_t, int32_t>> rg;
+    ranges(need(v, "p", "select"), rg);
+    for (const auto &t : rg) {
+      if (std::get<1>(t) > std::get<2>(t)) return gather(in, nullptr, 0);  // always false
+      const Rel::C *c = in.find(std::get<0>(t));
+      if (!c) fail(GBJ_ERR_INVALID, "plan: select column " + std::get<0>(t).second + " is not in its input");
+      int32_t *rows = alloc<int32_t>(in.n);
+      uint64_t *cnt = alloc<uint64_t>(1);
+      ck(gbj_select_range(ctx_, c->d, in.n, std::get<1>(t), std::get<2>(t), rows, cnt, nullptr), "select");
+      const uint64_t k = read1(cnt);
+      in = gather(in, rows, k);
+    }
+    return in;
+  }
+
+  struct JoinSides {
+    const JVal *build, *probe, *bk, *pk;
+    int32_t hash_bits = 0;
+    uint64_t max_build = 0;
+    bool radix = false;
+  };
+  JoinSides sides(const JVal &v) {
+    const std::string op = op_name(v);
+    JoinSides s{};
+    if (op == "join") {
+      const JVal &p = uncast(need(v, "p", "join"));
+      if (expr_name(p) != "eq") fail(GBJ_ERR_UNSUPPORTED, "plan: join predicates must be eq");
+      s.build = &need(v, "leftInput", "join");
+      s.probe = &need(v, "rightInput", "join");
+      s.bk = &need(p, "left", "eq");
+      s.pk = &need(p, "right", "eq");
+      s.radix = true;
+    } else {
+      s.build = &need(v, "build_input", op.c_str());
+      s.probe = &need(v, "probe_input", op.c_str());
+      s.bk = &need(v, "build_k", op.c_str());
+      s.pk = &need(v, "probe_k", op.c_str());
+      if (const JVal *h = v.get("hash_bits")) s.hash_bits = (int32_t)h->i;
+      if (const JVal *m = v.get("maxBuildInputSize")) s.max_build = (uint64_t)std::max<int64_t>(m->i, 0);
+      s.radix = op == "partitioned-hashjoin-chained";
+    }
+    return s;
+  }
+
+  Rel join(const JVal &v) {
+    const JoinSides s = sides(v);
+    const Rel b = rel(*s.build), p = rel(*s.probe);
+    const int32_t *bk = column(b, *s.bk), *pk = column(p, *s.pk);
+    gbj_table *t = nullptr;
+    ck(gbj_join_build(ctx_, bk, nullptr, b.n, s.hash_bits, std::max<uint64_t>(s.max_build, b.n), nullptr, &t),
+       "join build");
+    struct TableGuard {
+      gbj_ctx *c;
+      gbj_table *t;
+      ~TableGuard() { gbj_table_destroy(c, t); }
+    } guard{ctx_, t};
+    // count the matches, then write the pairs
+    const gbj_agg cnt_agg{GBJ_AGG_COUNT, GBJ_VAL_ONE};
+    int64_t *dcnt = alloc<int64_t>(1);
+    ck(gbj_join_probe_agg(ctx_, t, pk, nullptr, p.n, &cnt_agg, 1, dcnt, nullptr), "join probe");
+    const uint64_t m = (uint64_t)read1(dcnt);
+    int32_t *br = alloc<int32_t>(m), *pr = alloc<int32_t>(m);
+    uint64_t *dm = alloc<uint64_t>(1);
+    ck(gbj_join_probe_pairs(ctx_, t, pk, nullptr, p.n, br, pr, m, dm, nullptr), "join pairs");
+    sync();
+    Rel o = gather(b, br, m);
+    const Rel po = gather(p, pr, m);
+    o.cols.insert(o.cols.end(), po.cols.begin(), po.cols.end());
+    return o;
+  }
+
+  // Operand of a fused join aggregate, or -1 if the expression needs more.
+  struct Operand {
+    int operand;
+    int64_t scale;  // constants: sum of v over n rows = v * count
+  };
+  bool fusable(const JVal &e, const Rel &b, const Rel &p, const JoinSides &s, const int32_t **bcol,
+               const int32_t **pcol, Operand *out) {
+    const JVal &x = uncast(e);
+    int64_t c = 0;
+    if (is_const(x, &c)) {
+      *out = {GBJ_VAL_ONE, c};
+      return true;
+    }
+    auto side_of = [&](const JVal &col, int *which, const int32_t **d) {
+      const auto ra = projection(col);
+      if (const Rel::C *bc = b.find(ra)) {
+        *which = 0, *d = bc->d;
+        return true;
+      }
+      if (const Rel::C *pc = p.find(ra)) {
+        *which = 1, *d = pc->d;
+        return true;
+      }
+      return false;
+    };
+    auto take = [&](int which, const int32_t *d) {
+      const int32_t **slot = which == 0 ? bcol : pcol;
+      if (*slot && *slot != d) return false;
+      *slot = d;
+      return true;
+    };
+    const std::string n = expr_name(x);
+    if (n == "recordProjection") {
+      int w;
+      const int32_t *d;
+      if (!side_of(x, &w, &d)) return false;
+      if (w == 0 && projection(x) == projection(*s.bk)) {
+        *out = {GBJ_VAL_BUILD_KEY, 1};
+        return true;
+      }
+      if (!take(w, d)) return false;
+      *out = {w == 0 ? GBJ_VAL_BUILD : GBJ_VAL_PROBE, 1};
+      return true;
+    }
+    if (n == "multiply") {
+      int w1, w2;
+      const int32_t *d1, *d2;
+      if (!side_of(uncast(need(x, "left", "multiply")), &w1, &d1) ||
+          !side_of(uncast(need(x, "right", "multiply")), &w2, &d2) || w1 == w2)
+        return false;
+      if (!take(w1, d1) || !take(w2, d2)) return false;
+      *out = {GBJ_VAL_PRODUCT, 1};
+      return true;
+    }
+    return false;
+  }
+
+  void reduce(const JVal &v, gbj_result *res) {
+    const JVal &es = need(v, "e", "reduce"), &acc = need(v, "accumulator", "reduce");
+    if (es.a.size() != acc.a.size() || es.a.empty() || es.a.size() > GBJ_MAX_AGGS)
+      fail(GBJ_ERR_INVALID, "plan: reduce needs 1..8 expressions, one accumulator each");
+    const JVal &in = need(v, "input", "reduce");
+    const std::string iop = op_name(in);
+    std::vector<int64_t> out(es.a.size());
+    bool done = false;
+    if (iop == "hashjoin-chained" || iop == "partitioned-hashjoin-chained" || iop == "join") {
+      const JoinSides s = sides(in);
+      const Rel b = rel(*s.build), p = rel(*s.probe);
+      const int32_t *bcol = nullptr, *pcol = nullptr;
+      std::vector<Operand> ops(es.a.size());
+      bool ok = true;
+      for (size_t j = 0; j < es.a.size() && ok; ++j) ok = fusable(es.a[j], b, p, s, &bcol, &pcol, &ops[j]);
+      if (ok) {
+        // constant operands are computed from the match count
+        std::vector<gbj_agg> aggs(es.a.size());
+        for (size_t j = 0; j < es.a.size(); ++j)
+          aggs[j] = {ops[j].operand == GBJ_VAL_ONE ? GBJ_AGG_COUNT : monoid(acc.a[j].s), ops[j].operand};
+        int64_t *d = alloc<int64_t>(aggs.size());
+        const int32_t *bk = column(b, *s.bk), *pk = column(p, *s.pk);
+        if (s.radix) {
+          ck(gbj_radix_join_agg(ctx_, bk, bcol, b.n, pk, pcol, p.n, nullptr, aggs.data(), (int32_t)aggs.size(), d,
+                                nullptr),
+             "radix join");
+        } else {
+          gbj_table *t = nullptr;
+          ck(gbj_join_build(ctx_, bk, bcol, b.n, s.hash_bits, std::max<uint64_t>(s.max_build, b.n), nullptr, &t),
+             "join build");
+          const int rc = gbj_join_probe_agg(ctx_, t, pk, pcol, p.n, aggs.data(), (int32_t)aggs.size(), d, nullptr);
+          gbj_table_destroy(ctx_, t);
+          ck(rc, "join probe");
+        }
+        const std::vector<int64_t> h = to_host64(d, aggs.size());
+        for (size_t j = 0; j < aggs.size(); ++j) {
+          int64_t x = h[j];
+          if (ops[j].operand == GBJ_VAL_ONE) {  // sum = v * count; max/min = v if any match
+            const int m = monoid(acc.a[j].s);
+            x = m == GBJ_AGG_SUM ? ops[j].scale * h[j]
+                                 : (h[j] ? ops[j].scale : (m == GBJ_AGG_MAX ? INT64_MIN : INT64_MAX));
+          }
+          out[j] = x;
+        }
+        done = true;
+      }
+    }
+    if (!done) {
+      const Rel r = rel(in);
+      for (size_t j = 0; j < es.a.size(); ++j) {
+        const int m = monoid(acc.a[j].s);
+        int64_t c = 0;
+        if (is_const(es.a[j], &c)) {
+          out[j] = m == GBJ_AGG_SUM ? c * (int64_t)r.n : (r.n ? c : (m == GBJ_AGG_MAX ? INT64_MIN : INT64_MAX));
+          continue;
+        }
+        const int32_t *col = column(r, es.a[j]);
+        const gbj_agg a{m, GBJ_VAL_PROBE};
+        int64_t *d = alloc<int64_t>(1);
+        ck(gbj_reduce(ctx_, col, nullptr, r.n, &a, 1, d, nullptr), "reduce");
+        out[j] = to_host64(d, 1)[0];
+      }
+    }
+    res->rows = 1;
+    for (size_t j = 0; j < out.size(); ++j) {
+      res->names.push_back(acc.a[j].s + "_" + std::to_string(j));
+      res->cols.push_back({out[j]});
+    }
+  }
+
+  void groupby(const JVal &v, gbj_result *res) {
+    const char *op = "groupby";
+    const JVal &ks = need(v, "k", op), &es = need(v, "e", op);
+    if (ks.t != JVal::Arr || ks.a.size() != 1)
+      fail(GBJ_ERR_UNSUPPORTED, "plan: group-by takes one int32 key expression");
+    const Rel r = rel(need(v, "input", op));
+    const int32_t *key = column(r, ks.a[0]);
+    gbj_groupby_params prm{};
+    if (const JVal *h = v.get("hash_bits")) prm.hash_bits = (int32_t)h->i;
+    if (const JVal *m = v.get("maxInputSize")) prm.max_input_size = (uint64_t)std::max<int64_t>(m->i, 0);
+    // one gbj_groupby per distinct value column (COUNT/SUM/MIN/MAX of it);
+    // constants need only the counts
+    std::vector<const int32_t *> vcols;
+    std::vector<std::pair<int, int64_t>> spec;  // (value column index or -1, constant)
+    for (const JVal &x : es.a) {
+      int64_t c = 0;
+      if (is_const(need(x, "e", op), &c)) {
+        spec.push_back({-1, c});
+        continue;
+      }
+      const int32_t *col = column(r, need(x, "e", op));
+      auto it = std::find(vcols.begin(), vcols.end(), col);
+      spec.push_back({(int)(it - vcols.begin()), 0});
+      if (it == vcols.end()) vcols.push_back(col);
+    }
+    if (vcols.empty()) vcols.push_back(key);  // counts of the key column
+    const uint64_t cap = std::max<uint64_t>(r.n, 1);
+    std::map<int32_t, std::vector<int64_t>> groups;  // key -> per value column: cnt, sum, min, max
+    for (size_t i = 0; i < vcols.size(); ++i) {
+      int32_t *ok = alloc<int32_t>(cap);
+      int64_t *oc = alloc<int64_t>(cap), *os = alloc<int64_t>(cap);
+      int32_t *omn = alloc<int32_t>(cap), *omx = alloc<int32_t>(cap);
+      uint64_t *ng = alloc<uint64_t>(1);
+      ck(gbj_groupby(ctx_, key, vcols[i], r.n, &prm, ok, oc, os, omn, omx, cap, ng, nullptr), "groupby");
+      const uint64_t n = read1(ng);
+      const auto hk = to_host32(ok, n), hmn = to_host32(omn, n), hmx = to_host32(omx, n);
+      const auto hc = to_host64(oc, n), hs = to_host64(os, n);
+      for (uint64_t g = 0; g < n; ++g) {
+        auto &row = groups[(int32_t)hk[g]];
+        row.resize(4 * vcols.size());
+        row[4 * i] = hc[g], row[4 * i + 1] = hs[g], row[4 * i + 2] = hmn[g], row[4 * i + 3] = hmx[g];
+      }
+    }
+    res->rows = groups.size();
+    res->names.push_back(projection(ks.a[0]).second);
+    res->cols.emplace_back();
+    for (size_t j = 0; j < es.a.size(); ++j) {
+      res->names.push_back(need(es.a[j], "m", op).s + "_" + std::to_string(j));
+      res->cols.emplace_back();
+    }
+    for (const auto &kv : groups) {  // sorted by key
+      res->cols[0].push_back(kv.first);
+      for (size_t j = 0; j < spec.size(); ++j) {
+        const int m = monoid(need(es.a[j], "m", op).s);
+        const int vi = spec[j].first;
+        const int64_t cnt = kv.second[4 * std::max(vi, 0)];
+        int64_t x;
+        if (vi < 0) x = m == GBJ_AGG_SUM ? spec[j].second * cnt : spec[j].second;
+        else x = kv.second[4 * vi + (m == GBJ_AGG_SUM ? 1 : m == GBJ_AGG_MIN ? 2 : 3)];
+        res->cols[1 + j].push_back(x);
+      }
+    }
+  }
+};
+
+}  // namespace
+
+extern "C" int gbj_catalog_create(gbj_ctx *ctx, gbj_catalog **out) {
+  if (!ctx || !out) return GBJ_ERR_INVALID;
+  *out = new gbj_catalog();
+  (*out)->ctx = ctx;
+  return GBJ_OK;
+}
+
+extern "C" int gbj_catalog_add_column(gbj_catalog *cat, const char *rel, const char *attr, const int32_t *d_col,
+                                      uint64_t n) {
+  if (!cat || !rel || !attr || (n && !d_col)) return GBJ_ERR_INVALID;
+  const std::pair<std::string, std::string> k{rel, attr};
+  auto &attrs = cat->rel_attrs[rel];
+  if (!cat->cols.count(k)) attrs.push_back(attr);
+  cat->cols[k] = {d_col, n};
+  return GBJ_OK;
+}
+
+extern "C" int gbj_catalog_destroy(gbj_catalog *cat) {
+  delete cat;
+  return GBJ_OK;
+}
+
+extern "C" int gbj_plan_validate(const char *plan_json, char *err, uint64_t err_len) {
+  if (!plan_json) return GBJ_ERR_INVALID;
+  try {
+    validate(JsonParser(plan_json).parse());
+    if (err && err_len) err[0] = 0;
+    return GBJ_OK;
+  } catch (const PlanError &e) {
+    if (err && err_len) snprintf(err, err_len, "%s", e.msg.c_str());
+    return e.code;
+  }
+}
+
+extern "C" int gbj_plan_execute(gbj_catalog *cat, const char *plan_json, gbj_result **out) {
+  if (!cat || !plan_json || !out) return GBJ_ERR_INVALID;
+  *out = nullptr;
+  try {
+    const JVal root = JsonParser(plan_json).parse();
+    validate(root);
+    Exec ex(cat);
+    *out = ex.run(root);
+    return GBJ_OK;
+  } catch (const PlanError &e) {
+    return set_error(cat->ctx, e.code, e.msg);
+  } catch (const std::exception &e) {
+    return set_error(cat->ctx, GBJ_ERR_INVALID, std::string("plan: ") + e.what());
+  }
+}
+
+extern "C" int gbj_result_shape(const gbj_result *r, int32_t *n_cols, uint64_t *n_rows) {
+  if (!r) return GBJ_ERR_INVALID;
+  if (n_cols) *n_cols = (int32_t)r->cols.size();
+  if (n_rows) *n_rows = r->rows;
+  return GBJ_OK;
+}
+
+extern "C" const char *gbj_result_name(const gbj_result *r, int32_t col) {
+  if (!r || col < 0 || col >= (int32_t)r->names.size()) return nullptr;
+  return r->names[col].c_str();
+}
+
+extern "C" int gbj_result_column(const gbj_result *r, int32_t col, int64_t *h_out) {
+  if (!r || !h_out || col < 0 || col >= (int32_t)r->cols.size()) return GBJ_ERR_INVALID;
+  std::copy(r->cols[col].begin(), r->cols[col].end(), h_out);
+  return GBJ_OK;
+}
+
+extern "C" void gbj_result_destroy(gbj_result *r) { delete r; }
