@@ -78,7 +78,8 @@ class RadixJoin:
                             f"S=2^{self.ls} int32 keys (50% hits, Zipf theta 0/0.5/1.0), "
                             f"COUNT + SUM(rowid xor)",
                 "n_build": self.nr, "n_probe": self.ns, "thetas": list(self.THETAS),
-                "hit_rate": 0.5, "l2": "inputs larger than L2 (2 GiB probe keys per join)"}
+                "hit_rate": 0.5, "l2": "inputs larger than L2 (2 GiB probe keys per join)",
+                "radix_bits": getattr(self, "tuned_bits", None), "radix_bits_from": "autotuner"}
 
     def generate(self):
         from proteus_gb300 import engine
@@ -97,6 +98,9 @@ class RadixJoin:
         self.d_r = torch.from_numpy(self.rk).cuda()
         self.d_s = [torch.from_numpy(s).cuda() for s in self.sks]
         self.outs = [torch.empty(2, dtype=torch.int64, device="cuda") for _ in self.THETAS]
+        # the autotuner picks the partition bits for this shape (untimed);
+        # every timed join then runs with the cached choice
+        self.tuned_bits, self.tune_ms = ctx.autotune_radix_join(self.d_r, None, self.d_s[0], None, self.aggs)
 
     def step(self):
         for ds, o in zip(self.d_s, self.outs):

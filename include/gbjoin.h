@@ -411,6 +411,47 @@ int gbj_server_stats(gbj_server *srv, uint64_t *completed, uint64_t *batches,
 /* Drains, stops the request loop and frees the server. */
 int gbj_server_destroy(gbj_server *srv);
 
+/* -------------------------------------------------------------- autotuner */
+/* Times candidate plans on the caller's inputs (one warm-up run, then the
+ * fastest of two timed runs, CUDA events on `stream`) and caches the winner
+ * in the context under the operation and the log2 sizes of its inputs.
+ * Later calls of that shape that pass no explicit sizing use it:
+ *   radix join     partition bits 1..15 (bits > 8 means two passes) --
+ *                  gbj_radix_join_agg with params NULL or zero bits;
+ *   plain join     table size 2^hash_bits (load factor 1/2, 1/4, 1/8) --
+ *                  gbj_join_build with hash_bits 0;
+ *   group-by       strategy 1, or strategy 2 with its partition bits --
+ *                  gbj_groupby with strategy 0 and the same
+ *                  expected_groups.
+ * The reference sizes these by hand per plan (hash_bits, maxInputSize) and
+ * fixes its radix bits at compile time (NUM_RADIX_BITS,
+ * core/platform/lib/util/radix/joins/radix-join.cpp). */
+int gbj_autotune_radix_join(gbj_ctx *ctx, const int32_t *d_build_keys,
+                            const int32_t *d_build_payload, uint64_t n_build,
+                            const int32_t *d_probe_keys,
+                            const int32_t *d_probe_payload, uint64_t n_probe,
+                            const gbj_agg *aggs, int32_t n_aggs,
+                            int32_t *best_bits, double *best_ms, void *stream);
+int gbj_autotune_join(gbj_ctx *ctx, const int32_t *d_build_keys,
+                      const int32_t *d_build_payload, uint64_t n_build,
+                      const int32_t *d_probe_keys,
+                      const int32_t *d_probe_payload, uint64_t n_probe,
+                      const gbj_agg *aggs, int32_t n_aggs,
+                      int32_t *best_hash_bits, double *best_ms, void *stream);
+int gbj_autotune_groupby(gbj_ctx *ctx, const int32_t *d_keys,
+                         const int32_t *d_values, uint64_t n,
+                         uint64_t expected_groups, int32_t *best_strategy,
+                         int32_t *best_bits, double *best_ms, void *stream);
+/* Cached decision for op "radix" (a = n_build, b = n_probe), "join"
+ * (a = n_build, b = 0) or "groupby" (a = n, b = expected_groups; value =
+ * strategy << 8 | bits); -1 when none. */
+int gbj_tune_lookup(gbj_ctx *ctx, const char *op, uint64_t a, uint64_t b,
+                    int32_t *value);
+int gbj_tune_clear(gbj_ctx *ctx);
+/* Text file, one "op log2a log2b value" line per decision. */
+int gbj_tune_save(gbj_ctx *ctx, const char *path);
+int gbj_tune_load(gbj_ctx *ctx, const char *path);
+
 /* ------------------------------------------------------------ plan façade */
 /* Executes a JSON plan in the reference's plan format (operator names and
  * fields of core/olap/lib/plan/plan-parser.cpp; expressions of

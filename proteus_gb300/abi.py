@@ -127,6 +127,13 @@ SIGNATURES = {
     "gbj_server_drain": (C.c_int, [vp]),
     "gbj_server_stats": (C.c_int, [vp, P(u64), P(u64), P(u64)]),
     "gbj_server_destroy": (C.c_int, [vp]),
+    "gbj_autotune_radix_join": (C.c_int, [vp, vp, vp, u64, vp, vp, u64, P(Agg), i32, P(i32), P(dbl), vp]),
+    "gbj_autotune_join": (C.c_int, [vp, vp, vp, u64, vp, vp, u64, P(Agg), i32, P(i32), P(dbl), vp]),
+    "gbj_autotune_groupby": (C.c_int, [vp, vp, vp, u64, u64, P(i32), P(i32), P(dbl), vp]),
+    "gbj_tune_lookup": (C.c_int, [vp, C.c_char_p, u64, u64, P(i32)]),
+    "gbj_tune_clear": (C.c_int, [vp]),
+    "gbj_tune_save": (C.c_int, [vp, C.c_char_p]),
+    "gbj_tune_load": (C.c_int, [vp, C.c_char_p]),
     "gbj_catalog_create": (C.c_int, [vp, P(vp)]),
     "gbj_catalog_add_column": (C.c_int, [vp, C.c_char_p, C.c_char_p, vp, u64]),
     "gbj_catalog_destroy": (C.c_int, [vp]),

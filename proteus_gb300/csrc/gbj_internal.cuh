@@ -65,6 +65,8 @@ struct gbj_ctx {
   std::vector<cudaEvent_t> prof_events;
   std::unordered_map<cudaStream_t, cudaEvent_t> prof_last;
   std::map<std::string, std::pair<uint64_t, double>> prof_totals;
+  // autotuner decisions: "<op> <log2 size> <log2 size>" -> chosen value
+  std::map<std::string, int32_t> tuned;
 };
 
 struct gbj_table {
@@ -130,6 +132,10 @@ int after_launch(gbj_ctx *ctx, const char *name, cudaStream_t s);
 void prof_mark(gbj_ctx *ctx, cudaStream_t s);
 
 int validate_aggs(gbj_ctx *ctx, const gbj_agg *aggs, int32_t n_aggs);
+
+// Autotuner cache (keys built by tune_key; -1 = no decision yet).
+std::string tune_key(const char *op, uint64_t a, uint64_t b);
+int32_t tuned_value(gbj_ctx *ctx, const std::string &key);
 
 // Kernel-side aggregate description (passed by value).
 struct AggSpec {

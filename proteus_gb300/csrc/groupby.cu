@@ -456,6 +456,14 @@ extern "C" int gbj_groupby(gbj_ctx *ctx, const int32_t *d_keys, const int32_t *d
     strategy = params->strategy;
   }
   if (strategy < 0 || strategy > 2) return set_error(ctx, GBJ_ERR_INVALID, "groupby: bad strategy");
+  int32_t tuned_bits = 0;
+  if (strategy == 0) {  // an autotuned plan for this (rows, groups) bucket, if any
+    const int32_t tv = tuned_value(ctx, tune_key("groupby", n, hint));
+    if (tv > 0) {
+      strategy = tv >> 8;
+      tuned_bits = tv & 0xff;
+    }
+  }
   const uint64_t groups_cap =
       std::max<uint64_t>(1024, hint ? std::min<uint64_t>(hint, n) : std::min<uint64_t>(n, 1ull << 24));
   if (strategy == 0) strategy = (hint && hint <= kSlots / 2) ? 1 : (hint ? 2 : 1);
@@ -515,6 +523,7 @@ extern "C" int gbj_groupby(gbj_ctx *ctx, const int32_t *d_keys, const int32_t *d
     while (bits < free_bits && (n >> bits) > w / 2) ++bits;
     if (params && params->hash_bits > 0 && strategy == 2 && !hint)
       bits = std::min(params->hash_bits, kMaxPartBits);
+    if (tuned_bits > 0) bits = std::min<int>(tuned_bits, kMaxPartBits);
     const uint32_t P = 1u << bits;
     tslots_arg = (uint32_t)std::min<uint64_t>(
         kSlots, std::max<uint64_t>(64, next_pow2(4 * ((groups_cap + P - 1) >> bits))));

@@ -684,6 +684,11 @@ int gbj_radix_join_agg(gbj_ctx *ctx, const int32_t *d_build_keys,
     if (mean + 5.0 * std::sqrt(mean) <= (double)kRMax) break;
     ++bits;
   }
+  const bool explicit_bits = params && (params->log_parts > 0 || params->bits > 0);
+  if (!explicit_bits) {  // an autotuned choice for this size bucket, if any
+    const int32_t tb = tuned_value(ctx, tune_key("radix", n_build, n_probe));
+    if (tb > 0) bits = std::min<int>(tb, kMaxPartBits);
+  }
   if (params && params->log_parts > 0) bits = std::min(params->log_parts, kMaxPartBits);
   if (params && params->bits > 0) bits = std::min(params->bits, kMaxPartBits);
   if (params && params->passes > 2)

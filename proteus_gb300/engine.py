@@ -169,6 +169,47 @@ class Context:
                                           bits, _ptr(ok), _ptr(op), _ptr(off), self._s(stream)))
         return ok[:n], op[:n], off
 
+    # ---------------------------------------------------------- autotuner
+    def autotune_radix_join(self, bkeys, bpay, pkeys, ppay, aggs, stream=None):
+        """-> (partition bits, ms); later radix joins of this shape use it."""
+        arr = abi.aggs_array(aggs)
+        b, ms = C.c_int32(), C.c_double()
+        self.check(self.lib.gbj_autotune_radix_join(
+            self.handle, _ptr(bkeys), _ptr(bpay), bkeys.numel(), _ptr(pkeys), _ptr(ppay), pkeys.numel(),
+            arr, len(aggs), C.byref(b), C.byref(ms), self._s(stream)))
+        return b.value, ms.value
+
+    def autotune_join(self, bkeys, bpay, pkeys, ppay, aggs, stream=None):
+        """-> (hash_bits, ms); later builds of this size use it."""
+        arr = abi.aggs_array(aggs)
+        b, ms = C.c_int32(), C.c_double()
+        self.check(self.lib.gbj_autotune_join(
+            self.handle, _ptr(bkeys), _ptr(bpay), bkeys.numel(), _ptr(pkeys), _ptr(ppay), pkeys.numel(),
+            arr, len(aggs), C.byref(b), C.byref(ms), self._s(stream)))
+        return b.value, ms.value
+
+    def autotune_groupby(self, keys, values, expected_groups, stream=None):
+        """-> (strategy, bits, ms); later group-bys of this shape use it."""
+        st, b, ms = C.c_int32(), C.c_int32(), C.c_double()
+        self.check(self.lib.gbj_autotune_groupby(self.handle, _ptr(keys), _ptr(values), keys.numel(),
+                                                 expected_groups, C.byref(st), C.byref(b), C.byref(ms),
+                                                 self._s(stream)))
+        return st.value, b.value, ms.value
+
+    def tune_lookup(self, op: str, a: int, b: int) -> int:
+        v = C.c_int32()
+        self.check(self.lib.gbj_tune_lookup(self.handle, op.encode(), a, b, C.byref(v)))
+        return v.value
+
+    def tune_save(self, path: str):
+        self.check(self.lib.gbj_tune_save(self.handle, path.encode()))
+
+    def tune_load(self, path: str):
+        self.check(self.lib.gbj_tune_load(self.handle, path.encode()))
+
+    def tune_clear(self):
+        self.check(self.lib.gbj_tune_clear(self.handle))
+
     # ----------------------------------------------------------- group-by
     def groupby(self, keys, values, out_capacity, expected_groups=0, max_input_size=0,
                 hash_bits=0, strategy=0, stream=None):
