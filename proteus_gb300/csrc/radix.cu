@@ -13,12 +13,15 @@
 //
 // GB300 layout:
 //  * a histogram kernel counts the final partition ids (<= 2^15) once;
-//  * each pass (<= 8 digit bits) sorts 4096-tuple tiles by digit in shared
+//  * each pass (<= 8 digit bits) sorts 2048-tuple tiles by digit in shared
 //    memory (one histogram row per warp gives every tuple its rank), takes
 //    one output range per digit with a single global atomic, and writes the
 //    tile digit-run by digit-run, so stores are coalesced and at most 256
 //    output regions are open per pass (the first pass of a 2^14 fan-out
-//    writes 128 regions; the second writes inside one 32 MB bucket);
+//    writes 128 regions; the second writes inside one 32 MB bucket).  The
+//    pass is software-pipelined: a CTA issues the next tile's loads as soon
+//    as the current tile sits in shared memory, and the output-range atomic
+//    is in flight while the tile is scattered on chip;
 //  * radix bits are chosen so the largest build partition fits an on-chip
 //    table of kRMax tuples (the bench's 2^27-row side: 16384 partitions of
 //    8192 +- 90 tuples);
@@ -92,7 +95,7 @@ struct TileSmem {
 // digit = (f(key) >> dshift) & dmask; the output cursor of (bucket b,
 // digit d) is cursor[b * (dmask + 1) + d].
 template <int kDigit, bool kPairsIn, bool kAoSOut>
-__global__ void __launch_bounds__(kTileThreads, 4)
+__global__ void __launch_bounds__(kTileThreads, 3)  // 3 CTAs: no spills at 42 registers
     k_tile_pass(const int32_t *__restrict__ keys, const int32_t *__restrict__ vals,
                 const int2 *__restrict__ pin, uint64_t n, int dshift, uint32_t dmask,
                 const uint64_t *__restrict__ bucket_off, const uint64_t *__restrict__ tile_off,
@@ -103,9 +106,9 @@ __global__ void __launch_bounds__(kTileThreads, 4)
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const uint32_t ndig = dmask + 1;
   const uint64_t ntiles = kPairsIn ? tile_off[nb] : (n + kTile - 1) / kTile;
-  for (uint64_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
-    uint64_t lo, hi;
-    uint32_t b = 0;
+  // tile t -> its rows [lo, hi) and bucket b
+  auto tile_range = [&](uint64_t t, uint64_t &lo, uint64_t &hi, uint32_t &b) {
+    b = 0;
     if (kPairsIn) {
       uint32_t a = 0, z = nb;  // tile_off[a] <= t < tile_off[z]
       while (z - a > 1) {
@@ -119,10 +122,9 @@ __global__ void __launch_bounds__(kTileThreads, 4)
       lo = t * kTile;
       hi = lo + kTile < n ? lo + kTile : n;
     }
-    for (uint32_t d = lane; d < ndig; d += 32) S.whist[warp][d] = 0;
-    __syncwarp();
-    int2 tup[4];
-    uint32_t dg[4], rk[4];
+  };
+  int2 tup[4];
+  auto load_tile = [&](uint64_t lo, uint64_t hi) {
 #pragma unroll
     for (int j = 0; j < 4; ++j) {
       const uint64_t i = lo + tid + j * kTileThreads;
@@ -135,6 +137,20 @@ __global__ void __launch_bounds__(kTileThreads, 4)
         }
       }
     }
+  };
+  uint64_t t = blockIdx.x, lo = 0, hi = 0;
+  uint32_t b = 0;
+  if (t < ntiles) {
+    tile_range(t, lo, hi, b);
+    load_tile(lo, hi);
+  }
+  // Software pipeline: the next tile's loads are issued once this tile's
+  // tuples sit in shared memory, so their DRAM latency overlaps the write
+  // phase; the cursor atomic's L2 round trip overlaps the shared scatter.
+  for (; t < ntiles; t += gridDim.x) {
+    for (uint32_t d = lane; d < ndig; d += 32) S.whist[warp][d] = 0;
+    __syncwarp();
+    uint32_t dg[4], rk[4];
 #pragma unroll
     for (int j = 0; j < 4; ++j) {
       if (lo + tid + j * kTileThreads < hi) {
@@ -153,6 +169,9 @@ __global__ void __launch_bounds__(kTileThreads, 4)
         tot += c;
       }
     }
+    // this tile's run of each digit in the output (consumed after the scatter)
+    uint32_t gpos = 0;
+    if ((uint32_t)tid < ndig && tot) gpos = atomicAdd(&cursor[(uint64_t)b * ndig + tid], tot);
     // exclusive scan of the digit totals (ndig <= 256: warps 0..7)
     uint32_t incl = 0;
     if (tid < kMaxDigits) {
@@ -169,7 +188,6 @@ __global__ void __launch_bounds__(kTileThreads, 4)
       uint32_t add = 0;
       for (int w = 0; w < warp; ++w) add += S.wsum[w];
       S.dstart[tid] = add + incl - tot;
-      S.gpos[tid] = tot ? atomicAdd(&cursor[(uint64_t)b * ndig + tid], tot) : 0u;
     }
     __syncthreads();
 #pragma unroll
@@ -180,8 +198,14 @@ __global__ void __launch_bounds__(kTileThreads, 4)
         S.sdig[pos] = (uint16_t)dg[j];
       }
     }
-    __syncthreads();
+    if ((uint32_t)tid < ndig) S.gpos[tid] = gpos;
     const uint32_t cnt = (uint32_t)(hi - lo);
+    const uint64_t tn = t + gridDim.x;
+    if (tn < ntiles) {
+      tile_range(tn, lo, hi, b);
+      load_tile(lo, hi);
+    }
+    __syncthreads();
 #pragma unroll
     for (int j = 0; j < 4; ++j) {
       const uint32_t i = tid + j * kTileThreads;
