@@ -115,13 +115,44 @@ class RadixJoin:
         self.h_r = torch.from_numpy(self.rk).pin_memory()
         self.h_s = [torch.from_numpy(s).pin_memory() for s in self.sks]
         self.h_out = torch.empty((len(self.THETAS), 2), dtype=torch.int64).pin_memory()
+        # copies run on their own stream into double-buffered device columns,
+        # so the next probe side streams in while the current join computes
+        self.copy_stream = torch.cuda.Stream()
+        self.s_bufs = [self.d_s[0], self.d_s[1]]
+        self.r_bufs = [self.d_r, torch.empty_like(self.d_r)]
+        self.s_free = [torch.cuda.Event() for _ in range(2)]
+        self.r_free = [torch.cuda.Event() for _ in range(2)]
+        for e in self.s_free + self.r_free:
+            e.record()
+        self.joins, self.steps_done = 0, 0
 
     def e2e_step(self):
-        self.d_r.copy_(self.h_r, non_blocking=True)
-        for i, (hs, ds, o) in enumerate(zip(self.h_s, self.d_s, self.outs)):
-            ds.copy_(hs, non_blocking=True)
-            self.ctx.radix_join_agg(self.d_r, None, ds, None, self.aggs, out=o)
+        """Every step copies R and the three S columns host -> device and the
+        results back; copy i+1 overlaps join i (buffers guarded by events)."""
+        import torch
+
+        comp = torch.cuda.current_stream()
+        rb = self.r_bufs[self.steps_done % 2]
+        with torch.cuda.stream(self.copy_stream):
+            self.copy_stream.wait_event(self.r_free[self.steps_done % 2])
+            rb.copy_(self.h_r, non_blocking=True)
+            r_ready = torch.cuda.Event()
+            r_ready.record(self.copy_stream)
+        comp.wait_event(r_ready)
+        for i, (hs, o) in enumerate(zip(self.h_s, self.outs)):
+            b = self.joins % 2
+            with torch.cuda.stream(self.copy_stream):
+                self.copy_stream.wait_event(self.s_free[b])
+                self.s_bufs[b].copy_(hs, non_blocking=True)
+                ready = torch.cuda.Event()
+                ready.record(self.copy_stream)
+            comp.wait_event(ready)
+            self.ctx.radix_join_agg(rb, None, self.s_bufs[b], None, self.aggs, out=o)
+            self.s_free[b].record(comp)
             self.h_out[i].copy_(o, non_blocking=True)
+            self.joins += 1
+        self.r_free[self.steps_done % 2].record(comp)
+        self.steps_done += 1
 
     def e2e_results(self):
         return self.h_out.tolist()
