@@ -333,20 +333,17 @@ __global__ void __launch_bounds__(kThreads, 1)
   int32_t *tval = tkey + kCapMax;
   int2 *rp = reinterpret_cast<int2 *>(smem);
   unsigned short *tab = reinterpret_cast<unsigned short *>(rp + kRMax);
-  // unresolved probes of one round: {key, probe value, next group, -}
+  // unresolved probes of one round, 128 per warp: {key, probe value, next group, -}
   int4 *queue = reinterpret_cast<int4 *>(tval + kCapMax);
   __shared__ int64_t red[32 * GBJ_MAX_AGGS];
   __shared__ unsigned long long s_item;
   __shared__ uint32_t s_part;
   __shared__ int s_dup;
-  __shared__ uint32_t s_qn[2];
   gbjd::Acc acc;
   acc.init(spec);
   int64_t a_cnt = 0, a_sum = 0;
-  uint32_t round = 0;
   const uint64_t total = item_off[P];
   if (threadIdx.x == 0) {
-    s_qn[0] = s_qn[1] = 0;
     s_item = atomicAdd(item_ctr, 1ull);
     s_part = s_item < total ? item_partition(item_off, P, total, s_item) : 0;
   }
@@ -444,17 +441,20 @@ __global__ void __launch_bounds__(kThreads, 1)
         return em != 0;
       };
       // Probe rounds of 4 tuples per thread: every probe checks its first
-      // group; the few that must continue go to a shared queue that all
-      // lanes then drain together, so no warp idles behind one long walk.
-      // The next round's tuples are loaded while this round is probed.
+      // group; the few that must continue go to the warp's own queue, which
+      // the warp's lanes then drain together, so no lane idles behind one
+      // long walk and no CTA-wide barrier is needed.  The next round's
+      // tuples are loaded while this round is probed.
+      const int lane = threadIdx.x & 31;
+      const unsigned lt = (1u << lane) - 1u;
+      int4 *wq = queue + (threadIdx.x >> 5) * (4 * 32);
       int2 nxt[4];
 #pragma unroll
       for (int u = 0; u < 4; ++u) {
         const uint64_t j = sb + threadIdx.x + (uint64_t)u * kThreads;
         nxt[u] = j < se ? __ldcs(S + j) : make_int2(0, 0);
       }
-      for (uint64_t j0 = sb; j0 < se; j0 += 4 * kThreads, ++round) {
-        const int par = round & 1;
+      for (uint64_t j0 = sb; j0 < se; j0 += 4 * kThreads) {
         int2 t[4];
 #pragma unroll
         for (int u = 0; u < 4; ++u) {
@@ -462,21 +462,26 @@ __global__ void __launch_bounds__(kThreads, 1)
           const uint64_t j = j0 + 4 * kThreads + threadIdx.x + (uint64_t)u * kThreads;
           nxt[u] = j < se ? __ldcs(S + j) : make_int2(0, 0);
         }
+        uint32_t qn = 0;  // warp-uniform queue length
 #pragma unroll
         for (int u = 0; u < 4; ++u) {
-          if (j0 + threadIdx.x + (uint64_t)u * kThreads >= se) continue;
-          const uint32_t h = table_slot(t[u].x, bits, cap);
-          if (!group(t[u].x, t[u].y, h & ~3u, h & 3u)) {
+          bool more = false;
+          uint32_t h = 0;
+          if (j0 + threadIdx.x + (uint64_t)u * kThreads < se) {
+            h = table_slot(t[u].x, bits, cap);
+            more = !group(t[u].x, t[u].y, h & ~3u, h & 3u);
+          }
+          const unsigned bal = __ballot_sync(0xffffffffu, more);
+          if (more) {
             uint32_t g1 = (h & ~3u) + 4;
             if (g1 >= cap) g1 = 0;
-            queue[atomicAdd(&s_qn[par], 1u)] = make_int4(t[u].x, t[u].y, (int)g1, 0);
+            wq[qn + __popc(bal & lt)] = make_int4(t[u].x, t[u].y, (int)g1, 0);
           }
+          qn += __popc(bal);
         }
-        __syncthreads();
-        const uint32_t nq = s_qn[par];
-        if (threadIdx.x == 0) s_qn[par ^ 1] = 0;
-        for (uint32_t i = threadIdx.x; i < nq; i += kThreads) {
-          const int4 e = queue[i];
+        __syncwarp();
+        for (uint32_t i = lane; i < qn; i += 32) {
+          const int4 e = wq[i];
           uint32_t g0 = (uint32_t)e.z;
           for (uint32_t step = 4; step < cap; step += 4) {
             if (group(e.x, e.y, g0, 0)) break;
@@ -484,7 +489,7 @@ __global__ void __launch_bounds__(kThreads, 1)
             if (g0 >= cap) g0 = 0;
           }
         }
-        __syncthreads();
+        __syncwarp();
       }
     } else {
       // index table: plain linear probing, one slot per step
