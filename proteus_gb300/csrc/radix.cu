@@ -66,15 +66,36 @@ __global__ void __launch_bounds__(1024)
   for (uint32_t p = threadIdx.x; p < P; p += blockDim.x) sh[p] = 0;
   __syncthreads();
   const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
-  uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
-  for (; i + 3 * stride < n; i += 4 * stride) {
-    int32_t k[4];
+  const uint64_t tid = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+  uint64_t done = 0;
+  if ((reinterpret_cast<uintptr_t>(keys) & 15) == 0) {
+    // 16-byte loads, four in flight per thread (16 keys)
+    const int4 *k4 = reinterpret_cast<const int4 *>(keys);
+    const uint64_t n4 = n / 4;
+    uint64_t i = tid;
+    for (; i + 3 * stride < n4; i += 4 * stride) {
+      int4 k[4];
 #pragma unroll
-    for (int u = 0; u < 4; ++u) k[u] = __ldg(keys + i + u * stride);
+      for (int u = 0; u < 4; ++u) k[u] = __ldcs(k4 + i + u * stride);
 #pragma unroll
-    for (int u = 0; u < 4; ++u) atomicAdd(&sh[digit_of<kDigit>(k[u], shift, pmask)], 1u);
+      for (int u = 0; u < 4; ++u) {
+        atomicAdd(&sh[digit_of<kDigit>(k[u].x, shift, pmask)], 1u);
+        atomicAdd(&sh[digit_of<kDigit>(k[u].y, shift, pmask)], 1u);
+        atomicAdd(&sh[digit_of<kDigit>(k[u].z, shift, pmask)], 1u);
+        atomicAdd(&sh[digit_of<kDigit>(k[u].w, shift, pmask)], 1u);
+      }
+    }
+    for (; i < n4; i += stride) {
+      const int4 k = __ldcs(k4 + i);
+      atomicAdd(&sh[digit_of<kDigit>(k.x, shift, pmask)], 1u);
+      atomicAdd(&sh[digit_of<kDigit>(k.y, shift, pmask)], 1u);
+      atomicAdd(&sh[digit_of<kDigit>(k.z, shift, pmask)], 1u);
+      atomicAdd(&sh[digit_of<kDigit>(k.w, shift, pmask)], 1u);
+    }
+    done = n4 * 4;
   }
-  for (; i < n; i += stride) atomicAdd(&sh[digit_of<kDigit>(__ldg(keys + i), shift, pmask)], 1u);
+  for (uint64_t i = done + tid; i < n; i += stride)
+    atomicAdd(&sh[digit_of<kDigit>(__ldg(keys + i), shift, pmask)], 1u);
   __syncthreads();
   for (uint32_t p = threadIdx.x; p < P; p += blockDim.x)
     if (sh[p]) atomicAdd(&ghist[p], sh[p]);
@@ -585,7 +606,10 @@ int partition_impl(gbj_ctx *ctx, const int32_t *keys, const int32_t *vals, uint6
     const size_t smem = (size_t)P * sizeof(uint32_t);
     GBJ_CHECK_CUDA(ctx, cudaFuncSetAttribute(k_pid_hist<kDigit>,
                                              cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    const uint64_t grid = std::max<uint64_t>(1, std::min<uint64_t>(ctx->sm_count, (n + 16383) / 16384));
+    int per_sm = 1;
+    GBJ_CHECK_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_pid_hist<kDigit>, 1024, smem));
+    const uint64_t grid = std::max<uint64_t>(
+        1, std::min<uint64_t>((uint64_t)ctx->sm_count * std::max(per_sm, 1), (n + 16383) / 16384));
     k_pid_hist<kDigit><<<(unsigned)grid, 1024, smem, s>>>(keys, n, shift, pmask, hist);
     GBJ_TRY(after_launch(ctx, "k_pid_hist", s));
   }
