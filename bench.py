@@ -51,6 +51,8 @@ def parse():
     ap.add_argument("--log-s", type=int, default=None, help="log2 probe / input rows")
     ap.add_argument("--card", type=int, default=1 << 16, help="group-by cardinality")
     ap.add_argument("--theta", type=float, default=0.0, help="group-by Zipf exponent")
+    ap.add_argument("--bits", type=int, default=0,
+                    help="radix join: fixed partition bits instead of the autotuner's choice")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--cpu-sample-log", type=int, default=26,
@@ -72,6 +74,7 @@ class RadixJoin:
         self.lr = args.log_r or 27
         self.ls = args.log_s or 29
         self.nr, self.ns = 1 << self.lr, 1 << self.ls
+        self.fixed_bits = args.bits
 
     def describe(self):
         return {"workload": f"radix-partitioned hash join R=2^{self.lr} unique int32 keys, "
@@ -79,7 +82,8 @@ class RadixJoin:
                             f"COUNT + SUM(rowid xor)",
                 "n_build": self.nr, "n_probe": self.ns, "thetas": list(self.THETAS),
                 "hit_rate": 0.5, "l2": "inputs larger than L2 (2 GiB probe keys per join)",
-                "radix_bits": getattr(self, "tuned_bits", None), "radix_bits_from": "autotuner"}
+                "radix_bits": getattr(self, "tuned_bits", None),
+                "radix_bits_from": "fixed" if self.fixed_bits else "autotuner"}
 
     def generate(self):
         from proteus_gb300 import engine
@@ -100,11 +104,15 @@ class RadixJoin:
         self.outs = [torch.empty(2, dtype=torch.int64, device="cuda") for _ in self.THETAS]
         # the autotuner picks the partition bits for this shape (untimed);
         # every timed join then runs with the cached choice
-        self.tuned_bits, self.tune_ms = ctx.autotune_radix_join(self.d_r, None, self.d_s[0], None, self.aggs)
+        if self.fixed_bits:
+            self.tuned_bits, self.tune_ms = self.fixed_bits, None
+        else:
+            self.tuned_bits, self.tune_ms = ctx.autotune_radix_join(self.d_r, None, self.d_s[0], None,
+                                                                    self.aggs)
 
     def step(self):
         for ds, o in zip(self.d_s, self.outs):
-            self.ctx.radix_join_agg(self.d_r, None, ds, None, self.aggs, out=o)
+            self.ctx.radix_join_agg(self.d_r, None, ds, None, self.aggs, out=o, bits=self.fixed_bits)
 
     def results(self):
         return [o.cpu().tolist() for o in self.outs]
@@ -147,7 +155,7 @@ class RadixJoin:
                 ready = torch.cuda.Event()
                 ready.record(self.copy_stream)
             comp.wait_event(ready)
-            self.ctx.radix_join_agg(rb, None, self.s_bufs[b], None, self.aggs, out=o)
+            self.ctx.radix_join_agg(rb, None, self.s_bufs[b], None, self.aggs, out=o, bits=self.fixed_bits)
             self.s_free[b].record(comp)
             self.h_out[i].copy_(o, non_blocking=True)
             self.joins += 1
