@@ -472,6 +472,15 @@ typedef struct gbj_result gbj_result;
 int gbj_catalog_create(gbj_ctx *ctx, gbj_catalog **out);
 int gbj_catalog_add_column(gbj_catalog *cat, const char *rel,
                            const char *attr, const int32_t *d_col, uint64_t n);
+/* Loads the int32 columns (int, boolean, dictionary-coded string) of a
+ * catalog.json in the reference's columnar file layout (tools/prepare_data.py:
+ * one little-endian binary file per column at "<base_dir>/<path>.<attrName>")
+ * into the context's pool and registers them as (path, attrName); relation
+ * NULL loads every relation, else only the one whose key or path matches.
+ * int64 / date / float columns are skipped.  The catalog owns these columns. */
+int gbj_catalog_load(gbj_catalog *cat, const char *catalog_json,
+                     const char *base_dir, const char *relation,
+                     uint64_t *columns_loaded);
 int gbj_catalog_destroy(gbj_catalog *cat);
 /* Parses and checks a plan (operator names, required fields) without a GPU;
  * on failure err gets the message. */

@@ -136,6 +136,7 @@ SIGNATURES = {
     "gbj_tune_load": (C.c_int, [vp, C.c_char_p]),
     "gbj_catalog_create": (C.c_int, [vp, P(vp)]),
     "gbj_catalog_add_column": (C.c_int, [vp, C.c_char_p, C.c_char_p, vp, u64]),
+    "gbj_catalog_load": (C.c_int, [vp, C.c_char_p, C.c_char_p, C.c_char_p, P(u64)]),
     "gbj_catalog_destroy": (C.c_int, [vp]),
     "gbj_plan_validate": (C.c_int, [C.c_char_p, C.c_char_p, u64]),
     "gbj_plan_execute": (C.c_int, [vp, C.c_char_p, P(vp)]),

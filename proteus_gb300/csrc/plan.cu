@@ -20,6 +20,7 @@
 // them; other joins materialise (build row, probe row) pairs and gather the
 // columns their parents read.  Sizing fields are capacity hints.
 #include <algorithm>
+#include <cstdio>
 #include <cstdlib>
 #include <cstring>
 #include <map>
@@ -277,6 +278,7 @@ struct gbj_catalog {
   };
   std::map<std::pair<std::string, std::string>, Col> cols;
   std::map<std::string, std::vector<std::string>> rel_attrs;
+  std::vector<void *> owned;  // pool blocks of columns loaded from files
 };
 
 struct gbj_result {
@@ -747,7 +749,126 @@ extern "C" int gbj_catalog_add_column(gbj_catalog *cat, const char *rel, const c
 }
 
 extern "C" int gbj_catalog_destroy(gbj_catalog *cat) {
+  if (!cat) return GBJ_ERR_INVALID;
+  if (!cat->owned.empty()) cudaDeviceSynchronize();
+  for (void *p : cat->owned) gbj_pool_free(cat->ctx, p);
   delete cat;
+  return GBJ_OK;
+}
+
+namespace {
+
+// Streams one binary column file into a pool block: reads go into two pinned
+// staging buffers alternately, so the next read overlaps the previous copy.
+int load_column_file(gbj_catalog *cat, const std::string &file, uint64_t *n_out, void **d_out) {
+  gbj_ctx *ctx = cat->ctx;
+  FILE *f = fopen(file.c_str(), "rb");
+  if (!f) return set_error(ctx, GBJ_ERR_INVALID, "catalog: cannot open " + file);
+  fseek(f, 0, SEEK_END);
+  const long long bytes = ftell(f);
+  fseek(f, 0, SEEK_SET);
+  if (bytes < 0 || bytes % 4) {
+    fclose(f);
+    return set_error(ctx, GBJ_ERR_INVALID, "catalog: " + file + " is not a whole number of int32 values");
+  }
+  void *d = nullptr;
+  int rc = gbj_pool_alloc(ctx, std::max<uint64_t>((uint64_t)bytes, 16), &d);
+  if (rc) {
+    fclose(f);
+    return rc;
+  }
+  constexpr size_t kChunk = 64u << 20;
+  void *stage[2] = {nullptr, nullptr};
+  cudaEvent_t done[2] = {nullptr, nullptr};
+  cudaStream_t s = ctx->stream;
+  for (int i = 0; i < 2 && rc == GBJ_OK; ++i) {
+    if (cudaHostAlloc(&stage[i], kChunk, cudaHostAllocDefault) != cudaSuccess ||
+        cudaEventCreateWithFlags(&done[i], cudaEventDisableTiming) != cudaSuccess)
+      rc = set_error(ctx, GBJ_ERR_CUDA, "catalog: staging buffers");
+  }
+  uint64_t off = 0;
+  for (int k = 0; rc == GBJ_OK && off < (uint64_t)bytes; ++k) {
+    const int b = k & 1;
+    if (k >= 2) cudaEventSynchronize(done[b]);  // its previous copy has finished
+    const size_t want = (size_t)std::min<uint64_t>(kChunk, (uint64_t)bytes - off);
+    if (fread(stage[b], 1, want, f) != want) {
+      rc = set_error(ctx, GBJ_ERR_INVALID, "catalog: short read of " + file);
+      break;
+    }
+    if (cudaMemcpyAsync(static_cast<char *>(d) + off, stage[b], want, cudaMemcpyHostToDevice, s) != cudaSuccess ||
+        cudaEventRecord(done[b], s) != cudaSuccess)
+      rc = set_error(ctx, GBJ_ERR_CUDA, "catalog: copy of " + file);
+    off += want;
+  }
+  cudaStreamSynchronize(s);
+  for (int i = 0; i < 2; ++i) {
+    if (stage[i]) cudaFreeHost(stage[i]);
+    if (done[i]) cudaEventDestroy(done[i]);
+  }
+  fclose(f);
+  if (rc) {
+    gbj_pool_free(ctx, d);
+    return rc;
+  }
+  *n_out = (uint64_t)bytes / 4;
+  *d_out = d;
+  return GBJ_OK;
+}
+
+}  // namespace
+
+// Loads int32 columns described by a catalog.json in the reference's
+// columnar layout (tools/prepare_data.py: one binary file per column,
+// "<path>.<attrName>", int / boolean / dictionary-coded string columns as
+// 4-byte little-endian values; relation name = the entry's "path").
+// Columns of other types (int64, date, float) are skipped.
+extern "C" int gbj_catalog_load(gbj_catalog *cat, const char *catalog_json, const char *base_dir,
+                                const char *relation, uint64_t *columns_loaded) {
+  if (!cat || !catalog_json) return GBJ_ERR_INVALID;
+  gbj_ctx *ctx = cat->ctx;
+  std::string text;
+  {
+    FILE *f = fopen(catalog_json, "rb");
+    if (!f) return set_error(ctx, GBJ_ERR_INVALID, std::string("catalog: cannot open ") + catalog_json);
+    char buf[1 << 16];
+    size_t k;
+    while ((k = fread(buf, 1, sizeof(buf), f)) > 0) text.append(buf, k);
+    fclose(f);
+  }
+  uint64_t loaded = 0;
+  try {
+    const JVal root = JsonParser(text.c_str()).parse();
+    if (root.t != JVal::Obj) fail(GBJ_ERR_INVALID, "catalog: top level is not an object");
+    const std::string base = base_dir && *base_dir ? std::string(base_dir) + "/" : std::string();
+    for (const auto &kv : root.o) {
+      const JVal &e = kv.second;
+      const JVal *path = e.get("path");
+      if (!path || path->t != JVal::Str) continue;
+      if (relation && *relation && kv.first != relation && path->s != relation) continue;
+      const JVal *ty = e.get("type");
+      const JVal *inner = ty ? ty->get("inner") : nullptr;
+      const JVal *attrs = inner ? inner->get("attributes") : nullptr;
+      if (!attrs || attrs->t != JVal::Arr) fail(GBJ_ERR_INVALID, "catalog: " + kv.first + " has no attributes");
+      for (const JVal &a : attrs->a) {
+        const JVal *an = a.get("attrName");
+        const JVal *at = a.get("type");
+        const JVal *tn = at ? at->get("type") : nullptr;
+        if (!an || !tn) continue;
+        if (tn->s != "int" && tn->s != "dstring" && tn->s != "boolean") continue;
+        uint64_t n = 0;
+        void *d = nullptr;
+        const int rc = load_column_file(cat, base + path->s + "." + an->s, &n, &d);
+        if (rc) fail(rc, gbj_last_error(ctx));
+        cat->owned.push_back(d);
+        const int rc2 = gbj_catalog_add_column(cat, path->s.c_str(), an->s.c_str(), static_cast<int32_t *>(d), n);
+        if (rc2) fail(rc2, "catalog: register " + an->s);
+        ++loaded;
+      }
+    }
+  } catch (const PlanError &e) {
+    return set_error(ctx, e.code, e.msg);
+  }
+  if (columns_loaded) *columns_loaded = loaded;
   return GBJ_OK;
 }
 

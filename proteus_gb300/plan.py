@@ -155,6 +155,14 @@ class Catalog:
         self.ctx.check(self.ctx.lib.gbj_catalog_add_column(self.handle, rel.encode(), attr.encode(),
                                                            t.data_ptr(), t.numel()))
 
+    def load(self, catalog_json: str, base_dir: str = "", relation: str | None = None) -> int:
+        """Loads the int32 columns of a catalog.json in the reference's columnar
+        file layout into device memory; returns the number of columns."""
+        n = C.c_uint64()
+        self.ctx.check(self.ctx.lib.gbj_catalog_load(self.handle, catalog_json.encode(), base_dir.encode(),
+                                                     relation.encode() if relation else None, C.byref(n)))
+        return n.value
+
     def execute(self, plan) -> dict:
         """Runs a plan (RelBuilder, dict or JSON text) -> {name: int64 numpy column}."""
         lib = self.ctx.lib
