@@ -224,6 +224,23 @@ int gbj_groupby(gbj_ctx *ctx, const int32_t *d_keys, const int32_t *d_values,
                 int32_t *d_out_min, int32_t *d_out_max, uint64_t out_capacity,
                 uint64_t *d_n_groups, void *stream);
 
+/* ---------------------------------------------------------- hash rearrange */
+/* HashRearrange / GpuHashRearrange (core/olap/lib/operators/
+ * hash-rearrange.cpp:131-405, gpu/gpu-hash-rearrange.cpp:87-700): every row
+ * goes to bucket hash(key) mod num_buckets, hash = the expression hasher's
+ * 64-bit hash of an int32 (core/olap/lib/expressions/expressions-hasher.cpp:
+ * 39-58), unsigned remainder -- the same bucket as the reference.  The
+ * n_cols int32 columns (the key column among them) are written bucket-major
+ * to d_out_cols; d_bucket_offsets gets num_buckets + 1 entries (bucket b is
+ * rows [off[b], off[b+1])).  Rows keep no particular order inside a bucket,
+ * as the reference's concurrent block appends do not. */
+#define GBJ_REARRANGE_MAX_COLS 16
+
+int gbj_hash_rearrange(gbj_ctx *ctx, const int32_t *const *d_cols,
+                       int32_t n_cols, uint64_t n, int32_t key_col,
+                       uint32_t num_buckets, int32_t *const *d_out_cols,
+                       uint64_t *d_bucket_offsets, void *stream);
+
 /* ------------------------------------------------------ column helpers */
 /* Global aggregate over one int32 column restricted to an optional row list
  * (Reduce, core/olap/lib/operators/reduce-opt.cpp:52-481).  d_rows may be

@@ -210,6 +210,20 @@ class Context:
     def tune_clear(self):
         self.check(self.lib.gbj_tune_clear(self.handle))
 
+    # ------------------------------------------------------ hash rearrange
+    def hash_rearrange(self, cols, key_col: int, num_buckets: int, stream=None):
+        """-> (bucket-major output columns, bucket offsets [num_buckets + 1])."""
+        import torch
+
+        n = cols[0].numel()
+        outs = [torch.empty_like(c) for c in cols]
+        off = torch.empty(num_buckets + 1, dtype=torch.int64, device=cols[0].device)
+        ins = (C.c_void_p * len(cols))(*[c.data_ptr() for c in cols])
+        ous = (C.c_void_p * len(cols))(*[o.data_ptr() for o in outs])
+        self.check(self.lib.gbj_hash_rearrange(self.handle, ins, len(cols), n, key_col, num_buckets, ous,
+                                               _ptr(off), self._s(stream)))
+        return outs, off
+
     # ----------------------------------------------------------- group-by
     def groupby(self, keys, values, out_capacity, expected_groups=0, max_input_size=0,
                 hash_bits=0, strategy=0, stream=None):
