@@ -224,6 +224,23 @@ int gbj_groupby(gbj_ctx *ctx, const int32_t *d_keys, const int32_t *d_values,
                 int32_t *d_out_min, int32_t *d_out_max, uint64_t out_capacity,
                 uint64_t *d_n_groups, void *stream);
 
+/* ------------------------------------------------------------ bloom filter */
+/* BloomFilterBuild / BloomFilterProbe (core/olap/lib/operators/bloom-filter/
+ * bloom-filter-build.cpp:28-59, bloom-filter-probe.cpp:28-53): a filter of
+ * filter_size (power of two) flags; a key's flag is at key & (filter_size-1)
+ * (bloom-filter.cpp:65-95).  Build sets the flags of d_keys; probe writes the
+ * positions of the rows whose flag is set (ascending) and their number --
+ * exactly the rows the reference's probe passes to its parent.  Flags are
+ * bits: filter_size / 8 bytes from the pool. */
+typedef struct gbj_bloom gbj_bloom;
+
+int gbj_bloom_build(gbj_ctx *ctx, const int32_t *d_keys, uint64_t n,
+                    uint64_t filter_size, void *stream, gbj_bloom **out);
+int gbj_bloom_probe(gbj_ctx *ctx, const gbj_bloom *filter,
+                    const int32_t *d_keys, uint64_t n, int32_t *d_rows_out,
+                    uint64_t *d_count, void *stream);
+int gbj_bloom_destroy(gbj_ctx *ctx, gbj_bloom *filter);
+
 /* ---------------------------------------------------------- hash rearrange */
 /* HashRearrange / GpuHashRearrange (core/olap/lib/operators/
  * hash-rearrange.cpp:131-405, gpu/gpu-hash-rearrange.cpp:87-700): every row

@@ -1114,3 +1114,26 @@ int64_t orc_join_groupby(const int32_t *bk, const int32_t *bg, uint64_t nb, cons
   orc_join_free(&t);
   return rc;
 }
+
+/* ---------------------------------------------------------- bloom filter */
+/* BloomFilterBuild / BloomFilterProbe (bloom-filter-build.cpp:28-59,
+ * bloom-filter-probe.cpp:28-53): flags[key & (filter_size - 1)] set for every
+ * build key (bloom-filter.cpp:65-95; the key itself is the position); the
+ * probe keeps rows whose flag is set.  Returns the number of passing rows
+ * and writes their positions in order (up to cap). */
+int64_t orc_bloom_semijoin(const int32_t *build, uint64_t nb, const int32_t *probe, uint64_t np,
+                           uint64_t filter_size, int32_t *rows, uint64_t cap) {
+  if (!filter_size || (filter_size & (filter_size - 1))) return -1;
+  unsigned char *flags = (unsigned char *)calloc(filter_size, 1);
+  if (!flags) return -1;
+  const uint32_t mask = (uint32_t)(filter_size - 1);
+  for (uint64_t i = 0; i < nb; ++i) flags[(uint32_t)build[i] & mask] = 1;
+  int64_t m = 0;
+  for (uint64_t i = 0; i < np; ++i)
+    if (flags[(uint32_t)probe[i] & mask]) {
+      if ((uint64_t)m < cap && rows) rows[m] = (int32_t)i;
+      ++m;
+    }
+  free(flags);
+  return m;
+}

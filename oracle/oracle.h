@@ -152,6 +152,13 @@ int64_t orc_join_groupby(const int32_t *bk, const int32_t *bg, uint64_t nb,
                          int64_t *out_sum, int32_t *out_min, int32_t *out_max,
                          uint64_t cap);
 
+
+/* Bloom-filter semi-join with the reference's single-position filter
+ * (flags[key & (filter_size - 1)]): positions of passing probe rows. */
+int64_t orc_bloom_semijoin(const int32_t *build, uint64_t nb, const int32_t *probe,
+                           uint64_t np, uint64_t filter_size, int32_t *rows,
+                           uint64_t cap);
+
 #ifdef __cplusplus
 }
 #endif

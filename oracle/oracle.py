@@ -68,6 +68,8 @@ def lib():
         L.orc_groupby.argtypes = [vp, vp, u64, i32, C.c_int, vp, vp, vp, vp, vp, u64]
         L.orc_reduce.restype = None
         L.orc_reduce.argtypes = [vp, vp, u64, vp, vp, i32, vp]
+        L.orc_bloom_semijoin.restype = i64
+        L.orc_bloom_semijoin.argtypes = [vp, u64, vp, u64, u64, vp, u64]
         L.orc_join_groupby.restype = i64
         L.orc_join_groupby.argtypes = [vp, vp, u64, vp, vp, u64, C.c_int, vp, vp, vp, vp, vp, u64]
         L.orc_star_query.restype = i64
@@ -198,6 +200,16 @@ def reduce(col, aggs, rows=None):
     n = len(rows) if rows is not None else len(col)
     L.orc_reduce(_p(col), _p(rows), n, _p(ops), _p(opd), len(aggs), _p(out))
     return [int(x) for x in out]
+
+
+def bloom_semijoin(build, probe, filter_size):
+    """Positions of the probe rows the reference's bloom filter passes."""
+    L = lib()
+    build, probe = _i32(build), _i32(probe)
+    out = np.empty(max(len(probe), 1), dtype=np.int32)
+    m = L.orc_bloom_semijoin(_p(build), len(build), _p(probe), len(probe), filter_size, _p(out), len(out))
+    assert m >= 0
+    return out[:m]
 
 
 def join_groupby(bk, bg, pk, pv, threads=1):

@@ -134,6 +134,9 @@ SIGNATURES = {
     "gbj_tune_clear": (C.c_int, [vp]),
     "gbj_tune_save": (C.c_int, [vp, C.c_char_p]),
     "gbj_tune_load": (C.c_int, [vp, C.c_char_p]),
+    "gbj_bloom_build": (C.c_int, [vp, vp, u64, u64, vp, P(vp)]),
+    "gbj_bloom_probe": (C.c_int, [vp, vp, vp, u64, vp, vp, vp]),
+    "gbj_bloom_destroy": (C.c_int, [vp, vp]),
     "gbj_hash_rearrange": (C.c_int, [vp, P(vp), i32, u64, i32, C.c_uint32, P(vp), vp, vp]),
     "gbj_catalog_create": (C.c_int, [vp, P(vp)]),
     "gbj_catalog_add_column": (C.c_int, [vp, C.c_char_p, C.c_char_p, vp, u64]),

@@ -13,6 +13,7 @@
 // allowed) and a probe row meets every build row with an equal key.
 #include <cooperative_groups.h>
 
+#include "compact.cuh"
 #include "gbj_internal.cuh"
 #include "scan.cuh"
 
@@ -202,60 +203,15 @@ __global__ void k_gather(const int32_t *__restrict__ col,
     out[i] = col[rows[i]];
 }
 
-constexpr int kSelTile = 4096;  // rows per select tile (one block)
-
-__global__ void __launch_bounds__(1024)
-    k_select_count(const int32_t *__restrict__ col, uint64_t n, int32_t lo,
-                   int32_t hi, uint64_t *tile_counts) {
-  __shared__ uint32_t c;
-  if (threadIdx.x == 0) c = 0;
-  __syncthreads();
-  uint32_t mine = 0;
-  const uint64_t base = (uint64_t)blockIdx.x * kSelTile;
-  for (int j = threadIdx.x; j < kSelTile; j += blockDim.x) {
-    uint64_t i = base + j;
-    if (i < n) {
-      int32_t v = col[i];
-      mine += (v >= lo && v <= hi);
-    }
+// Range predicate of gbj_select_range (inclusive bounds).
+struct RangePred {
+  const int32_t *col;
+  int32_t lo, hi;
+  __device__ __forceinline__ bool operator()(uint64_t i) const {
+    const int32_t v = col[i];
+    return v >= lo && v <= hi;
   }
-  mine = __reduce_add_sync(0xffffffffu, mine);
-  if ((threadIdx.x & 31) == 0) atomicAdd(&c, mine);
-  __syncthreads();
-  if (threadIdx.x == 0) tile_counts[blockIdx.x] = c;
-}
-
-// Stable compaction: rows of a tile are emitted in order, chunk by chunk.
-__global__ void __launch_bounds__(1024)
-    k_select_write(const int32_t *__restrict__ col, uint64_t n, int32_t lo,
-                   int32_t hi, const uint64_t *tile_off, int32_t *out) {
-  __shared__ uint32_t warp_cnt[32];
-  __shared__ uint64_t run;
-  if (threadIdx.x == 0) run = tile_off[blockIdx.x];
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const uint64_t base = (uint64_t)blockIdx.x * kSelTile;
-  for (int j0 = 0; j0 < kSelTile; j0 += blockDim.x) {
-    __syncthreads();
-    const uint64_t i = base + j0 + threadIdx.x;
-    const bool pass = i < n && col[i] >= lo && col[i] <= hi;
-    const uint32_t b = __ballot_sync(0xffffffffu, pass);
-    if (lane == 0) warp_cnt[warp] = __popc(b);
-    __syncthreads();
-    uint64_t before = run;
-    for (int w = 0; w < warp; ++w) before += warp_cnt[w];
-    if (pass) out[before + __popc(b & ((1u << lane) - 1))] = (int32_t)i;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-      uint64_t t = 0;
-      for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += warp_cnt[w];
-      run += t;
-    }
-  }
-}
-
-__global__ void k_copy_total(const uint64_t *off, uint64_t ntiles, uint64_t *dst) {
-  *dst = off[ntiles];
-}
+};
 
 int grid_for_sms(int sm_count, uint64_t work, int threads, int per_sm = 4) {
   uint64_t blocks = (work + threads - 1) / threads;
@@ -476,17 +432,7 @@ int gbj_select_range(gbj_ctx *ctx, const int32_t *d_col, uint64_t n, int32_t lo,
     GBJ_CHECK_CUDA(ctx, cudaMemsetAsync(d_count, 0, sizeof(uint64_t), s));
     return GBJ_OK;
   }
-  const uint64_t ntiles = (n + kSelTile - 1) / kSelTile;
-  Scratch scratch(ctx, s);
-  uint64_t *cnt;
-  GBJ_TRY(scratch.get(ntiles + 1, &cnt));
-  k_select_count<<<(unsigned)ntiles, 1024, 0, s>>>(d_col, n, lo, hi, cnt);
-  GBJ_TRY(after_launch(ctx, "k_select_count", s));
-  GBJ_TRY(scan_u64(ctx, cnt, cnt, ntiles, s));
-  k_select_write<<<(unsigned)ntiles, 1024, 0, s>>>(d_col, n, lo, hi, cnt, d_rows_out);
-  GBJ_TRY(after_launch(ctx, "k_select_write", s));
-  k_copy_total<<<1, 1, 0, s>>>(cnt, ntiles, d_count);
-  return after_launch(ctx, "k_copy_total", s);
+  return compact_rows(ctx, RangePred{d_col, lo, hi}, n, d_rows_out, d_count, s);
 }
 
 int gbj_join_agg_noalloc(const int32_t *d_build_keys, const int32_t *d_build_payload,
@@ -567,3 +513,8 @@ int gbj_join_agg_noalloc(const int32_t *d_build_keys, const int32_t *d_build_pay
 }
 
 }  // extern "C"
+
+// Shared by every ordered compaction (compact.cuh): the total row count.
+__global__ void gbj::k_compact_total(const uint64_t *off, uint64_t ntiles, uint64_t *dst) {
+  *dst = off[ntiles];
+}

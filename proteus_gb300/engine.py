@@ -210,6 +210,27 @@ class Context:
     def tune_clear(self):
         self.check(self.lib.gbj_tune_clear(self.handle))
 
+    # -------------------------------------------------------- bloom filter
+    def bloom_build(self, keys, filter_size: int, stream=None):
+        h = C.c_void_p()
+        self.check(self.lib.gbj_bloom_build(self.handle, _ptr(keys), keys.numel(), filter_size,
+                                            self._s(stream), C.byref(h)))
+        return h.value
+
+    def bloom_probe(self, bloom, keys, stream=None):
+        """-> (passing row ids, count tensor)."""
+        import torch
+
+        n = keys.numel()
+        rows = torch.empty(max(n, 1), dtype=torch.int32, device=keys.device)
+        cnt = torch.zeros(1, dtype=torch.int64, device=keys.device)
+        self.check(self.lib.gbj_bloom_probe(self.handle, bloom, _ptr(keys), n, _ptr(rows), _ptr(cnt),
+                                            self._s(stream)))
+        return rows, cnt
+
+    def bloom_destroy(self, bloom):
+        self.check(self.lib.gbj_bloom_destroy(self.handle, bloom))
+
     # ------------------------------------------------------ hash rearrange
     def hash_rearrange(self, cols, key_col: int, num_buckets: int, stream=None):
         """-> (bucket-major output columns, bucket offsets [num_buckets + 1])."""
