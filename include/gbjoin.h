@@ -258,6 +258,19 @@ int gbj_hash_rearrange(gbj_ctx *ctx, const int32_t *const *d_cols,
                        uint32_t num_buckets, int32_t *const *d_out_cols,
                        uint64_t *d_bucket_offsets, void *stream);
 
+/* ------------------------------------------------------------------ sort */
+/* ORDER BY one int32 column (the reference's GPU sort, core/olap/lib/
+ * operators/gpu/gpu-sort.cpp, which calls thrust::sort from
+ * core/platform/lib/util/sort/gpu/sort-util.cu:191-218): writes the n_cols
+ * int32 columns to d_out_cols with rows ordered by column key_col, signed
+ * ascending (descending != 0: descending); rows with equal keys keep their
+ * input order. */
+#define GBJ_SORT_MAX_COLS 16
+
+int gbj_sort_by_key(gbj_ctx *ctx, const int32_t *const *d_cols, int32_t n_cols,
+                    uint64_t n, int32_t key_col, int32_t descending,
+                    int32_t *const *d_out_cols, void *stream);
+
 /* ------------------------------------------------------ column helpers */
 /* Global aggregate over one int32 column restricted to an optional row list
  * (Reduce, core/olap/lib/operators/reduce-opt.cpp:52-481).  d_rows may be

@@ -231,6 +231,19 @@ class Context:
     def bloom_destroy(self, bloom):
         self.check(self.lib.gbj_bloom_destroy(self.handle, bloom))
 
+    # ----------------------------------------------------------------- sort
+    def sort_by_key(self, cols, key_col: int, descending=False, stream=None):
+        """-> the columns with rows ordered by cols[key_col] (stable)."""
+        import torch
+
+        n = cols[0].numel()
+        outs = [torch.empty_like(c) for c in cols]
+        ins = (C.c_void_p * len(cols))(*[c.data_ptr() for c in cols])
+        ous = (C.c_void_p * len(cols))(*[o.data_ptr() for o in outs])
+        self.check(self.lib.gbj_sort_by_key(self.handle, ins, len(cols), n, key_col, 1 if descending else 0,
+                                            ous, self._s(stream)))
+        return outs
+
     # ------------------------------------------------------ hash rearrange
     def hash_rearrange(self, cols, key_col: int, num_buckets: int, stream=None):
         """-> (bucket-major output columns, bucket offsets [num_buckets + 1])."""
