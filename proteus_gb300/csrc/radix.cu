@@ -13,7 +13,7 @@
 //
 // GB300 layout:
 //  * a histogram kernel counts the final partition ids (<= 2^15) once;
-//  * each pass (<= 8 digit bits) sorts 2048-tuple tiles by digit in shared
+//  * each pass (<= 8 digit bits) sorts 4096-tuple tiles by digit in shared
 //    memory (one histogram row per warp gives every tuple its rank), takes
 //    one output range per digit with a single global atomic, and writes the
 //    tile digit-run by digit-run, so stores are coalesced and at most 256
@@ -43,8 +43,10 @@ using namespace gbj;
 
 namespace {
 
-constexpr int kTile = 2048;          // tuples per tile of a partition pass
-constexpr int kTileThreads = 512;    // 4 tuples per thread, 4 CTAs per SM
+constexpr int kTile = 4096;          // tuples per tile of a partition pass
+constexpr int kTileThreads = 512;
+constexpr int kTilePer = kTile / kTileThreads;  // tuples per thread
+constexpr int kTileCtas = 2;                    // CTAs per SM (register budget)
 constexpr int kTileWarps = kTileThreads / 32;
 constexpr int kMaxDigits = 256;      // <= 8 digit bits per pass
 constexpr int32_t kEmpty = INT32_MIN;
@@ -116,7 +118,7 @@ struct TileSmem {
 // digit = (f(key) >> dshift) & dmask; the output cursor of (bucket b,
 // digit d) is cursor[b * (dmask + 1) + d].
 template <int kDigit, bool kPairsIn, bool kAoSOut>
-__global__ void __launch_bounds__(kTileThreads, 3)  // 3 CTAs: no spills at 42 registers
+__global__ void __launch_bounds__(kTileThreads, kTileCtas)
     k_tile_pass(const int32_t *__restrict__ keys, const int32_t *__restrict__ vals,
                 const int2 *__restrict__ pin, uint64_t n, int dshift, uint32_t dmask,
                 const uint64_t *__restrict__ bucket_off, const uint64_t *__restrict__ tile_off,
@@ -144,10 +146,10 @@ __global__ void __launch_bounds__(kTileThreads, 3)  // 3 CTAs: no spills at 42 r
       hi = lo + kTile < n ? lo + kTile : n;
     }
   };
-  int2 tup[4];
+  int2 tup[kTilePer];
   auto load_tile = [&](uint64_t lo, uint64_t hi) {
 #pragma unroll
-    for (int j = 0; j < 4; ++j) {
+    for (int j = 0; j < kTilePer; ++j) {
       const uint64_t i = lo + tid + j * kTileThreads;
       if (i < hi) {
         if (kPairsIn) {
@@ -171,9 +173,9 @@ __global__ void __launch_bounds__(kTileThreads, 3)  // 3 CTAs: no spills at 42 r
   for (; t < ntiles; t += gridDim.x) {
     for (uint32_t d = lane; d < ndig; d += 32) S.whist[warp][d] = 0;
     __syncwarp();
-    uint32_t dg[4], rk[4];
+    uint32_t dg[kTilePer], rk[kTilePer];
 #pragma unroll
-    for (int j = 0; j < 4; ++j) {
+    for (int j = 0; j < kTilePer; ++j) {
       if (lo + tid + j * kTileThreads < hi) {
         dg[j] = digit_of<kDigit>(tup[j].x, dshift, dmask);
         rk[j] = atomicAdd(&S.whist[warp][dg[j]], 1u);
@@ -212,7 +214,7 @@ __global__ void __launch_bounds__(kTileThreads, 3)  // 3 CTAs: no spills at 42 r
     }
     __syncthreads();
 #pragma unroll
-    for (int j = 0; j < 4; ++j) {
+    for (int j = 0; j < kTilePer; ++j) {
       if (lo + tid + j * kTileThreads < hi) {
         const uint32_t pos = S.dstart[dg[j]] + S.whist[warp][dg[j]] + rk[j];
         S.sorted[pos] = tup[j];
@@ -228,7 +230,7 @@ __global__ void __launch_bounds__(kTileThreads, 3)  // 3 CTAs: no spills at 42 r
     }
     __syncthreads();
 #pragma unroll
-    for (int j = 0; j < 4; ++j) {
+    for (int j = 0; j < kTilePer; ++j) {
       const uint32_t i = tid + j * kTileThreads;
       if (i < cnt) {
         const uint32_t d = S.sdig[i];
