@@ -152,6 +152,14 @@ class RelBuilder {
     return RelBuilder("{\"operator\":\"reduce\",\"input\":" + json_ + ",\"e\":[" + es + "],\"accumulator\":[" +
                       as + "],\"p\":{\"expression\":\"bool\",\"v\":true}}");
   }
+  // ORDER BY: (expression, "ASC" | "DESC" | "NONE") per key (reference's sort).
+  RelBuilder sort(const std::vector<std::pair<Expr, std::string>> &keys) const {
+    std::string es;
+    for (const auto &k : keys)
+      es += (es.empty() ? "" : ",") + std::string("{\"expression\":") + k.first.json() +
+            ",\"direction\":" + Expr::q(k.second) + "}";
+    return RelBuilder("{\"operator\":\"sort\",\"input\":" + json_ + ",\"e\":[" + es + "]}");
+  }
   PreparedStatement prepare(gbj_catalog *cat) const { return PreparedStatement(cat, json_); }
   const std::string &json() const { return json_; }
 

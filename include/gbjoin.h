@@ -504,9 +504,10 @@ int gbj_tune_load(gbj_ctx *ctx, const char *path);
  * fields of core/olap/lib/plan/plan-parser.cpp; expressions of
  * core/olap/lib/plan/expression-parser.cpp) over int32 device columns named
  * in a catalog (relation name = the scan plugin's "name", attribute = the
- * projection's "attrName").  Supported operators: scan, select,
- * hashjoin-chained, partitioned-hashjoin-chained, join, groupby /
- * hashgroupby-chained (one int32 key) and reduce (the last two at the root);
+ * projection's "attrName").  Supported operators: scan, select, project,
+ * sort, hash-rearrange / hash-pack, hashjoin-chained,
+ * partitioned-hashjoin-chained, join, groupby / hashgroupby-chained (one
+ * int32 key) and reduce (the last two at the root, or under a root sort);
  * expressions recordProjection, int, int64, bool, cast, eq, lt, le, gt, ge,
  * and, multiply; accumulators sum, max, min.  Anything else gives
  * GBJ_ERR_UNSUPPORTED with a message naming it.  Sizing fields (hash_bits,

@@ -3,7 +3,9 @@
 // by lowering each operator onto the C ABI.
 //
 // Operators: scan (plugin.name + projections, plan-parser.cpp scan cases),
-// select (p), hashjoin-chained (build_input, probe_input, build_k, probe_k,
+// select (p), project (e), sort (e[{expression, direction}], :353-389),
+// hash-rearrange / hash-pack (e, projections, buckets; :1424-1458),
+// hashjoin-chained (build_input, probe_input, build_k, probe_k,
 // hash_bits, maxBuildInputSize; plan-parser.cpp:977-1006),
 // partitioned-hashjoin-chained (:851-976) and join (radix; p{eq},
 // leftInput, rightInput; :1007-1139), groupby / hashgroupby-chained (input,
@@ -260,10 +262,27 @@ void validate(const JVal &v) {
     for (const JVal &a : acc.a) monoid(a.s);
     need(v, "e", "reduce");
     validate(need(v, "input", "reduce"));
+  } else if (op == "sort") {
+    const JVal &e = need(v, "e", "sort");
+    for (const JVal &x : e.a) {
+      need(x, "expression", "sort");
+      const std::string d = need(x, "direction", "sort").s;
+      if (d != "ASC" && d != "DESC" && d != "NONE")
+        fail(GBJ_ERR_INVALID, "plan: sort direction '" + d + "' (ASC, DESC, NONE)");
+    }
+    validate(need(v, "input", "sort"));
+  } else if (op == "project") {
+    need(v, "e", "project");
+    validate(need(v, "input", "project"));
+  } else if (op == "hash-rearrange" || op == "hash-pack") {
+    need(v, "e", op.c_str());
+    need(v, "projections", op.c_str());
+    validate(need(v, "input", op.c_str()));
   } else {
     fail(GBJ_ERR_UNSUPPORTED, "plan: operator '" + op +
-                                  "' is not supported (scan, select, hashjoin-chained, "
-                                  "partitioned-hashjoin-chained, join, groupby, hashgroupby-chained, reduce are)");
+                                  "' is not supported (scan, select, project, sort, hashjoin-chained, "
+                                  "partitioned-hashjoin-chained, join, groupby, hashgroupby-chained, "
+                                  "reduce, hash-rearrange, hash-pack are)");
   }
 }
 
@@ -314,10 +333,17 @@ class Exec {
   gbj_result *run(const JVal &root) {
     auto res = std::make_unique<gbj_result>();
     const std::string op = op_name(root);
+    const std::string iop = op == "sort" ? op_name(need(root, "input", "sort")) : std::string();
     if (op == "reduce") {
       reduce(root, res.get());
     } else if (op == "groupby" || op == "hashgroupby-chained") {
       groupby(root, res.get());
+    } else if (iop == "groupby" || iop == "hashgroupby-chained" || iop == "reduce") {
+      // ORDER BY over an aggregate's (small, int64) result: ordered on the host
+      const JVal &in = need(root, "input", "sort");
+      if (iop == "reduce") reduce(in, res.get());
+      else groupby(in, res.get());
+      host_sort(root, res.get());
     } else {
       const Rel r = rel(root);
       res->rows = r.n;
@@ -377,10 +403,115 @@ class Exec {
     if (op == "scan") return scan(v);
     if (op == "select") return select(v);
     if (op == "hashjoin-chained" || op == "partitioned-hashjoin-chained" || op == "join") return join(v);
+    if (op == "sort") return sort(v);
+    if (op == "project") return project(v);
+    if (op == "hash-rearrange" || op == "hash-pack") return rearrange(v);
     if (op == "groupby" || op == "hashgroupby-chained" || op == "reduce")
       fail(GBJ_ERR_UNSUPPORTED, "plan: '" + op + "' is supported only as the plan's root");
     validate(v);  // raises the unsupported-operator error
     fail(GBJ_ERR_UNSUPPORTED, "plan: operator '" + op + "'");
+  }
+
+  // ORDER BY: stable device sorts from the last key to the first.
+  Rel sort(const JVal &v) {
+    Rel r = rel(need(v, "input", "sort"));
+    const JVal &es = need(v, "e", "sort");
+    if (r.cols.empty() || r.n == 0) return r;
+    if (r.cols.size() > GBJ_SORT_MAX_COLS) fail(GBJ_ERR_UNSUPPORTED, "plan: sort of more than 16 columns");
+    for (size_t k = es.a.size(); k-- > 0;) {
+      const std::string dir = need(es.a[k], "direction", "sort").s;
+      if (dir == "NONE") continue;
+      const auto ra = projection(need(es.a[k], "expression", "sort"));
+      int key = -1;
+      for (size_t c = 0; c < r.cols.size(); ++c)
+        if (r.find(ra) == &r.cols[c]) key = (int)c;
+      if (key < 0) fail(GBJ_ERR_INVALID, "plan: sort key " + ra.second + " is not in its input");
+      std::vector<const int32_t *> in;
+      std::vector<int32_t *> out;
+      for (auto &c : r.cols) {
+        in.push_back(c.d);
+        out.push_back(alloc<int32_t>(r.n));
+      }
+      ck(gbj_sort_by_key(ctx_, in.data(), (int32_t)in.size(), r.n, key, dir == "DESC", out.data(), nullptr),
+         "sort");
+      for (size_t c = 0; c < r.cols.size(); ++c) r.cols[c].d = out[c];
+    }
+    return r;
+  }
+
+  Rel project(const JVal &v) {
+    const Rel r = rel(need(v, "input", "project"));
+    Rel o;
+    o.n = r.n;
+    for (const JVal &e : need(v, "e", "project").a) {
+      const auto ra = projection(e);
+      const Rel::C *c = r.find(ra);
+      if (!c) fail(GBJ_ERR_INVALID, "plan: project column " + ra.second + " is not in its input");
+      o.cols.push_back(*c);
+    }
+    return o;
+  }
+
+  // Router-side partition: rows bucket-major by hash(e) mod buckets.
+  Rel rearrange(const JVal &v) {
+    const std::string op = op_name(v);
+    const Rel r = rel(need(v, "input", op.c_str()));
+    const auto key = projection(need(v, "e", op.c_str()));
+    int32_t buckets = 2;  // the reference's default
+    if (const JVal *b = v.get("buckets")) buckets = (int32_t)b->i;
+    Rel o;
+    o.n = r.n;
+    std::vector<const int32_t *> in;
+    std::vector<int32_t *> out;
+    int key_col = -1;
+    for (const JVal &p : need(v, "projections", op.c_str()).a) {
+      const auto ra = projection(p);
+      const Rel::C *c = r.find(ra);
+      if (!c) fail(GBJ_ERR_INVALID, "plan: " + op + " column " + ra.second + " is not in its input");
+      if (ra.second == key.second && (key.first.empty() || ra.first.empty() || ra.first == key.first))
+        key_col = (int)in.size();
+      in.push_back(c->d);
+      out.push_back(alloc<int32_t>(r.n));
+      o.cols.push_back({c->rel, c->attr, out.back()});
+    }
+    if (key_col < 0) {  // the hash key need not be projected
+      const Rel::C *c = r.find(key);
+      if (!c) fail(GBJ_ERR_INVALID, "plan: " + op + " key " + key.second + " is not in its input");
+      key_col = (int)in.size();
+      in.push_back(c->d);
+      out.push_back(alloc<int32_t>(r.n));
+    }
+    if (in.size() > GBJ_REARRANGE_MAX_COLS) fail(GBJ_ERR_UNSUPPORTED, "plan: more than 16 columns to rearrange");
+    uint64_t *off = alloc<uint64_t>((uint64_t)buckets + 1);
+    ck(gbj_hash_rearrange(ctx_, in.data(), (int32_t)in.size(), r.n, key_col, (uint32_t)buckets, out.data(), off,
+                          nullptr),
+       op.c_str());
+    return o;
+  }
+
+  // ORDER BY over an aggregate's host result (stable, last key first).
+  void host_sort(const JVal &v, gbj_result *res) {
+    const JVal &es = need(v, "e", "sort");
+    std::vector<size_t> order(res->rows);
+    for (size_t i = 0; i < order.size(); ++i) order[i] = i;
+    for (size_t k = es.a.size(); k-- > 0;) {
+      const std::string dir = need(es.a[k], "direction", "sort").s;
+      if (dir == "NONE") continue;
+      const auto ra = projection(need(es.a[k], "expression", "sort"));
+      int c = -1;
+      for (size_t j = 0; j < res->names.size(); ++j)
+        if (res->names[j] == ra.second || res->names[j] == ra.first + "." + ra.second) c = (int)j;
+      if (c < 0) fail(GBJ_ERR_INVALID, "plan: sort key " + ra.second + " is not an output column");
+      const auto &col = res->cols[c];
+      std::stable_sort(order.begin(), order.end(), [&](size_t a, size_t b) {
+        return dir == "DESC" ? col[a] > col[b] : col[a] < col[b];
+      });
+    }
+    for (auto &col : res->cols) {
+      std::vector<int64_t> t(col.size());
+      for (size_t i = 0; i < order.size(); ++i) t[i] = col[order[i]];
+      col.swap(t);
+    }
   }
 
   Rel scan(const JVal &v) {

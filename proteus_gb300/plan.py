@@ -126,6 +126,18 @@ class RelBuilder:
         return RelBuilder({"operator": "reduce", "input": self.node, "e": [x.node for x in e],
                            "accumulator": list(accumulators), "p": lit(True).node})
 
+    def sort(self, keys) -> "RelBuilder":
+        """keys: [(Expr, "ASC" | "DESC" | "NONE")]."""
+        return RelBuilder({"operator": "sort", "input": self.node,
+                           "e": [{"expression": x.node, "direction": d} for x, d in keys]})
+
+    def project(self, e) -> "RelBuilder":
+        return RelBuilder({"operator": "project", "input": self.node, "e": [x.node for x in e]})
+
+    def hash_rearrange(self, key: Expr, projections, buckets: int = 2) -> "RelBuilder":
+        return RelBuilder({"operator": "hash-rearrange", "input": self.node, "e": key.node,
+                           "projections": [x.node for x in projections], "buckets": buckets})
+
     def json(self) -> str:
         return json.dumps(self.node)
 

@@ -146,3 +146,25 @@ def test_cpp_relbuilder_executes(golden, tmp_path):
     for name in ("multinestReserves", "nestBagTPCH"):
         got = sorted(zip(res[name]["sum_0"], res[name]["max_1"]))
         assert [list(x) for x in got] == expected(golden, name)["count_max"]
+
+
+def test_sort_over_groupby_and_relation(cat, golden, big):
+    # ORDER BY over a group-by (host-ordered aggregate result)
+    out = cat.execute(plan_cases.multinest_reserves().sort([(col(plan_cases.R, "sid"), "DESC")]))
+    assert out["sid"].tolist() == sorted(out["sid"].tolist(), reverse=True)
+    # ORDER BY over a relation (device sort), two keys, stable
+    c, bk, bp, pk, pp = big
+    plan = (RelBuilder.scan("S", ["k", "p"]).filter(col("S", "p") < 50)
+            .sort([(col("S", "p"), "ASC"), (col("S", "k"), "DESC")]))
+    o = c.execute(plan)
+    m = pp < 50
+    exp = sorted(zip(pp[m].tolist(), (-pk[m].astype(np.int64)).tolist()))
+    assert list(zip(o["S.p"].tolist(), (-o["S.k"]).tolist())) == exp
+
+
+def test_project_and_rearrange(big):
+    c, bk, bp, pk, pp = big
+    o = c.execute(RelBuilder.scan("S", ["k", "p"]).project([col("S", "p")]))
+    assert list(o) == ["S.p"] and (o["S.p"] == pp).all()
+    o = c.execute(RelBuilder.scan("S", ["k", "p"]).hash_rearrange(col("S", "k"), [col("S", "k"), col("S", "p")], 64))
+    assert sorted(zip(o["S.k"].tolist(), o["S.p"].tolist())) == sorted(zip(pk.tolist(), pp.tolist()))

@@ -65,3 +65,16 @@ def test_cpp_relbuilder_plans_validate(lib, tmp_path):
     lines = [x.split(" ", 2) for x in out if x.strip()]
     assert [x[0] for x in lines] == ["sailorsJoinLeft3", "multinestReserves", "nestBagTPCH"]
     assert all(x[1] == "0" for x in lines), lines
+
+
+def test_sort_project_rearrange_validate(lib):
+    from proteus_gb300.plan import RelBuilder, col, lit
+
+    g = plan_cases.nest_reserves().sort([(col(plan_cases.R, "sid"), "DESC")])
+    assert validate(g)[0] == abi.OK
+    s = RelBuilder.scan("a", ["k", "v"]).project([col("a", "v")]).hash_rearrange(col("a", "v"), [col("a", "v")], 8)
+    assert validate(s)[0] == abi.OK
+    bad = json.loads(g.json())
+    bad["e"][0]["direction"] = "UP"
+    rc, msg = validate(bad)
+    assert rc == abi.ERR_INVALID and "UP" in msg
