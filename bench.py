@@ -60,6 +60,25 @@ def parse():
     return ap.parse_args()
 
 
+def max_over_ranks(ms: float, world: int, device: str = "cuda") -> float:
+    """The slowest rank's time: every rank's timed region ends when all have
+    finished (all-reduce MAX over the process group; any backend)."""
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+
+        t = torch.tensor([ms], dtype=torch.float64, device=device)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    return ms
+
+
+def job_value(units_per_rank_step: float, steps: int, ms: float, world: int, scale: float) -> float:
+    """Whole-job throughput: the units all ranks processed / the slowest
+    rank's time (replicas: every rank runs the same per-rank work)."""
+    return world * units_per_rank_step * steps / (ms / 1e3) / scale
+
+
 def dist_env():
     return (int(os.environ.get("RANK", 0)), int(os.environ.get("LOCAL_RANK", 0)),
             int(os.environ.get("WORLD_SIZE", 1)))
@@ -795,13 +814,6 @@ def run_gpu(args):
             torch.distributed.barrier()
         torch.cuda.synchronize()
 
-    def max_over_ranks(ms):
-        if world > 1:
-            t = torch.tensor([ms], device="cuda")
-            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-            ms = float(t.item())
-        return ms
-
     # ---- device-timed steps (inputs resident) ----
     clocks = ClockSampler(local_rank)
     barrier()
@@ -814,14 +826,14 @@ def run_gpu(args):
         wl.step()
     e1.record(stream)
     barrier()
-    ms = max_over_ranks(e0.elapsed_time(e1))
+    ms = max_over_ranks(e0.elapsed_time(e1), world)
     launches = ctx.launches() - launches0
     prof = ctx.profile_dump()
     ctx.profile(False)
     clk = clocks.stop()
     ctx.sync()
     scale = getattr(wl, "scale", 1e9)
-    value = world * wl.units_per_step() * args.steps / (ms / 1e3) / scale
+    value = job_value(wl.units_per_step(), args.steps, ms, world, scale)
 
     # ---- roofline of the dominant kernel ----
     peak, peak_kind = hbm_peak()
@@ -852,9 +864,9 @@ def run_gpu(args):
             wl.e2e_step()
         f1.record(stream)
         barrier()
-        ems = max_over_ranks(f0.elapsed_time(f1))
+        ems = max_over_ranks(f0.elapsed_time(f1), world)
         assert wl.e2e_results() == results, "e2e results differ from resident results"
-        e2e = {"value": world * wl.units_per_step() * args.steps / (ems / 1e3) / scale,
+        e2e = {"value": job_value(wl.units_per_step(), args.steps, ems, world, scale),
                "unit": wl.unit, "h2d_bytes_per_step": wl.h2d_bytes(),
                "d2h_bytes_per_step": wl.d2h_bytes(), "ms_per_step": ems / args.steps}
 
