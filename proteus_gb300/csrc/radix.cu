@@ -47,6 +47,10 @@ constexpr int kTile = 4096;          // tuples per tile of a partition pass
 constexpr int kTileThreads = 512;
 constexpr int kTilePer = kTile / kTileThreads;  // tuples per thread
 constexpr int kTileCtas = 2;                    // CTAs per SM (register budget)
+// Join kernel: largest build chunk held on chip, threads and CTAs per SM.
+constexpr int kJoinRMax = 9216;
+constexpr int kJoinThreads = 1024;
+constexpr int kJoinCtas = 1;
 constexpr int kTileWarps = kTileThreads / 32;
 constexpr int kMaxDigits = 256;      // <= 8 digit bits per pass
 constexpr int32_t kEmpty = INT32_MIN;
@@ -343,7 +347,7 @@ __device__ __forceinline__ void join_match(const gbj::AggSpec &spec, gbjd::Acc &
 //   keys[cap] + values[cap]            (every partition but one), or
 //   pairs[kRMax] + index[cap] (16-bit) (the partition INT32_MIN maps to).
 template <int kRMax, int kThreads, int kAgg>
-__global__ void __launch_bounds__(kThreads, 1)
+__global__ void __launch_bounds__(kThreads, kJoinCtas)
     k_radix_join(const int2 *__restrict__ R, const uint64_t *__restrict__ ro,
                  const int2 *__restrict__ S, const uint64_t *__restrict__ so,
                  const uint64_t *__restrict__ item_off, uint32_t P, int bits, uint64_t w,
@@ -405,7 +409,7 @@ __global__ void __launch_bounds__(kThreads, 1)
           if (++h == cap) h = 0;
         }
       };
-      // the whole chunk's loads in flight at once (m <= 9216 = 9 per thread)
+      // the whole chunk's loads in flight at once (8 per thread per round)
       for (uint64_t i0 = rb + threadIdx.x; i0 < re; i0 += 8 * kThreads) {
         int2 t[8];
 #pragma unroll
@@ -732,7 +736,7 @@ int gbj_radix_join_agg(gbj_ctx *ctx, const int32_t *d_build_keys,
 
   // ---- plan: fewest radix bits whose largest expected build partition
   //      (mean + 5 sd) fits the on-chip table; explicit params override ----
-  constexpr int kRMax = 9216;
+  constexpr int kRMax = kJoinRMax;
   int bits = 1;
   while (bits < kMaxPartBits) {
     const double mean = (double)n_build / (double)(1u << bits);
@@ -772,12 +776,12 @@ int gbj_radix_join_agg(gbj_ctx *ctx, const int32_t *d_build_keys,
   GBJ_CHECK_CUDA(ctx, cudaMemsetAsync(ctr, 0, sizeof(unsigned long long), s));
   const bool two = spec.n == 2 && spec.op[0] == GBJ_AGG_COUNT && spec.op[1] == GBJ_AGG_SUM;
   if (two && spec.operand[1] == GBJ_VAL_ROWID_XOR)
-    return launch_join<kRMax, 1024, kAggCountXor>(ctx, R, ro, S, so, items, P, bits, w, sentinel_part,
+    return launch_join<kRMax, kJoinThreads, kAggCountXor>(ctx, R, ro, S, so, items, P, bits, w, sentinel_part,
                                                   spec, d_out, ctr, s);
   if (two && spec.operand[1] == GBJ_VAL_PRODUCT)
-    return launch_join<kRMax, 1024, kAggCountProduct>(ctx, R, ro, S, so, items, P, bits, w,
+    return launch_join<kRMax, kJoinThreads, kAggCountProduct>(ctx, R, ro, S, so, items, P, bits, w,
                                                       sentinel_part, spec, d_out, ctr, s);
-  return launch_join<kRMax, 1024, kAggGeneric>(ctx, R, ro, S, so, items, P, bits, w, sentinel_part,
+  return launch_join<kRMax, kJoinThreads, kAggGeneric>(ctx, R, ro, S, so, items, P, bits, w, sentinel_part,
                                                spec, d_out, ctr, s);
 }
 
