@@ -188,6 +188,20 @@ int gbj_partition(gbj_ctx *ctx, const int32_t *d_keys,
  * reads GBJ_VAL_BUILD/PROBE/PRODUCT, its row position if one reads a rowid
  * operand (mixing both on one side gives GBJ_ERR_UNSUPPORTED).  Work items
  * are sized on the device, so the call never synchronises with the host. */
+/* Radix clustering of {int64 key, int64 payload} tuples: the aggregation
+ * twins radix_cluster_nopadding / partitionHT of core/platform/lib/util/
+ * radix/aggregations/radix-aggr.cpp:82-155,237-259 (agg::tuple_t, KEY_8B).
+ * Digit = (key >> shift) & (2^bits - 1) of the 64-bit key; output
+ * partition-major (unordered inside a partition), offsets 2^bits + 1;
+ * d_payload NULL carries 0-based row ids.  partitionHT's clustering is two
+ * calls (shift 0, bits 7; then per the reference, bits 7..13) or one call
+ * with bits 14, which gives the same clusters and counts. */
+int gbj_partition_i64(gbj_ctx *ctx, const int64_t *d_keys,
+                      const int64_t *d_payload, uint64_t n, int32_t shift,
+                      int32_t bits, int64_t *d_out_keys,
+                      int64_t *d_out_payload, uint64_t *d_offsets,
+                      void *stream);
+
 typedef struct gbj_radix_params {
   int32_t bits;       /* radix bits, 0 = autotuned                        */
   int32_t passes;     /* 1 or 2, 0 = autotuned                            */

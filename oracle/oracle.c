@@ -1137,3 +1137,47 @@ int64_t orc_bloom_semijoin(const int32_t *build, uint64_t nb, const int32_t *pro
   free(flags);
   return m;
 }
+
+/* ----------------------------------- radix clustering of int64-key tuples */
+/* The aggregation twin of radix_cluster_nopadding (core/platform/lib/util/
+ * radix/aggregations/radix-aggr.cpp:82-155): stable counting sort of
+ * agg::tuple_t {int64 key; int64 payload} on digit
+ * (key & (((1 << D) - 1) << R)) >> R of the 64-bit key. */
+void orc_radix_cluster_i64(const int64_t *keys, const int64_t *payload, uint64_t n, int32_t R, int32_t D,
+                           int64_t *out_keys, int64_t *out_payload, uint64_t *offsets) {
+  const uint64_t M = ((1ULL << D) - 1) << R;
+  const uint64_t parts = 1ULL << D;
+  uint64_t *hist = (uint64_t *)calloc(parts + 1, sizeof(uint64_t));
+  for (uint64_t i = 0; i < n; ++i) hist[(((uint64_t)keys[i]) & M) >> R]++;
+  uint64_t acc = 0;
+  for (uint64_t p = 0; p < parts; ++p) {
+    const uint64_t c = hist[p];
+    hist[p] = acc;
+    if (offsets) offsets[p] = acc;
+    acc += c;
+  }
+  if (offsets) offsets[parts] = acc;
+  for (uint64_t i = 0; i < n; ++i) {
+    const uint64_t d = (((uint64_t)keys[i]) & M) >> R;
+    const uint64_t o = hist[d]++;
+    out_keys[o] = keys[i];
+    out_payload[o] = payload ? payload[i] : (int64_t)i;
+  }
+  free(hist);
+}
+
+/* partitionHT of the twin (radix-aggr.cpp:237-259): two passes (bits [0,7)
+ * then [7,14)), then the number of tuples per cluster key & (2^14 - 1).
+ * out_keys / out_payload get the clustered tuples (payload = row id). */
+void orc_partition_ht_agg(const int64_t *keys, uint64_t n, int32_t *counts, int64_t *out_keys,
+                          int64_t *out_payload) {
+  int64_t *tk = (int64_t *)malloc((n ? n : 1) * sizeof(int64_t));
+  int64_t *tp = (int64_t *)malloc((n ? n : 1) * sizeof(int64_t));
+  orc_radix_cluster_i64(keys, 0, n, 0, ORC_RADIX_BITS / ORC_PASSES, tk, tp, 0);
+  orc_radix_cluster_i64(tk, tp, n, ORC_RADIX_BITS / ORC_PASSES, ORC_RADIX_BITS - ORC_RADIX_BITS / ORC_PASSES,
+                        out_keys, out_payload, 0);
+  memset(counts, 0, sizeof(int32_t) << ORC_RADIX_BITS);
+  for (uint64_t i = 0; i < n; ++i) counts[(uint64_t)out_keys[i] & ((1u << ORC_RADIX_BITS) - 1)]++;
+  free(tk);
+  free(tp);
+}

@@ -159,6 +159,16 @@ int64_t orc_bloom_semijoin(const int32_t *build, uint64_t nb, const int32_t *pro
                            uint64_t np, uint64_t filter_size, int32_t *rows,
                            uint64_t cap);
 
+
+/* Aggregation twins (core/platform/lib/util/radix/aggregations/radix-aggr.cpp):
+ * stable radix cluster of {int64 key, int64 payload} tuples (payload 0 =
+ * row ids) and partitionHT's two-pass cluster + counts on 2^14 clusters. */
+void orc_radix_cluster_i64(const int64_t *keys, const int64_t *payload,
+                           uint64_t n, int32_t R, int32_t D, int64_t *out_keys,
+                           int64_t *out_payload, uint64_t *offsets);
+void orc_partition_ht_agg(const int64_t *keys, uint64_t n, int32_t *counts,
+                          int64_t *out_keys, int64_t *out_payload);
+
 #ifdef __cplusplus
 }
 #endif

@@ -68,6 +68,10 @@ def lib():
         L.orc_groupby.argtypes = [vp, vp, u64, i32, C.c_int, vp, vp, vp, vp, vp, u64]
         L.orc_reduce.restype = None
         L.orc_reduce.argtypes = [vp, vp, u64, vp, vp, i32, vp]
+        L.orc_radix_cluster_i64.restype = None
+        L.orc_radix_cluster_i64.argtypes = [vp, vp, u64, i32, i32, vp, vp, vp]
+        L.orc_partition_ht_agg.restype = None
+        L.orc_partition_ht_agg.argtypes = [vp, u64, vp, vp, vp]
         L.orc_bloom_semijoin.restype = i64
         L.orc_bloom_semijoin.argtypes = [vp, u64, vp, u64, u64, vp, u64]
         L.orc_join_groupby.restype = i64
@@ -87,6 +91,8 @@ def ref_lib():
         R.ref_rj_stepwise.argtypes = [vp, C.c_uint32, vp, C.c_uint32]
         R.ref_partition_ht.restype = None
         R.ref_partition_ht.argtypes = [vp, C.c_uint32, vp, vp, vp]
+        R.ref_partition_ht_agg.restype = None
+        R.ref_partition_ht_agg.argtypes = [vp, C.c_uint32, vp, vp, vp]
         R.ref_num_radix_bits.restype = i32
         _ref = R
     return _ref
@@ -202,6 +208,29 @@ def reduce(col, aggs, rows=None):
     return [int(x) for x in out]
 
 
+def radix_cluster_i64(keys, payload, R, D):
+    """-> (clustered keys, payloads, offsets[2^D + 1]), stable."""
+    L = lib()
+    keys = np.ascontiguousarray(keys, dtype=np.int64)
+    pay = None if payload is None else np.ascontiguousarray(payload, dtype=np.int64)
+    n = len(keys)
+    ok, op = np.empty(max(n, 1), np.int64), np.empty(max(n, 1), np.int64)
+    off = np.empty((1 << D) + 1, np.uint64)
+    L.orc_radix_cluster_i64(_p(keys), _p(pay), n, R, D, _p(ok), _p(op), _p(off))
+    return ok[:n], op[:n], off
+
+
+def partition_ht_agg(keys):
+    """partitionHT of the int64-key twin -> (counts[2^14], keys, row ids)."""
+    L = lib()
+    keys = np.ascontiguousarray(keys, dtype=np.int64)
+    n = len(keys)
+    c = np.empty(1 << 14, np.int32)
+    ok, op = np.empty(max(n, 1), np.int64), np.empty(max(n, 1), np.int64)
+    L.orc_partition_ht_agg(_p(keys), n, _p(c), _p(ok), _p(op))
+    return c, ok[:n], op[:n]
+
+
 def bloom_semijoin(build, probe, filter_size):
     """Positions of the probe rows the reference's bloom filter passes."""
     L = lib()
@@ -278,6 +307,19 @@ def ref_rj_stepwise(rkeys, skeys):
         return None
     rkeys, skeys = _i32(rkeys), _i32(skeys)
     return int(R.ref_rj_stepwise(_p(rkeys), len(rkeys), _p(skeys), len(skeys)))
+
+
+def ref_partition_ht_agg(keys):
+    """The reference's own int64-key partitionHT (oracle/_ref)."""
+    R = ref_lib()
+    if R is None:
+        return None
+    keys = np.ascontiguousarray(keys, dtype=np.int64)
+    n = len(keys)
+    c = np.empty(1 << 14, dtype=np.int32)
+    ok, op = np.empty(max(n, 1), np.int64), np.empty(max(n, 1), np.int64)
+    R.ref_partition_ht_agg(_p(keys), n, _p(c), _p(ok), _p(op))
+    return c, ok[:n], op[:n]
 
 
 def ref_partition_ht(keys):

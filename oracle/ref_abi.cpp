@@ -1,8 +1,11 @@
 // extern "C" entry points over the reference's own radix-join helpers
-// (core/platform/lib/util/radix/joins/radix-join.cpp), compiled from the
+// (core/platform/lib/util/radix/joins/radix-join.cpp) and their int64-key
+// aggregation twins (core/platform/lib/util/radix/aggregations/
+// radix-aggr.cpp), compiled from the
 // reference sources in place by oracle/Makefile into oracle/_ref/.  TEST
 // INFRASTRUCTURE ONLY: used to pin the oracle's restatement and to produce
 // the committed golden counts under tests/golden/.
+#include <platform/util/radix/aggregations/radix-aggr.hpp>
 #include <platform/util/radix/joins/radix-join.hpp>
 
 #include <cstdlib>
@@ -42,6 +45,23 @@ void ref_partition_ht(const int32_t *keys, uint32_t n, int32_t *counts,
   for (uint32_t i = 0; i < n; ++i) {
     if (out_keys) out_keys[i] = t[i].key;
     if (out_rows) out_rows[i] = t[i].payload;
+  }
+  free(c);
+  free(t);
+}
+
+// partitionHT of the aggregation twin: agg::tuple_t {int64 key; int64
+// payload} (core/platform/include/platform/util/radix/aggregations/types.h),
+// clustered in place on the low NUM_RADIX_BITS key bits; counts per cluster.
+void ref_partition_ht_agg(const int64_t *keys, uint32_t n, int32_t *counts, int64_t *out_keys,
+                          int64_t *out_payload) {
+  agg::tuple_t *t = (agg::tuple_t *)malloc(n * sizeof(agg::tuple_t) + 64);
+  for (uint32_t i = 0; i < n; ++i) t[i] = {keys[i], (int64_t)i};
+  int *c = partitionHT(n, t);
+  memcpy(counts, c, sizeof(int) << NUM_RADIX_BITS);
+  for (uint32_t i = 0; i < n; ++i) {
+    if (out_keys) out_keys[i] = t[i].key;
+    if (out_payload) out_payload[i] = t[i].payload;
   }
   free(c);
   free(t);

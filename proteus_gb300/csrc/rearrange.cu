@@ -60,7 +60,60 @@ __global__ void __launch_bounds__(256)
   }
 }
 
+// Digit of an int64 key: (key >> shift) & mask over the 64-bit key.
+__global__ void __launch_bounds__(256)
+    k_digits_i64(const int64_t *__restrict__ keys, uint64_t n, int shift, uint64_t mask, int32_t *__restrict__ ids) {
+  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += stride)
+    ids[i] = (int32_t)(((uint64_t)__ldcs(keys + i) >> shift) & mask);
+}
+
+// Clustered {int64 key, int64 payload} tuples (payload null: row ids).
+__global__ void __launch_bounds__(256)
+    k_gather_i64(const int2 *__restrict__ pairs, uint64_t n, const int64_t *__restrict__ keys,
+                 const int64_t *__restrict__ payload, int64_t *__restrict__ out_keys, int64_t *__restrict__ out_payload) {
+  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += stride) {
+    const uint32_t r = (uint32_t)__ldcs(&pairs[i].y);
+    out_keys[i] = __ldg(keys + r);
+    out_payload[i] = payload ? __ldg(payload + r) : (int64_t)r;
+  }
+}
+
 }  // namespace
+
+// Radix clustering of 16-byte {int64 key, int64 payload} tuples, the
+// aggregation twin of radix_cluster_nopadding / partitionHT
+// (core/platform/lib/util/radix/aggregations/radix-aggr.cpp:82-155,237-259):
+// one digit kernel, the tile-pass partitioner on (digit, row) pairs, one
+// gather of the 16-byte tuples.
+extern "C" int gbj_partition_i64(gbj_ctx *ctx, const int64_t *d_keys, const int64_t *d_payload, uint64_t n,
+                                 int32_t shift, int32_t bits, int64_t *d_out_keys, int64_t *d_out_payload,
+                                 uint64_t *d_offsets, void *stream) {
+  if (!ctx) return GBJ_ERR_INVALID;
+  if (bits < 1 || bits > kMaxPartBits || shift < 0 || shift > 63)
+    return set_error(ctx, GBJ_ERR_INVALID, "partition_i64: bits must be 1..15, shift 0..63");
+  if (n && (!d_keys || !d_out_keys || !d_out_payload)) return set_error(ctx, GBJ_ERR_INVALID, "partition_i64: null column");
+  if (!d_offsets) return set_error(ctx, GBJ_ERR_INVALID, "partition_i64: null offsets");
+  if (n >= (1ull << 31)) return set_error(ctx, GBJ_ERR_INVALID, "partition_i64: n >= 2^31");
+  cudaStream_t s = pick_stream(ctx, stream);
+  prof_mark(ctx, s);
+  if (n == 0) {
+    GBJ_CHECK_CUDA(ctx, cudaMemsetAsync(d_offsets, 0, sizeof(uint64_t) * ((1ull << bits) + 1), s));
+    return GBJ_OK;
+  }
+  Scratch scratch(ctx, s);
+  int32_t *ids;
+  int2 *pairs;
+  GBJ_TRY(scratch.get(n, &ids));
+  GBJ_TRY(scratch.get(n, &pairs));
+  const unsigned grid = (unsigned)std::min<uint64_t>((n + 255) / 256, (uint64_t)ctx->sm_count * 16);
+  k_digits_i64<<<grid, 256, 0, s>>>(d_keys, n, shift, (1ull << bits) - 1, ids);
+  GBJ_TRY(after_launch(ctx, "k_digits_i64", s));
+  GBJ_TRY(partition_tuples(ctx, ids, nullptr, n, GBJ_DIGIT_KEY, 0, bits, pairs, nullptr, nullptr, d_offsets, s));
+  k_gather_i64<<<grid, 256, 0, s>>>(pairs, n, d_keys, d_payload, d_out_keys, d_out_payload);
+  return after_launch(ctx, "k_gather_i64", s);
+}
 
 extern "C" int gbj_hash_rearrange(gbj_ctx *ctx, const int32_t *const *d_cols, int32_t n_cols, uint64_t n,
                                   int32_t key_col, uint32_t num_buckets, int32_t *const *d_out_cols,

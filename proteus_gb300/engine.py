@@ -231,6 +231,18 @@ class Context:
     def bloom_destroy(self, bloom):
         self.check(self.lib.gbj_bloom_destroy(self.handle, bloom))
 
+    # ------------------------------------------- int64-key radix clustering
+    def partition_i64(self, keys, payload, bits, shift=0, stream=None):
+        """-> (clustered keys, payloads, offsets[2^bits + 1]) of int64 tuples."""
+        import torch
+
+        ok = torch.empty_like(keys)
+        op = torch.empty_like(keys)
+        off = torch.empty((1 << bits) + 1, dtype=torch.int64, device=keys.device)
+        self.check(self.lib.gbj_partition_i64(self.handle, _ptr(keys), _ptr(payload), keys.numel(), shift, bits,
+                                              _ptr(ok), _ptr(op), _ptr(off), self._s(stream)))
+        return ok, op, off
+
     # ----------------------------------------------------------------- sort
     def sort_by_key(self, cols, key_col: int, descending=False, stream=None):
         """-> the columns with rows ordered by cols[key_col] (stable)."""

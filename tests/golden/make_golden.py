@@ -163,11 +163,44 @@ def rjstepwise_cases():
     }
 
 
+def partition_ht_agg_cases():
+    """The reference's int64-key partitionHT (radix-aggr.cpp) on seeded keys."""
+    from oracle import oracle as O
+    from proteus_gb300 import abi
+
+    O.build()
+    if not O.build_ref(REF):
+        raise SystemExit("reference tree not found; cannot build oracle/_ref")
+    lib = abi.load()
+    cases = []
+    for seed, n, span in ((21, 1 << 12, 1 << 40), (22, 1 << 16, 1 << 62), (23, 50001, 1 << 20),
+                          (24, 1 << 17, 1 << 63)):
+        keys = np.array([int(lib.gbj_gen_rand(seed, 0x6A00, i)) % span for i in range(n)], dtype=np.uint64)
+        keys = keys.view(np.int64) - (np.int64(span // 2) if span < (1 << 63) else 0)
+        counts, ok, orows = O.ref_partition_ht_agg(keys)
+        cases.append({
+            "seed": seed, "n": n, "span": str(span),
+            "keys_sha": hashlib.sha256(keys.tobytes()).hexdigest()[:16],
+            "counts_sha": hashlib.sha256(counts.astype(np.int32).tobytes()).hexdigest()[:16],
+            "clustered_rows_sha": hashlib.sha256(orows.astype(np.int64).tobytes()).hexdigest()[:16],
+            "nonempty": int((counts > 0).sum()),
+        })
+    return {
+        "about": "partitionHT of the reference's int64-key aggregation twin "
+                 "(core/platform/lib/util/radix/aggregations/radix-aggr.cpp), compiled from source by "
+                 "oracle/Makefile (target ref); keys = gbj_gen_rand(seed, 0x6A00, i) mod span, shifted "
+                 "to be signed; row ids in clustered order pin the stable two-pass order.",
+        "cases": cases,
+    }
+
+
 def main():
     with open(os.path.join(OUT, "reference_cases.json"), "w") as f:
         json.dump(reference_cases(), f, indent=1)
     with open(os.path.join(OUT, "rjstepwise_cases.json"), "w") as f:
         json.dump(rjstepwise_cases(), f, indent=1)
+    with open(os.path.join(OUT, "partition_ht_agg_cases.json"), "w") as f:
+        json.dump(partition_ht_agg_cases(), f, indent=1)
     print("wrote", OUT)
 
 
