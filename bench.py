@@ -566,17 +566,23 @@ class Serve:
         lib = abi.load()
         return [int(lib.gbj_gen_rand(SEED, 0x6000 + salt, i)) % self.nt for i in range(n)]
 
-    def _closed(self, srv, n, salt):
+    def _submit(self, srv, t, out, tables):
+        """Template t's query; with `tables`, against its resident build table."""
+        if tables:
+            _, _, pk, pv = self.dev[t]
+            return srv.submit(None, None, pk, pv, self.shapes[t].cardinality, out, table=tables[t])
+        return srv.submit(*self.dev[t], self.shapes[t].cardinality, out)
+
+    def _closed(self, srv, n, salt, tables=None):
         order = self._order(n, salt)
         t0 = time.perf_counter()
-        tickets = [srv.submit(*self.dev[t], self.shapes[t].cardinality, self.ring_outs[i % self.ring])
-                   for i, t in enumerate(order)]
+        tickets = [self._submit(srv, t, self.ring_outs[i % self.ring], tables) for i, t in enumerate(order)]
         srv.drain()
         dt = time.perf_counter() - t0
         bad = sum(srv.wait(tk) != 0 for tk in tickets)
         return n / dt, bad
 
-    def _open(self, srv, rate, n, salt):
+    def _open(self, srv, rate, n, salt, tables=None):
         from proteus_gb300 import serve
 
         order = self._order(n, salt)
@@ -586,8 +592,7 @@ class Serve:
         for i, t in enumerate(order):
             while time.perf_counter() - t0 < arr[i]:
                 pass
-            tickets.append(srv.submit(*self.dev[t], self.shapes[t].cardinality,
-                                      self.ring_outs[i % self.ring]))
+            tickets.append(self._submit(srv, t, self.ring_outs[i % self.ring], tables))
         srv.drain()
         lat, first, last = [], None, None
         for tk in tickets:
@@ -611,10 +616,10 @@ class Serve:
     SLOS_MS = (5.0, 10.0, 20.0, 50.0)
     HEADLINE_SLO_MS = 10.0
 
-    def _sweep(self, srv, cap, salt):
+    def _sweep(self, srv, cap, salt, tables=None):
         runs = []
         for k, frac in enumerate((0.3, 0.5, 0.7, 0.85, 0.95)):
-            runs.append(self._open(srv, frac * cap, self.n_open, salt + k))
+            runs.append(self._open(srv, frac * cap, self.n_open, salt + k, tables))
         return runs
 
     @staticmethod
@@ -639,28 +644,49 @@ class Serve:
         p_runs = self._sweep(plain, plain_cap, 10)
         plain.close()
 
-        batched = serve.Server(ctx, max_batch=64, max_inflight=4, use_graph=True, large_slots=2,
-                               small_rows=1 << 22)
+        def batched_server():
+            return serve.Server(ctx, max_batch=64, max_inflight=4, use_graph=True, large_slots=2,
+                                small_rows=1 << 22)
+
+        batched = batched_server()
         self._closed(batched, 256, 4)
         bat_cap, bad_b = self._closed(batched, 1536, 5)
         b_runs = self._sweep(batched, bat_cap, 20)
         st = batched.stats()
         batched.close()
-        slo = {f"p99<={s:g}ms": {"plain_qps": self._best(p_runs, s), "batched_qps": self._best(b_runs, s)}
+        # batched, every template's build relation registered once as a
+        # resident table: queries only probe and group
+        resident = batched_server()
+        tables = [resident.register_table(bk, bg, self.shapes[t].cardinality)
+                  for t, (bk, bg, _, _) in enumerate(self.dev)]
+        table_bytes = resident.stats()["peak_bytes"]
+        self._closed(resident, 256, 6, tables)
+        res_cap, bad_r = self._closed(resident, 1536, 7, tables)
+        r_runs = self._sweep(resident, res_cap, 30, tables)
+        st_r = resident.stats()
+        resident.close()
+        slo = {f"p99<={s:g}ms": {"plain_qps": self._best(p_runs, s), "batched_qps": self._best(b_runs, s),
+                                 "batched_resident_qps": self._best(r_runs, s)}
                for s in self.SLOS_MS}
         for v in slo.values():
             v["ratio"] = round(v["batched_qps"] / v["plain_qps"], 2) if v["plain_qps"] else None
+            v["resident_ratio"] = round(v["batched_resident_qps"] / v["plain_qps"], 2) if v["plain_qps"] else None
         head = slo[f"p99<={self.HEADLINE_SLO_MS:g}ms"]
         return head["batched_qps"], {
             "slo_ms": self.HEADLINE_SLO_MS,
             "plain": {"capacity_qps": round(plain_cap, 1), "sweep": p_runs},
             "batched": {"capacity_qps": round(bat_cap, 1), "sweep": b_runs,
                         "batches": st["batches"], "peak_pool_bytes": st["peak_bytes"]},
+            "batched_resident_tables": {"capacity_qps": round(res_cap, 1), "sweep": r_runs,
+                                        "batches": st_r["batches"], "table_bytes": table_bytes,
+                                        "peak_pool_bytes": st_r["peak_bytes"]},
             "throughput_at_p99_slo": slo,
             "batched_over_plain_at_equal_p99": head["ratio"],
+            "batched_resident_over_plain_at_equal_p99": head["resident_ratio"],
             "batched_over_plain_capacity": round(bat_cap / plain_cap, 2),
-            "closed_loop_errors": bad_p + bad_b,
-            "mismatch_vs_alone": sum(r["mismatch_vs_alone"] for r in p_runs + b_runs),
+            "batched_resident_over_plain_capacity": round(res_cap / plain_cap, 2),
+            "closed_loop_errors": bad_p + bad_b + bad_r,
+            "mismatch_vs_alone": sum(r["mismatch_vs_alone"] for r in p_runs + b_runs + r_runs),
         }
 
     def cpu(self, threads, sample_log):

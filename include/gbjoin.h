@@ -428,6 +428,10 @@ typedef struct gbj_serve_query {
   int64_t *out_sum;
   uint64_t *out_n_groups;
   uint64_t out_capacity;
+  uint64_t table_id;             /* 0: build from d_build_keys/d_build_group
+                                    per query; else a table registered with
+                                    gbj_server_register_table (the build
+                                    columns and n_build are then ignored) */
 } gbj_serve_query;
 
 typedef struct gbj_server_params {
@@ -471,6 +475,18 @@ int gbj_server_stats(gbj_server *srv, uint64_t *completed, uint64_t *batches,
                      uint64_t *peak_bytes);
 /* Drains, stops the request loop and frees the server. */
 int gbj_server_destroy(gbj_server *srv);
+/* Builds the join table and group-key map of one build relation once and
+ * keeps it resident in the pool, counted against the HBM budget, until
+ * unregistered.  Queries that set table_id to *table_id skip the clear and
+ * build phases and reset only their own group counters.  Builds
+ * synchronously on the context's stream; the build columns may be freed on
+ * return.  GBJ_ERR_BUDGET if it does not fit the budget. */
+int gbj_server_register_table(gbj_server *srv, const int32_t *d_build_keys,
+                              const int32_t *d_build_group, uint64_t n_build,
+                              uint64_t expected_groups, uint64_t *table_id);
+/* Drains the server, then frees the table.  No query naming it may be
+ * submitted while this runs. */
+int gbj_server_unregister_table(gbj_server *srv, uint64_t table_id);
 
 /* -------------------------------------------------------------- autotuner */
 /* Times candidate plans on the caller's inputs (one warm-up run, then the

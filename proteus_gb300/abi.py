@@ -73,7 +73,8 @@ class ServeQuery(C.Structure):
     _fields_ = [("d_build_keys", C.c_void_p), ("d_build_group", C.c_void_p), ("n_build", C.c_uint64),
                 ("d_probe_keys", C.c_void_p), ("d_probe_vals", C.c_void_p), ("n_probe", C.c_uint64),
                 ("expected_groups", C.c_uint64), ("out_group", C.c_void_p), ("out_count", C.c_void_p),
-                ("out_sum", C.c_void_p), ("out_n_groups", C.c_void_p), ("out_capacity", C.c_uint64)]
+                ("out_sum", C.c_void_p), ("out_n_groups", C.c_void_p), ("out_capacity", C.c_uint64),
+                ("table_id", C.c_uint64)]
 
 
 class ServerParams(C.Structure):
@@ -127,6 +128,8 @@ SIGNATURES = {
     "gbj_server_drain": (C.c_int, [vp]),
     "gbj_server_stats": (C.c_int, [vp, P(u64), P(u64), P(u64)]),
     "gbj_server_destroy": (C.c_int, [vp]),
+    "gbj_server_register_table": (C.c_int, [vp, vp, vp, u64, u64, P(u64)]),
+    "gbj_server_unregister_table": (C.c_int, [vp, u64]),
     "gbj_autotune_radix_join": (C.c_int, [vp, vp, vp, u64, vp, vp, u64, P(Agg), i32, P(i32), P(dbl), vp]),
     "gbj_autotune_join": (C.c_int, [vp, vp, vp, u64, vp, vp, u64, P(Agg), i32, P(i32), P(dbl), vp]),
     "gbj_autotune_groupby": (C.c_int, [vp, vp, vp, u64, u64, P(i32), P(i32), P(dbl), vp]),

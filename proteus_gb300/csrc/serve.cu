@@ -35,6 +35,7 @@
 #include <condition_variable>
 #include <cstring>
 #include <deque>
+#include <map>
 #include <thread>
 #include <vector>
 
@@ -56,6 +57,8 @@ constexpr int kProbeThreads = 512;
 constexpr int kL1 = 2048;  // shared-memory group slots per probe CTA
 constexpr uint32_t kFlip = 0x80000000u;
 constexpr unsigned long long kEmptySlot = 0x80000000ull;  // key half INT32_MIN, group 0
+// clear phase: join table, group keys, per-query group counters
+enum : int32_t { kClearTable = 1, kClearKeys = 2, kClearCounts = 4 };
 
 enum { kPhClear = 0, kPhBuild = 1, kPhProbe = 2, kPhEmit = 3, kPhases = 4 };
 
@@ -66,7 +69,9 @@ struct SQ {
   unsigned long long *table;
   uint64_t tmask;  // join table slots - 1
   int32_t *side;   // groups of build rows whose key is INT32_MIN
+  unsigned long long *side_n;  // its length (per batch slot, or kept with a resident table)
   int32_t use_l1;  // pre-aggregate in shared memory
+  int32_t clear_mode;  // kClear* bits: what the clear phase resets
   uint32_t *gkey;  // group table: key' (0 empty); slot gmask + 1 = INT32_MIN
   unsigned long long *gcnt, *gsum;
   uint64_t gmask;
@@ -136,9 +141,11 @@ __global__ void __launch_bounds__(kThreads) k_serve_clear(const SBatch *__restri
       const uint64_t lo = (local - q.clear_t_items) * q.chunk[kPhClear];
       const uint64_t hi = min(lo + q.chunk[kPhClear], q.gmask + 2);
       for (uint64_t i = lo + threadIdx.x; i < hi; i += blockDim.x) {
-        q.gkey[i] = 0u;
-        q.gcnt[i] = 0ull;
-        q.gsum[i] = 0ull;
+        if (q.clear_mode & kClearKeys) q.gkey[i] = 0u;
+        if (q.clear_mode & kClearCounts) {
+          q.gcnt[i] = 0ull;
+          q.gsum[i] = 0ull;
+        }
       }
     }
   }
@@ -207,7 +214,7 @@ __global__ void __launch_bounds__(kThreads) k_serve_build(const SBatch *__restri
         continue;
       }
       if (k == INT32_MIN) {
-        q.side[atomicAdd(&slot->side_n[qi], 1ull)] = (int32_t)gs;
+        q.side[atomicAdd(q.side_n, 1ull)] = (int32_t)gs;
         continue;
       }
       const unsigned long long e = (unsigned long long)(uint32_t)k | ((unsigned long long)gs << 32);
@@ -246,7 +253,7 @@ __global__ void __launch_bounds__(kProbeThreads) k_serve_probe(const SBatch *__r
     const SQ q = d->q[qi];  // by value: registers, not reloads after atomics
     const uint64_t lo = (it - q.item0[kPhProbe]) * q.chunk[kPhProbe], hi = min(lo + q.chunk[kPhProbe], q.np);
     const bool use_l1 = q.use_l1 != 0;
-    const unsigned long long side_n = slot->side_n[qi];
+    const unsigned long long side_n = *q.side_n;
     auto add = [&](uint32_t gs, int32_t v) {
       if (use_l1) {
         atomicAdd(&l1_cnt[gs], 1u);
@@ -363,8 +370,23 @@ struct Slot {
 
 }  // namespace
 
+// A registered build relation's join table, kept resident in the pool: the
+// table, its group-key map (group slots) and the INT32_MIN side list.
+struct ResTable {
+  void *mem = nullptr;
+  uint64_t bytes = 0;
+  unsigned long long *table = nullptr;
+  uint64_t tmask = 0;
+  uint32_t *gkey = nullptr;
+  uint64_t gmask = 0;
+  int32_t *side = nullptr;
+  unsigned long long *side_n = nullptr;
+};
+
 struct gbj_server {
   gbj_ctx *ctx = nullptr;
+  std::map<uint64_t, ResTable> tables;
+  uint64_t next_table = 1;
   gbj_server_params prm{};
   uint64_t budget = 0;
   std::mutex mu;
@@ -391,10 +413,30 @@ uint64_t group_slots(const gbj_serve_query &q) {
   uint64_t e = q.expected_groups ? q.expected_groups : std::min<uint64_t>(std::max<uint64_t>(q.n_build, 1), 1u << 20);
   return next_pow2(std::max<uint64_t>(2 * e, 64));
 }
-// Pool bytes of one query: join table + group table (+ its INT32_MIN slot).
-uint64_t query_bytes(const gbj_serve_query &q) {
+// Pool bytes of one query: join table + group table (+ its INT32_MIN slot)
+// + side list; with a resident table only the group counters.
+uint64_t query_bytes(const gbj_server *sv, const gbj_serve_query &q) {
+  if (q.table_id) {
+    const ResTable &t = sv->tables.at(q.table_id);
+    return (t.gmask + 2) * 16 + 256;
+  }
   const uint64_t gs = group_slots(q) + 1;
   return table_slots(q.n_build) * 8 + gs * (8 + 8 + 4) + q.n_build * 4 + 512;
+}
+
+// Work items of one query (clear, build, probe, emit) from its layout.
+void size_items(gbj_ctx *ctx, SQ &q, uint64_t ts, uint64_t gs, uint64_t n_items[kPhases]) {
+  const uint64_t clear_t = (q.clear_mode & kClearTable) ? ts : 0;
+  const uint64_t work[kPhases] = {clear_t + gs + 1, q.nb, q.np, gs + 1};
+  const uint64_t per = 8 * (uint64_t)ctx->sm_count;
+  for (int ph = 0; ph < kPhases; ++ph)
+    q.chunk[ph] = std::min(kChunkMax[ph], std::max(kChunkMin[ph], next_pow2((work[ph] + per - 1) / per)));
+  auto div_up = [](uint64_t a, uint64_t b) { return (a + b - 1) / b; };
+  q.clear_t_items = div_up(clear_t, q.chunk[kPhClear]);
+  n_items[kPhClear] = q.clear_t_items + div_up(gs + 1, q.chunk[kPhClear]);
+  n_items[kPhBuild] = div_up(q.nb, q.chunk[kPhBuild]);
+  n_items[kPhProbe] = div_up(q.np, q.chunk[kPhProbe]);
+  n_items[kPhEmit] = div_up(gs + 1, q.chunk[kPhEmit]);
 }
 
 int launched(gbj_ctx *ctx, const char *name, bool count) {
@@ -493,19 +535,37 @@ bool launch_batch(gbj_server *sv, Slot &sl) {
     QueryRec &r = sv->recs[take[i] - 1];
     const gbj_serve_query &u = r.q;
     SQ &q = b->q[i];
-    const uint64_t ts = table_slots(u.n_build), gs = group_slots(u);
     char *p = static_cast<char *>(r.mem);
-    q.table = reinterpret_cast<unsigned long long *>(p);
-    q.gcnt = reinterpret_cast<unsigned long long *>(p + ts * 8);
-    q.gsum = q.gcnt + (gs + 1);
-    q.gkey = reinterpret_cast<uint32_t *>(q.gsum + (gs + 1));
-    q.side = reinterpret_cast<int32_t *>(q.gkey + (gs + 1));
+    uint64_t ts = 0, gs = 0;
+    if (u.table_id) {  // resident table: only this query's group counters are fresh
+      const ResTable &t = sv->tables.at(u.table_id);
+      ts = t.tmask + 1;
+      gs = t.gmask + 1;
+      q.table = t.table;
+      q.gkey = t.gkey;
+      q.side = t.side;
+      q.side_n = t.side_n;
+      q.gcnt = reinterpret_cast<unsigned long long *>(p);
+      q.gsum = q.gcnt + (gs + 1);
+      q.nb = 0;
+      q.clear_mode = kClearCounts;
+    } else {
+      ts = table_slots(u.n_build);
+      gs = group_slots(u);
+      q.table = reinterpret_cast<unsigned long long *>(p);
+      q.gcnt = reinterpret_cast<unsigned long long *>(p + ts * 8);
+      q.gsum = q.gcnt + (gs + 1);
+      q.gkey = reinterpret_cast<uint32_t *>(q.gsum + (gs + 1));
+      q.side = reinterpret_cast<int32_t *>(q.gkey + (gs + 1));
+      q.side_n = &sl.d_slot->side_n[i];
+      q.nb = u.n_build;
+      q.clear_mode = kClearTable | kClearKeys | kClearCounts;
+    }
     q.use_l1 = gs + 1 <= (uint64_t)kL1 ? 1 : 0;
     q.tmask = ts - 1;
     q.gmask = gs - 1;
     q.bk = u.d_build_keys;
     q.bg = u.d_build_group;
-    q.nb = u.n_build;
     q.pk = u.d_probe_keys;
     q.pv = u.d_probe_vals;
     q.np = u.n_probe;
@@ -514,16 +574,8 @@ bool launch_batch(gbj_server *sv, Slot &sl) {
     q.out_s = u.out_sum;
     q.out_n = u.out_n_groups;
     q.out_cap = u.out_capacity;
-    const uint64_t work[kPhases] = {ts + gs + 1, u.n_build, u.n_probe, gs + 1};
-    const uint64_t per = 8 * (uint64_t)ctx->sm_count;
-    for (int ph = 0; ph < kPhases; ++ph)
-      q.chunk[ph] = std::min(kChunkMax[ph], std::max(kChunkMin[ph], next_pow2((work[ph] + per - 1) / per)));
-    auto div_up = [](uint64_t a, uint64_t b) { return (a + b - 1) / b; };
-    q.clear_t_items = div_up(ts, q.chunk[kPhClear]);
-    const uint64_t n_items[kPhases] = {q.clear_t_items + div_up(gs + 1, q.chunk[kPhClear]),
-                                       div_up(u.n_build, q.chunk[kPhBuild]),
-                                       div_up(u.n_probe, q.chunk[kPhProbe]),
-                                       div_up(gs + 1, q.chunk[kPhEmit])};
+    uint64_t n_items[kPhases];
+    size_items(ctx, q, ts, gs, n_items);
     for (int ph = 0; ph < kPhases; ++ph) {
       q.item0[ph] = items[ph];
       items[ph] += n_items[ph];
@@ -703,7 +755,7 @@ extern "C" int gbj_server_create(gbj_ctx *ctx, const gbj_server_params *params, 
 
 namespace {
 int check_query(gbj_ctx *ctx, const gbj_serve_query *q) {
-  if ((q->n_build && (!q->d_build_keys || !q->d_build_group)) ||
+  if ((!q->table_id && q->n_build && (!q->d_build_keys || !q->d_build_group)) ||
       (q->n_probe && (!q->d_probe_keys || !q->d_probe_vals)))
     return set_error(ctx, GBJ_ERR_INVALID, "server: null input column");
   if (!q->out_group || !q->out_count || !q->out_sum || !q->out_n_groups || q->out_capacity == 0)
@@ -717,11 +769,12 @@ int check_query(gbj_ctx *ctx, const gbj_serve_query *q) {
 uint64_t enqueue_query(gbj_server *sv, const gbj_serve_query *q, double t) {
   QueryRec r;
   r.q = *q;
-  r.bytes = query_bytes(*q);
+  r.bytes = query_bytes(sv, *q);
   r.t_sub = t;
   sv->recs.push_back(r);
   const uint64_t ticket = sv->recs.size();
-  const bool large = sv->prm.large_slots > 0 && q->n_build + q->n_probe > sv->prm.small_rows;
+  const uint64_t build_rows = q->table_id ? 0 : q->n_build;
+  const bool large = sv->prm.large_slots > 0 && build_rows + q->n_probe > sv->prm.small_rows;
   sv->queue[large ? 1 : 0].push_back(ticket);
   return ticket;
 }
@@ -737,6 +790,9 @@ extern "C" int gbj_server_submit_batch(gbj_server *sv, const gbj_serve_query *qs
   for (uint64_t i = 0; i < n; ++i) GBJ_TRY(check_query(sv->ctx, &qs[i]));
   std::lock_guard<std::mutex> lk(sv->mu);
   if (sv->stop) return set_error(sv->ctx, GBJ_ERR_CANCELLED, "server: stopping");
+  for (uint64_t i = 0; i < n; ++i)
+    if (qs[i].table_id && !sv->tables.count(qs[i].table_id))
+      return set_error(sv->ctx, GBJ_ERR_INVALID, "server: unknown table_id");
   const double t = sv->now();
   for (uint64_t i = 0; i < n; ++i) tickets[i] = enqueue_query(sv, &qs[i], t);
   sv->cv_work.notify_one();
@@ -797,5 +853,102 @@ extern "C" int gbj_server_destroy(gbj_server *sv) {
   for (int i = 0; i < sv->nslots; ++i) cudaStreamSynchronize(sv->slots[i].stream);
   free_slots(sv);
   delete sv;
+  return GBJ_OK;
+}
+
+extern "C" int gbj_server_register_table(gbj_server *sv, const int32_t *d_build_keys,
+                                         const int32_t *d_build_group, uint64_t n_build,
+                                         uint64_t expected_groups, uint64_t *table_id) {
+  if (!sv || !table_id) return GBJ_ERR_INVALID;
+  gbj_ctx *ctx = sv->ctx;
+  if (n_build && (!d_build_keys || !d_build_group))
+    return set_error(ctx, GBJ_ERR_INVALID, "server: null build column");
+  if (n_build >= (1ull << 31)) return set_error(ctx, GBJ_ERR_INVALID, "server: n_build must be < 2^31");
+  gbj_serve_query tmp{};
+  tmp.n_build = n_build;
+  tmp.expected_groups = expected_groups;
+  const uint64_t ts = table_slots(n_build), gs = group_slots(tmp);
+  const uint64_t bytes = ts * 8 + 64 + (gs + 1) * 4 + n_build * 4 + 64;
+  std::lock_guard<std::mutex> lk(sv->mu);
+  if (sv->held + bytes > sv->budget) return set_error(ctx, GBJ_ERR_BUDGET, "server: table does not fit the budget");
+  cudaStream_t s = ctx->stream;
+  ResTable t;
+  GBJ_TRY(pool_alloc(ctx, bytes, s, &t.mem));
+  char *p = static_cast<char *>(t.mem);
+  t.bytes = bytes;
+  t.table = reinterpret_cast<unsigned long long *>(p);
+  t.side_n = reinterpret_cast<unsigned long long *>(p + ts * 8);
+  t.gkey = reinterpret_cast<uint32_t *>(p + ts * 8 + 64);
+  t.side = reinterpret_cast<int32_t *>(t.gkey + (gs + 1));
+  t.tmask = ts - 1;
+  t.gmask = gs - 1;
+  // build with the batch kernels: one query, clear (table + keys) and build
+  SBatch *h = new SBatch();
+  std::memset(h, 0, sizeof(SBatch));
+  h->nq = 1;
+  SQ &q = h->q[0];
+  q.table = t.table;
+  q.tmask = t.tmask;
+  q.gkey = t.gkey;
+  q.gmask = t.gmask;
+  q.side = t.side;
+  q.side_n = t.side_n;
+  q.bk = d_build_keys;
+  q.bg = d_build_group;
+  q.nb = n_build;
+  q.use_l1 = gs + 1 <= (uint64_t)kL1 ? 1 : 0;
+  q.clear_mode = kClearTable | kClearKeys;
+  uint64_t n_items[kPhases];
+  size_items(ctx, q, ts, gs, n_items);
+  h->items[kPhClear] = n_items[kPhClear];
+  h->items[kPhBuild] = n_items[kPhBuild];
+  SBatch *d_desc = nullptr;
+  SlotDev *d_slot = nullptr;
+  int rc = pool_alloc(ctx, sizeof(SBatch), s, reinterpret_cast<void **>(&d_desc));
+  if (rc == GBJ_OK) rc = pool_alloc(ctx, sizeof(SlotDev), s, reinterpret_cast<void **>(&d_slot));
+  uint32_t status = 0;
+  if (rc == GBJ_OK) {
+    cudaMemcpyAsync(d_desc, h, sizeof(SBatch), cudaMemcpyHostToDevice, s);
+    cudaMemsetAsync(d_slot, 0, sizeof(SlotDev), s);
+    cudaMemsetAsync(t.side_n, 0, sizeof(unsigned long long), s);
+    auto g = [&](int ph) {
+      return (int)std::max<uint64_t>(1, std::min<uint64_t>(n_items[ph], (uint64_t)sv->grid[ph]));
+    };
+    k_serve_clear<<<g(kPhClear), kThreads, 0, s>>>(d_desc, d_slot);
+    rc = launched(ctx, "k_serve_clear", true);
+    if (rc == GBJ_OK) {
+      k_serve_build<<<g(kPhBuild), kThreads, 0, s>>>(d_desc, d_slot);
+      rc = launched(ctx, "k_serve_build", true);
+    }
+    if (rc == GBJ_OK) {
+      const cudaError_t e = cudaMemcpyAsync(&status, d_slot->status, sizeof(uint32_t), cudaMemcpyDeviceToHost, s);
+      const cudaError_t e2 = cudaStreamSynchronize(s);
+      if (e != cudaSuccess || e2 != cudaSuccess) rc = cuda_error(ctx, e != cudaSuccess ? e : e2, "server: build");
+    }
+  }
+  delete h;
+  if (d_desc) pool_release(ctx, d_desc, s);
+  if (d_slot) pool_release(ctx, d_slot, s);
+  if (rc == GBJ_OK && status) rc = set_error(ctx, GBJ_ERR_CAPACITY, "server: table build overflowed");
+  if (rc != GBJ_OK) {
+    pool_release(ctx, t.mem, s);
+    return rc;
+  }
+  *table_id = sv->next_table++;
+  sv->tables[*table_id] = t;
+  sv->held += bytes;
+  sv->peak = std::max(sv->peak, sv->held);
+  return GBJ_OK;
+}
+
+extern "C" int gbj_server_unregister_table(gbj_server *sv, uint64_t table_id) {
+  if (!sv) return GBJ_ERR_INVALID;
+  gbj_server_drain(sv);  // no query may still read it
+  std::lock_guard<std::mutex> lk(sv->mu);
+  auto it = sv->tables.find(table_id);
+  if (it == sv->tables.end()) return set_error(sv->ctx, GBJ_ERR_INVALID, "server: unknown table_id");
+  pool_release(sv->ctx, it->second.mem, sv->ctx->stream);
+  sv->held -= it->second.bytes;
+  sv->tables.erase(it);
   return GBJ_OK;
 }

@@ -113,20 +113,33 @@ class Server:
         return cls(ctx, hbm_budget, max_batch=1, max_inflight=1, use_graph=False)
 
     @staticmethod
-    def _query(bk, bg, pk, pv, expected_groups, out):
-        return abi.ServeQuery(bk.data_ptr(), bg.data_ptr(), bk.numel(), pk.data_ptr(), pv.data_ptr(),
+    def _query(bk, bg, pk, pv, expected_groups, out, table=0):
+        """bk/bg: build columns, or None with `table` a registered table id."""
+        return abi.ServeQuery(bk.data_ptr() if bk is not None else None,
+                              bg.data_ptr() if bg is not None else None,
+                              bk.numel() if bk is not None else 0, pk.data_ptr(), pv.data_ptr(),
                               pk.numel(), expected_groups, out.group.data_ptr(), out.count.data_ptr(),
-                              out.sum.data_ptr(), out.n.data_ptr(), out.capacity)
+                              out.sum.data_ptr(), out.n.data_ptr(), out.capacity, table)
 
-    def submit(self, bk, bg, pk, pv, expected_groups: int, out: Output) -> int:
-        q = self._query(bk, bg, pk, pv, expected_groups, out)
+    def register_table(self, bk, bg, expected_groups: int = 0) -> int:
+        """Builds (bk, bg)'s join table once, resident in the pool; returns its id."""
+        t = C.c_uint64()
+        self.ctx.check(self.ctx.lib.gbj_server_register_table(self.handle, bk.data_ptr(), bg.data_ptr(),
+                                                              bk.numel(), expected_groups, C.byref(t)))
+        return t.value
+
+    def unregister_table(self, table_id: int):
+        self.ctx.check(self.ctx.lib.gbj_server_unregister_table(self.handle, table_id))
+
+    def submit(self, bk, bg, pk, pv, expected_groups: int, out: Output, table: int = 0) -> int:
+        q = self._query(bk, bg, pk, pv, expected_groups, out, table)
         t = C.c_uint64()
         self.ctx.check(self.ctx.lib.gbj_server_submit(self.handle, C.byref(q), C.byref(t)))
         self._keep[t.value] = (bk, bg, pk, pv, out)
         return t.value
 
     def submit_many(self, queries) -> list:
-        """queries: [(bk, bg, pk, pv, expected_groups, out)], queued together."""
+        """queries: [(bk, bg, pk, pv, expected_groups, out[, table])], queued together."""
         arr = (abi.ServeQuery * len(queries))(*[self._query(*q) for q in queries])
         tk = (C.c_uint64 * len(queries))()
         self.ctx.check(self.ctx.lib.gbj_server_submit_batch(self.handle, arr, len(queries), tk))

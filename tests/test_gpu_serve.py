@@ -159,3 +159,69 @@ def test_serve_larger_queries(ctx, oracle):
         assert status[i] == abi.OK
         same(outs[i].sorted(), expected(oracle, host[i]))
     srv.close()
+
+
+@pytest.mark.parametrize("use_graph", [True, False])
+def test_serve_resident_tables(ctx, oracle, use_graph):
+    """Queries against registered (resident) build tables, mixed with queries
+    that build their own, give the oracle's results; the tables survive many
+    batches and several queries read one table in the same batch."""
+    import torch
+
+    rng = np.random.default_rng(11)
+    builds = []
+    for nb, card in [(5000, 40), (1 << 15, 3000), (300, 7)]:
+        bk = rng.integers(-nb, nb, nb).astype(np.int32)  # duplicates included
+        bg = rng.integers(-card, card, nb).astype(np.int32)
+        bk[::97] = np.iinfo(np.int32).min
+        bg[::31] = np.iinfo(np.int32).min
+        builds.append((bk, bg, 2 * card + 2))
+    srv = serve.Server(ctx, max_batch=16, max_inflight=3, use_graph=use_graph)
+    ids = [srv.register_table(dev(bk), dev(bg), eg) for bk, bg, eg in builds]
+    assert len(set(ids)) == 3 and 0 not in ids
+    held = srv.stats()["peak_bytes"]
+    assert held > 0
+    qs, exp = [], []
+    for r in range(4):  # rounds of queries, so every table serves many batches
+        for j in range(12):
+            b = j % 3
+            bk, bg, eg = builds[b]
+            npb = int(rng.integers(0, 40000))
+            pk = rng.integers(-len(bk) - 5, len(bk) + 5, npb).astype(np.int32)
+            pk[::13] = np.iinfo(np.int32).min
+            pv = rng.integers(-1000, 1000, npb).astype(np.int32)
+            resident = (j % 4) != 3
+            qs.append((b, resident, dev(bk), dev(bg), dev(pk) if npb else torch.empty(0, dtype=torch.int32,
+                       device="cuda"), dev(pv) if npb else torch.empty(0, dtype=torch.int32, device="cuda"), eg))
+            exp.append(expected(oracle, (bk, bg, pk, pv)))
+    outs = [serve.Output(q[6] + 8) for q in qs]
+    batch = [((None if q[1] else q[2]), (None if q[1] else q[3]), q[4], q[5], q[6], o, ids[q[0]] if q[1] else 0)
+             for q, o in zip(qs, outs)]
+    tickets = srv.submit_many(batch)
+    for t, o, e in zip(tickets, outs, exp):
+        assert srv.wait(t, timeout=120.0) == abi.OK
+        same(o.sorted(), e)
+    # one by one, after all the batches above
+    for i in (0, 1, 2):
+        o = serve.Output(qs[i][6] + 8)
+        t = srv.submit(None, None, qs[i][4], qs[i][5], qs[i][6], o, table=ids[qs[i][0]])
+        assert srv.wait(t, timeout=120.0) == abi.OK
+        same(o.sorted(), exp[i])
+    # unknown ids are refused; an unregistered table's id is unknown
+    with pytest.raises(abi.GbjError):
+        srv.submit(None, None, qs[0][4], qs[0][5], qs[0][6], serve.Output(8), table=12345)
+    srv.unregister_table(ids[2])
+    with pytest.raises(abi.GbjError):
+        srv.unregister_table(ids[2])
+    with pytest.raises(abi.GbjError):
+        srv.submit(None, None, qs[2][4], qs[2][5], qs[2][6], serve.Output(8), table=ids[2])
+    srv.close()
+
+
+def test_serve_resident_table_budget(ctx):
+    bk = dev(np.arange(1 << 16, dtype=np.int32))
+    srv = serve.Server(ctx, hbm_budget=1 << 16)
+    with pytest.raises(abi.GbjError) as e:
+        srv.register_table(bk, bk, 1 << 16)
+    assert e.value.code == abi.ERR_BUDGET
+    srv.close()
