@@ -7,13 +7,12 @@
 // next != self (hash-group-by-chained.cpp:638-853).
 //
 // GB300 design:
-//  * level 1 lives in shared memory: for at most 64 groups each warp keeps a
-//    private 128-slot table where count and biased sum share one 64-bit
-//    atomic per row (flushed to level 2 every 4096 rows of the warp, which
-//    bounds the packed fields); otherwise one table of up to 4096 slots per
-//    CTA with count and sum atomics.  Min and max atomics are issued only
-//    when the value improves the stored extreme, so they fade out as a
-//    group fills;
+//  * level 1 is one open-addressing table of up to 4096 slots per CTA in
+//    shared memory, updated with 32-bit atomics only (count, and the sum as
+//    two 16-bit halves of the biased value, which stay exact while a slot
+//    takes at most 65535 rows between flushes; hot slots move to level 2
+//    before that).  Min and max atomics are issued only when the value
+//    improves the stored extreme, so they fade out as a group fills;
 //  * level 2 is a global open-addressing table that receives level 1 when a
 //    CTA finishes (and rows that find level 1 full), with integer atomics,
 //    so the result is exact in any order;
@@ -38,11 +37,9 @@ namespace {
 
 constexpr int kThreads = 512;
 constexpr int kWarps = kThreads / 32;
-constexpr int kSlots = 4096;     // CTA level-1 table slots
-constexpr int kPrivSlots = 128;  // per-warp level-1 table slots (<= 64 groups)
+constexpr int kSlots = 4096;     // level-1 table slots per CTA (at most)
 constexpr int kProbeL1 = 32;     // level-1 probe limit before spilling to level 2
 constexpr uint32_t kFlip = 0x80000000u;
-constexpr uint64_t kPrivMaxGroups = 64;
 
 struct GTable {
   uint32_t *key;  // key' (0 = empty)
@@ -91,16 +88,6 @@ __device__ __forceinline__ void g_row(const GTable &g, int32_t key, uint64_t c, 
   g_update(g, slot, c, s, mn_enc, mx_enc);
 }
 
-// A level-1 table (CTA-shared or one warp's private table).
-struct L1 {
-  uint32_t *key;
-  uint32_t *cnt;
-  unsigned long long *sum;
-  uint32_t *mn, *mx;
-  uint32_t mask;   // slots - 1
-  uint32_t shift;  // 32 - log2(slots): the home slot is the hash's top bits
-};
-
 struct Out {
   int32_t *keys;
   int64_t *cnt, *sum;
@@ -122,181 +109,199 @@ __device__ __forceinline__ void emit(const Out &o, uint64_t pos, int32_t key, ui
   if (o.mx) o.mx[pos] = mx;
 }
 
-// Level-1 slot of key' kk (claimed with CAS when new), or -1 when the probe
-// limit is reached.  The home slot comes from the top bits of the hash: the
-// partitioning digit is its low bits, so within a partition those are equal.
-__device__ __forceinline__ int l1_slot(const L1 &t, int32_t k, uint32_t kk) {
-  uint32_t h = gbjd::fmix32((uint32_t)k) >> t.shift;
-  for (int step = 0; step < kProbeL1; ++step) {
-    uint32_t cur = t.key[h];
-    if (cur == 0) cur = atomicCAS(&t.key[h], 0u, kk);
-    if (cur == 0 || cur == kk) return (int)h;
-    h = (h + 1) & t.mask;
+// Level 1: one table per CTA in shared memory, updated with 32-bit atomics
+// only (64-bit shared atomics have no native form and cost a CAS loop).
+// A slot holds
+//   meta = {key', min', max', count}
+//   sums = {A, B}: with u = value + 2^31 (unsigned, < 2^32), A sums the low
+//          16 bits of u and B the high 16 bits, so
+//          SUM(value) = B * 2^16 + A - count * 2^31.
+// A, B and count stay exact while a slot takes at most 65535 rows between
+// flushes; the kernel tracks a CTA-wide bound on every slot's count and moves
+// slots above kHot rows to level 2 before the bound could pass 65535.
+struct L1 {
+  uint4 *meta;
+  uint2 *sums;
+  uint32_t mask;   // slots - 1
+  uint32_t shift;  // 32 - log2(slots): the home slot is the hash's top bits
+};
+
+constexpr uint32_t kChunk = 32768;        // rows per step between bound checks
+constexpr uint32_t kCountLimit = 65535;   // rows a slot may take between flushes
+constexpr uint32_t kHot = kCountLimit - kChunk;  // slots above go to level 2 at a check
+
+// Shared-memory accesses of the level-1 table, in the shared state space
+// explicitly (32-bit atomics only; a load of a slot may run ahead of an
+// earlier row's atomics: it only decides the claim path, which re-checks with
+// CAS, and whether a min/max atomic is worth issuing).
+__device__ __forceinline__ uint32_t s_addr(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+__device__ __forceinline__ uint4 s_ld4(uint32_t a) {
+  uint4 r;
+  asm("ld.shared.v4.u32 {%0, %1, %2, %3}, [%4];" : "=r"(r.x), "=r"(r.y), "=r"(r.z), "=r"(r.w) : "r"(a));
+  return r;
+}
+__device__ __forceinline__ uint32_t s_ld_volatile(uint32_t a) {
+  uint32_t r;
+  asm volatile("ld.volatile.shared.u32 %0, [%1];" : "=r"(r) : "r"(a) : "memory");
+  return r;
+}
+__device__ __forceinline__ void s_red_add(uint32_t a, uint32_t v) {
+  asm volatile("red.shared.add.u32 [%0], %1;" ::"r"(a), "r"(v) : "memory");
+}
+// red.max issued only when v is above the loaded hint (predicated, no branch).
+__device__ __forceinline__ void s_red_max_above(uint32_t a, uint32_t v, uint32_t hint) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\tsetp.gt.u32 p, %1, %2;\n\t@p red.shared.max.u32 [%0], %1;\n\t}" ::"r"(a),
+      "r"(v), "r"(hint)
+      : "memory");
+}
+__device__ __forceinline__ uint32_t s_cas(uint32_t a, uint32_t cmp, uint32_t v) {
+  uint32_t r;
+  asm volatile("atom.shared.cas.b32 %0, [%1], %2, %3;" : "=r"(r) : "r"(a), "r"(cmp), "r"(v) : "memory");
+  return r;
+}
+
+// Home slot: Fibonacci hashing, top bits.  Independent of the fmix32 low bits
+// that pick a key's partition, so it also spreads the keys of one partition.
+__device__ __forceinline__ uint32_t l1_home(const L1 &t, int32_t k) {
+  return ((uint32_t)k * 0x9E3779B1u) >> t.shift;
+}
+
+__device__ __forceinline__ int64_t l1_sum(uint2 ab, uint32_t c) {
+  return (int64_t)(((uint64_t)ab.y << 16) + ab.x) - (int64_t)c * (int64_t)kFlip;
+}
+
+// The slow path of a row whose key is not in its home slot: probes on,
+// claiming an empty slot with CAS.  Returns the slot, or -1 after sending
+// the row to level 2 (INT32_MIN keys, or no slot within kProbeL1 steps).
+__device__ __forceinline__ int l1_find(const L1 &t, const GTable &g, int32_t k, int32_t v, uint32_t h,
+                                    uint32_t *status) {
+  const uint32_t u = (uint32_t)v ^ kFlip;
+  if (k != INT32_MIN) {
+    const uint32_t kk = (uint32_t)k ^ kFlip;
+    const uint32_t base = s_addr(t.meta);
+    for (int step = 0; step < kProbeL1; ++step) {
+      const uint32_t a = base + h * (uint32_t)sizeof(uint4);
+      uint32_t cur = s_ld_volatile(a);
+      if (cur == 0) cur = s_cas(a, 0u, kk);
+      if (cur == 0 || cur == kk) return (int)h;
+      h = (h + 1) & t.mask;
+    }
   }
+  g_row(g, k, 1, v, ~u, u, status);
   return -1;
 }
 
-// Packed per-warp accumulator: count in bits [44, 64), sum of the biased
-// values (v + 2^31, each < 2^32) in bits [0, 44).  Exact while a slot sees at
-// most 4096 rows between flushes (4096 * 2^32 = 2^44), which the per-warp
-// flush every kPrivFlushRows rows guarantees.
-constexpr int kPackShift = 44;
-constexpr uint32_t kPrivFlushRows = 4096;
-constexpr int kMergeMin = 5;
-
-// Applies c rows of key k (sum s, extremes mn/mx) to a level-1 table.
-// kPrivate: the table belongs to this warp, count and biased sum travel in
-// one packed 64-bit atomic (in `sum`).  Otherwise: count and sum atomics.
-// Min and max use an atomic only when the value improves the stored extreme.
-template <bool kPrivate>
-__device__ __forceinline__ void l1_apply(const L1 &t, const GTable &g, int32_t k, uint32_t c,
-                                         int64_t s, int32_t mn, int32_t mx, bool &spill,
-                                         uint32_t *status) {
-  const uint32_t emn = enc_min(mn), emx = enc_max(mx);
-  if (k == INT32_MIN) {
-    g_row(g, k, c, s, emn, emx, status);
-    spill = true;
-    return;
-  }
-  const uint32_t kk = (uint32_t)k ^ kFlip;
-  const int slot = l1_slot(t, k, kk);
-  if (slot < 0) {
-    g_row(g, k, c, s, emn, emx, status);
-    spill = true;
-    return;
-  }
-  if (kPrivate) {
-    atomicAdd(&t.sum[slot], ((unsigned long long)c << kPackShift) +
-                                (unsigned long long)(s + (int64_t)c * (int64_t)kFlip));
-  } else {
-    atomicAdd(&t.cnt[slot], c);
-    atomicAdd(&t.sum[slot], (unsigned long long)s);
-  }
-  if (emn > t.mn[slot]) atomicMax(&t.mn[slot], emn);
-  if (emx > t.mx[slot]) atomicMax(&t.mx[slot], emx);
-}
-
-// One row per lane (ok = lane holds a row); called by the whole warp.  When
-// at least kMergeMin lanes share the key of the first active lane they are
-// merged first with warp reductions (the sum as signed high and unsigned low
-// 16-bit halves, exact in 32 bits for 32 lanes), so a hot key costs one set
-// of atomics per warp instead of one per row.  A second merge round runs
-// only when the first merged (skewed input); other inputs pay two ballots.
-// Below the threshold the duplicate atomics are cheaper than the merge.
-template <bool kPrivate>
-__device__ __forceinline__ void warp_rows(const L1 &t, const GTable &g, int32_t k, int32_t v,
-                                          bool ok, bool &spill, uint32_t *status) {
-  const int lane = threadIdx.x & 31;
-  unsigned act = __ballot_sync(0xffffffffu, ok);
-#pragma unroll
-  for (int round = 0; round < 2; ++round) {
-    if (!act) return;
-    const int lead = __ffs(act) - 1;
-    const int32_t k0 = __shfl_sync(0xffffffffu, k, lead);
-    const bool same = ok && k == k0;
-    const unsigned m = __ballot_sync(0xffffffffu, same);
-    if (__popc(m) < kMergeMin) break;
-    const uint32_t lo = __reduce_add_sync(0xffffffffu, same ? ((uint32_t)v & 0xffffu) : 0u);
-    const int32_t hi = (int32_t)__reduce_add_sync(0xffffffffu, same ? (uint32_t)(v >> 16) : 0u);
-    const int32_t mn = __reduce_min_sync(0xffffffffu, same ? v : INT32_MAX);
-    const int32_t mx = __reduce_max_sync(0xffffffffu, same ? v : INT32_MIN);
-    if (lane == lead)
-      l1_apply<kPrivate>(t, g, k0, (uint32_t)__popc(m), (int64_t)hi * 65536 + (int64_t)lo, mn, mx,
-                         spill, status);
-    ok = ok && !same;
-    act &= ~m;
-  }
-  if (ok) l1_apply<kPrivate>(t, g, k, 1u, v, v, v, spill, status);
-}
-
-// Moves one slot of a level-1 table to level 2 (packed or plain form).
-template <bool kPacked>
-__device__ __forceinline__ void slot_to_l2(const GTable &g, uint32_t key, uint32_t cnt,
-                                           unsigned long long sum, uint32_t mn, uint32_t mx,
-                                           uint32_t *status) {
-  uint64_t c = cnt;
-  int64_t s = (int64_t)sum;
-  if (kPacked) {
-    c = sum >> kPackShift;
-    s = (int64_t)(sum & ((1ull << kPackShift) - 1)) - (int64_t)c * (int64_t)kFlip;
-  }
-  if (c == 0) return;
-  const int32_t k = (int32_t)(key ^ kFlip);
-  g_update(g, g_slot(g, k, status), c, s, mn, mx);
-}
-
-// A warp flushes its private table to level 2 and resets the accumulators
-// (keys stay claimed).
-__device__ __forceinline__ void warp_flush(const L1 &t, const GTable &g, uint32_t *status) {
-  __syncwarp();
-  for (int i = threadIdx.x & 31; i <= (int)t.mask; i += 32) {
-    if (t.key[i] != 0) {
-      slot_to_l2<true>(g, t.key[i], 0, t.sum[i], t.mn[i], t.mx[i], status);
-      t.sum[i] = 0;
-      t.mn[i] = 0;
-      t.mx[i] = 0;
+// One row into level 1; rows that go to level 2 set `spill`.
+__device__ __forceinline__ void l1_row(const L1 &t, const GTable &g, int32_t k, int32_t v, bool &spill,
+                                       uint32_t *status) {
+  const uint32_t u = (uint32_t)v ^ kFlip;  // biased value = max' encoding; ~u = min'
+  uint32_t h = l1_home(t, k);
+  const uint32_t mb = s_addr(t.meta), sb = s_addr(t.sums);
+  uint4 m = s_ld4(mb + h * (uint32_t)sizeof(uint4));
+  // INT32_MIN's key' is 0 (the empty mark), so it always takes the slow path
+  if (m.x != ((uint32_t)k ^ kFlip) || k == INT32_MIN) {
+    const int f = l1_find(t, g, k, v, h, status);
+    if (f < 0) {
+      spill = true;
+      return;
     }
+    h = (uint32_t)f;
+    m = s_ld4(mb + h * (uint32_t)sizeof(uint4));
   }
-  __syncwarp();
+  const uint32_t ma = mb + h * (uint32_t)sizeof(uint4), sa = sb + h * (uint32_t)sizeof(uint2);
+  s_red_add(ma + 12, 1u);
+  s_red_add(sa, u & 0xffffu);
+  s_red_add(sa + 4, u >> 16);
+  s_red_max_above(ma + 4, ~u, m.y);
+  s_red_max_above(ma + 8, u, m.z);
+}
+
+// Moves one level-1 slot to level 2.
+__device__ __forceinline__ void slot_to_l2(const GTable &g, uint4 m, uint2 ab, uint32_t *status) {
+  if (m.w == 0) return;
+  const int32_t k = (int32_t)(m.x ^ kFlip);
+  g_update(g, g_slot(g, k, status), m.w, l1_sum(ab, m.w), m.y, m.z);
+}
+
+// Reads keys/values rows [i, i+4) with 16-byte loads.
+__device__ __forceinline__ void load4(const int32_t *__restrict__ keys, const int32_t *__restrict__ vals,
+                                      uint64_t i, int4 &k, int4 &v) {
+  k = __ldcs(reinterpret_cast<const int4 *>(keys + i));
+  v = __ldcs(reinterpret_cast<const int4 *>(vals + i));
 }
 
 // Aggregation kernel.  Work item i covers rows [item_lo(i), item_hi(i)) of
 // either the raw SoA input (items of w rows; level 1 persists across items
 // and is flushed to level 2 when the CTA finishes) or the partitioned AoS
 // pairs (one partition, or a w-row piece of one; level 1 is cleared per
-// item and a whole partition is emitted directly).
-template <bool kPrivate, bool kPairs>
+// item and a whole partition is emitted directly).  kVec: the raw columns
+// are 16-byte aligned and read 4 rows per thread per load.
+template <bool kPairs, bool kVec>
 __global__ void __launch_bounds__(kThreads)
     k_groupby(const int32_t *__restrict__ keys, const int32_t *__restrict__ vals,
               const int2 *__restrict__ pairs, uint64_t n, uint64_t w,
               const uint64_t *__restrict__ poff, const uint64_t *__restrict__ item_off, uint32_t P,
               uint32_t tslots, GTable g, Out o, unsigned long long *item_ctr, uint32_t *status) {
-  static_assert(!(kPrivate && kPairs), "private tables are for raw input");
   extern __shared__ __align__(16) unsigned char smem[];
   // shared-table size: a power of two <= kSlots chosen by the host from the
-  // expected groups per item; the arrays below are laid out for kSlots
-  const int kTab = kPrivate ? kPrivSlots * kWarps : (int)tslots;
-  constexpr int kLayout = kPrivate ? kPrivSlots * kWarps : kSlots;
-  unsigned long long *sum_all = reinterpret_cast<unsigned long long *>(smem);
-  uint32_t *key_all = reinterpret_cast<uint32_t *>(sum_all + kLayout);
-  uint32_t *cnt_all = key_all + kLayout;
-  uint32_t *mn_all = cnt_all + kLayout;
-  uint32_t *mx_all = mn_all + kLayout;
+  // expected groups per item
+  const int kTab = (int)tslots;
+  L1 t{reinterpret_cast<uint4 *>(smem), reinterpret_cast<uint2 *>(smem + (size_t)kTab * sizeof(uint4)),
+       tslots - 1, 32u - (uint32_t)__popc(tslots - 1)};
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  L1 t;
-  if (kPrivate) {
-    const int o0 = warp * kPrivSlots;
-    t = L1{key_all + o0, cnt_all + o0, sum_all + o0, mn_all + o0, mx_all + o0, kPrivSlots - 1,
-           32u - (uint32_t)__popc(kPrivSlots - 1)};
-  } else {
-    t = L1{key_all, cnt_all, sum_all, mn_all, mx_all, tslots - 1, 32u - (uint32_t)__popc(tslots - 1)};
-  }
   __shared__ unsigned long long s_item;
   __shared__ int s_spill;
   __shared__ uint32_t s_warp[kWarps];
   __shared__ unsigned long long s_base;
+  __shared__ uint32_t s_bound;  // >= every slot's count
   const uint64_t total_items = kPairs ? item_off[P] : (n + w - 1) / w;
 
   auto clear = [&]() {
     for (int i = threadIdx.x; i < kTab; i += kThreads) {
-      key_all[i] = 0;
-      cnt_all[i] = 0;
-      sum_all[i] = 0;
-      mn_all[i] = 0;
-      mx_all[i] = 0;
+      t.meta[i] = make_uint4(0, 0, 0, 0);
+      t.sums[i] = make_uint2(0, 0);
     }
+    if (threadIdx.x == 0) s_bound = 0;
   };
-  // level 1 -> level 2 (every occupied slot of the CTA's tables)
+  // level 1 -> level 2 (every occupied slot)
   auto flush = [&]() {
+    for (int i = threadIdx.x; i < kTab; i += kThreads) slot_to_l2(g, t.meta[i], t.sums[i], status);
+  };
+  // Before adding `rows` rows: if the bound could pass kCountLimit, move the
+  // hot slots to level 2 and recompute the bound.  Called by the whole CTA.
+  auto make_room = [&](uint32_t rows, bool &spill) {
+    if (s_bound + rows <= kCountLimit) {
+      __syncthreads();
+      if (threadIdx.x == 0) s_bound += rows;
+      return;
+    }
+    __syncthreads();
+    uint32_t mx = 0;
     for (int i = threadIdx.x; i < kTab; i += kThreads) {
-      if (key_all[i] != 0)
-        slot_to_l2<kPrivate>(g, key_all[i], cnt_all[i], sum_all[i], mn_all[i], mx_all[i], status);
+      const uint4 m = t.meta[i];
+      if (m.w > kHot) {
+        slot_to_l2(g, m, t.sums[i], status);
+        t.meta[i] = make_uint4(m.x, 0, 0, 0);
+        t.sums[i] = make_uint2(0, 0);
+        spill = true;
+      } else {
+        mx = max(mx, m.w);
+      }
+    }
+    mx = __reduce_max_sync(0xffffffffu, mx);
+    if (lane == 0) s_warp[warp] = mx;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      uint32_t b = 0;
+      for (int w2 = 0; w2 < kWarps; ++w2) b = max(b, s_warp[w2]);
+      s_bound = b + rows;
     }
   };
 
   clear();
-  uint32_t warp_rows_done = 0;  // rows this warp added since its last flush
   for (;;) {
+    __syncthreads();
     if (threadIdx.x == 0) {
       s_item = atomicAdd(item_ctr, 1ull);
       s_spill = 0;
@@ -321,38 +326,57 @@ __global__ void __launch_bounds__(kThreads)
       hi = lo + w < n ? lo + w : n;
     }
     bool spill = false;
-    // 4 rows per thread per round, loads issued together; whole warps run
-    // every round (a private table is flushed every kPrivFlushRows rows of
-    // its warp)
-    for (uint64_t base = lo; base < hi; base += 4 * kThreads) {
-      int32_t k[4], v[4];
-      bool ok[4];
-#pragma unroll
-      for (int u = 0; u < 4; ++u) {
-        const uint64_t i = base + threadIdx.x + (uint64_t)u * kThreads;
-        ok[u] = i < hi;
-        if (ok[u]) {
-          if (kPairs) {
-            const int2 pv = __ldcs(pairs + i);
-            k[u] = pv.x;
-            v[u] = pv.y;
+    for (uint64_t c0 = lo; c0 < hi; c0 += kChunk) {
+      const uint64_t c1 = c0 + kChunk < hi ? c0 + kChunk : hi;
+      make_room((uint32_t)(c1 - c0), spill);
+      __syncthreads();
+      if (!kPairs && kVec) {
+        // 4 rows per thread per step; the loads of the next two steps are
+        // in flight while this step's rows are applied
+        constexpr uint64_t kStep = 4 * kThreads;
+        uint64_t i = c0 + 4 * (uint64_t)threadIdx.x;
+        int4 ka = make_int4(0, 0, 0, 0), va = ka, kb = ka, vb = ka;
+        if (i + 4 <= c1) load4(keys, vals, i, ka, va);
+        if (i + kStep + 4 <= c1) load4(keys, vals, i + kStep, kb, vb);
+        for (; i < c1; i += kStep) {
+          const int4 kc = ka, vc = va;
+          ka = kb;
+          va = vb;
+          const bool full = i + 4 <= c1;
+          if (i + 2 * kStep + 4 <= c1) load4(keys, vals, i + 2 * kStep, kb, vb);
+          if (full) {
+            l1_row(t, g, kc.x, vc.x, spill, status);
+            l1_row(t, g, kc.y, vc.y, spill, status);
+            l1_row(t, g, kc.z, vc.z, spill, status);
+            l1_row(t, g, kc.w, vc.w, spill, status);
           } else {
-            k[u] = __ldcs(keys + i);
-            v[u] = __ldcs(vals + i);
+            for (uint64_t r = i; r < c1; ++r) l1_row(t, g, __ldcs(keys + r), __ldcs(vals + r), spill, status);
           }
-        } else {
-          k[u] = 0;
-          v[u] = 0;
         }
-      }
+      } else {
+        for (uint64_t base = c0; base < c1; base += 4 * kThreads) {
+          int32_t k[4], v[4];
+          bool ok[4];
 #pragma unroll
-      for (int u = 0; u < 4; ++u)
-        warp_rows<kPrivate>(t, g, k[u], v[u], ok[u], spill, status);
-      if (kPrivate) {
-        warp_rows_done += 4 * 32;
-        if (warp_rows_done >= kPrivFlushRows) {
-          warp_flush(t, g, status);
-          warp_rows_done = 0;
+          for (int u = 0; u < 4; ++u) {
+            const uint64_t i = base + threadIdx.x + (uint64_t)u * kThreads;
+            ok[u] = i < c1;
+            k[u] = 0;
+            v[u] = 0;
+            if (ok[u]) {
+              if (kPairs) {
+                const int2 pv = __ldcs(pairs + i);
+                k[u] = pv.x;
+                v[u] = pv.y;
+              } else {
+                k[u] = __ldcs(keys + i);
+                v[u] = __ldcs(vals + i);
+              }
+            }
+          }
+#pragma unroll
+          for (int u = 0; u < 4; ++u)
+            if (ok[u]) l1_row(t, g, k[u], v[u], spill, status);
         }
       }
     }
@@ -362,7 +386,7 @@ __global__ void __launch_bounds__(kThreads)
       if (whole && !s_spill) {
         // final groups of a whole partition: compact straight to the output
         uint32_t mine = 0;
-        for (int i = threadIdx.x; i < kTab; i += kThreads) mine += key_all[i] != 0;
+        for (int i = threadIdx.x; i < kTab; i += kThreads) mine += t.meta[i].w != 0;
         mine = __reduce_add_sync(0xffffffffu, mine);
         if (lane == 0) s_warp[warp] = mine;
         __syncthreads();
@@ -376,11 +400,12 @@ __global__ void __launch_bounds__(kThreads)
         for (int w2 = 0; w2 < warp; ++w2) pos += s_warp[w2];
         for (int i0 = warp * 32; i0 < kTab; i0 += kThreads) {
           const int i = i0 + lane;
-          const bool occ = key_all[i] != 0;
+          const uint4 m = i < kTab ? t.meta[i] : make_uint4(0, 0, 0, 0);
+          const bool occ = m.w != 0;
           const unsigned b = __ballot_sync(0xffffffffu, occ);
           if (occ)
-            emit(o, pos + __popc(b & ((1u << lane) - 1)), (int32_t)(key_all[i] ^ kFlip), cnt_all[i],
-                 (int64_t)sum_all[i], dec_min(mn_all[i]), dec_max(mx_all[i]), status);
+            emit(o, pos + __popc(b & ((1u << lane) - 1)), (int32_t)(m.x ^ kFlip), m.w, l1_sum(t.sums[i], m.w),
+                 dec_min(m.y), dec_max(m.z), status);
           pos += __popc(b);
         }
       } else {
@@ -389,7 +414,6 @@ __global__ void __launch_bounds__(kThreads)
       __syncthreads();
       clear();
     }
-    __syncthreads();
   }
   if (!kPairs) {
     __syncthreads();
@@ -467,7 +491,6 @@ extern "C" int gbj_groupby(gbj_ctx *ctx, const int32_t *d_keys, const int32_t *d
   const uint64_t groups_cap =
       std::max<uint64_t>(1024, hint ? std::min<uint64_t>(hint, n) : std::min<uint64_t>(n, 1ull << 24));
   if (strategy == 0) strategy = (hint && hint <= kSlots / 2) ? 1 : (hint ? 2 : 1);
-  const bool priv = strategy == 1 && hint && hint <= kPrivMaxGroups;
 
   Scratch scratch(ctx, s);
   // level-2 table: cap slots + 1 dedicated INT32_MIN group
@@ -492,7 +515,7 @@ extern "C" int gbj_groupby(gbj_ctx *ctx, const int32_t *d_keys, const int32_t *d
   uint32_t tslots_arg = kSlots;
   auto launch = [&](auto kern, int tab, const int2 *pairs, uint64_t w, const uint64_t *poff,
                     const uint64_t *items, uint32_t P) -> int {
-    const size_t smem = (size_t)tab * (8 + 4 + 4 + 4 + 4);
+    const size_t smem = (size_t)tab * (sizeof(uint4) + sizeof(uint2));
     GBJ_CHECK_CUDA(ctx, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     int per_sm = 1;
     GBJ_CHECK_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kThreads, smem));
@@ -506,12 +529,10 @@ extern "C" int gbj_groupby(gbj_ctx *ctx, const int32_t *d_keys, const int32_t *d
     // raw input in items of w rows; level 1 persists for the CTA's lifetime
     const uint64_t w = std::max<uint64_t>(1u << 16, (n + ctx->sm_count * 8 - 1) / (ctx->sm_count * 8));
     const uint64_t wq = (w + 3) / 4 * 4;
-    if (priv) {
-      GBJ_TRY(launch(k_groupby<true, false>, kPrivSlots * kWarps, nullptr, wq, nullptr, nullptr, 0));
-    } else {
-      tslots_arg = (uint32_t)std::min<uint64_t>(kSlots, std::max<uint64_t>(64, next_pow2(2 * groups_cap)));
-      GBJ_TRY(launch(k_groupby<false, false>, kSlots, nullptr, wq, nullptr, nullptr, 0));
-    }
+    tslots_arg = (uint32_t)std::min<uint64_t>(kSlots, std::max<uint64_t>(64, next_pow2(4 * (hint ? hint : groups_cap))));
+    const bool vec = (reinterpret_cast<uintptr_t>(d_keys) | reinterpret_cast<uintptr_t>(d_values)) % 16 == 0;
+    if (vec) GBJ_TRY(launch(k_groupby<false, true>, (int)tslots_arg, nullptr, wq, nullptr, nullptr, 0));
+    else GBJ_TRY(launch(k_groupby<false, false>, (int)tslots_arg, nullptr, wq, nullptr, nullptr, 0));
   } else {
     // partition so each partition holds ~kSlots/4 groups; add bits (without
     // adding a partitioning pass) so partitions fit one work item of w rows
@@ -537,7 +558,7 @@ extern "C" int gbj_groupby(gbj_ctx *ctx, const int32_t *d_keys, const int32_t *d
     k_groupby_items<<<(P + 255) / 256, 256, 0, s>>>(poff, P, w, items);
     GBJ_TRY(after_launch(ctx, "k_groupby_items", s));
     GBJ_TRY(scan_u64(ctx, items, items, P, s));
-    GBJ_TRY(launch(k_groupby<false, true>, kSlots, pairs, w, poff, items, P));
+    GBJ_TRY(launch(k_groupby<true, false>, (int)tslots_arg, pairs, w, poff, items, P));
   }
   const uint64_t emit_threads = 256;
   const uint64_t emit_blocks =

@@ -275,6 +275,8 @@ class Context:
                 hash_bits=0, strategy=0, stream=None):
         import torch
 
+        if keys.numel() != values.numel():
+            raise ValueError("groupby: keys and values differ in length")
         dev = keys.device
         cap = max(out_capacity, 1)
         ok = torch.empty(cap, dtype=torch.int32, device=dev)

@@ -76,3 +76,31 @@ def test_groupby_full_config(ctx, oracle, card, theta):
     """2^29 rows, value U[-2^20, 2^20): full size."""
     k, v = engine.gen_groupby(900 + card.bit_length() + int(theta), 1 << 29, card, theta)
     check(ctx, oracle, k, v, expected_groups=card)
+
+
+@pytest.mark.parametrize("strategy", [1, 2])
+def test_groupby_hot_groups_wrap(ctx, oracle, strategy):
+    """Groups far above 65535 rows per CTA with extreme values: the on-chip
+    16-bit sum halves and counts are moved to level 2 before they wrap."""
+    i32 = np.iinfo(np.int32)
+    rng = np.random.default_rng(21)
+    n = (1 << 22) + 3
+    k = rng.integers(0, 3, n).astype(np.int32)
+    k[rng.integers(0, n, 1000)] = i32.min
+    v = np.where(rng.random(n) < 0.5, i32.max, i32.min).astype(np.int32)
+    v[::7] = -1
+    check(ctx, oracle, k, v, expected_groups=4, strategy=strategy)
+
+
+def test_groupby_unaligned_columns(ctx, oracle):
+    """Columns that do not start on a 16-byte boundary take the scalar-load form."""
+    k, v = engine.gen_groupby(31, (1 << 20) + 5, 700, 0.5)
+    ks, vs = slice(1, len(k) - 4), slice(3, len(v) - 2)  # equal lengths, offsets 4 and 12 bytes
+    exp = oracle.groupby(k[ks], v[vs], threads=cpu_threads())
+    dk, dv = dev(k), dev(v)
+    assert dk[ks].numel() == dv[vs].numel() == len(k) - 5
+    res = ctx.groupby(dk[ks], dv[vs], len(exp[0]), expected_groups=700, strategy=1)
+    ctx.sync()
+    got = sort_groups(*[host(t) for t in res[:5]], host(res[5])[0])
+    for a, b in zip(got, exp):
+        assert (a == b).all()
