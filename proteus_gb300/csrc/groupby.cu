@@ -51,8 +51,6 @@ struct GTable {
   // dedicated INT32_MIN group at index mask + 1 of cnt/sum/mn/mx
 };
 
-__device__ __forceinline__ uint32_t enc_max(int32_t v) { return (uint32_t)v ^ kFlip; }
-__device__ __forceinline__ uint32_t enc_min(int32_t v) { return ~((uint32_t)v ^ kFlip); }
 __device__ __forceinline__ int32_t dec_max(uint32_t u) { return (int32_t)(u ^ kFlip); }
 __device__ __forceinline__ int32_t dec_min(uint32_t u) { return (int32_t)(~u ^ kFlip); }
 
@@ -111,20 +109,90 @@ __device__ __forceinline__ void emit(const Out &o, uint64_t pos, int32_t key, ui
 
 // Level 1: one table per CTA in shared memory, updated with 32-bit atomics
 // only (64-bit shared atomics have no native form and cost a CAS loop).
-// A slot holds
-//   meta = {key', min', max', count}
-//   sums = {A, B}: with u = value + 2^31 (unsigned, < 2^32), A sums the low
-//          16 bits of u and B the high 16 bits, so
-//          SUM(value) = B * 2^16 + A - count * 2^31.
-// A, B and count stay exact while a slot takes at most 65535 rows between
+// Structure of arrays, so that the atomics of a warp's 32 random slots
+// spread over all 32 banks:
+//   key[]  key' (0 = empty)
+//   ext[]  {min', max'}: also the hints that decide whether a min/max
+//          atomic is issued
+//   cnt[]  rows
+//   a[], b[]  with u = value + 2^31 (unsigned, < 2^32), a sums the low 16
+//          bits of u and b the high 16 bits, so
+//          SUM(value) = b * 2^16 + a - count * 2^31.
+// a, b and cnt stay exact while a slot takes at most 65535 rows between
 // flushes; the kernel tracks a CTA-wide bound on every slot's count and moves
 // slots above kHot rows to level 2 before the bound could pass 65535.
+// cnt, a and b have 2^rlog columns per slot, column = lane mod 2^rlog: a
+// shared atomic costs a data-pipe pass per bank it hits twice, and with
+// lane-indexed columns the lanes of a warp that land on slots in one bank
+// fall on different banks (32 columns: never two lanes on one bank).  The
+// host takes as many columns as shared memory allows; a slot's value is the
+// sum of its columns.
+__device__ __forceinline__ uint32_t s_ld(uint32_t a) {
+  uint32_t r;
+  asm("ld.shared.u32 %0, [%1];" : "=r"(r) : "r"(a));
+  return r;
+}
+__device__ __forceinline__ uint2 s_ld2(uint32_t a) {
+  uint2 r;
+  asm("ld.shared.v2.u32 {%0, %1}, [%2];" : "=r"(r.x), "=r"(r.y) : "r"(a));
+  return r;
+}
+__device__ __forceinline__ void s_st(uint32_t a, uint32_t v) {
+  asm volatile("st.shared.u32 [%0], %1;" ::"r"(a), "r"(v) : "memory");
+}
+__device__ __forceinline__ void s_st2(uint32_t a, uint2 v) {
+  asm volatile("st.shared.v2.u32 [%0], {%1, %2};" ::"r"(a), "r"(v.x), "r"(v.y) : "memory");
+}
+
+// The table's arrays by their shared-state-space addresses (32-bit).
 struct L1 {
-  uint4 *meta;
-  uint2 *sums;
+  uint32_t ext, key, cnt, a, b;
   uint32_t mask;   // slots - 1
   uint32_t shift;  // 32 - log2(slots): the home slot is the hash's top bits
+  uint32_t rlog;   // log2 of the columns of cnt, a, b
+
+  // Lays the arrays out from shared address `base` for `slots` slots.
+  __device__ __forceinline__ void place(uint32_t base, uint32_t slots, uint32_t rlog_) {
+    rlog = rlog_;
+    ext = base;
+    key = ext + 8u * slots;
+    cnt = key + 4u * slots;
+    a = cnt + (4u * slots << rlog);
+    b = a + (4u * slots << rlog);
+    mask = slots - 1;
+    shift = 32u - (uint32_t)__popc(slots - 1);
+  }
+  // this lane's column of slot h (byte offset into cnt / a / b)
+  __device__ __forceinline__ uint32_t col(uint32_t h) const {
+    return ((h << rlog) + ((threadIdx.x & 31) & ((1u << rlog) - 1))) * 4u;
+  }
+  __device__ __forceinline__ uint32_t sum_cols(uint32_t arr, int i) const {
+    uint32_t v = 0;
+    for (uint32_t r = 0; r < (1u << rlog); ++r) v += s_ld(arr + (((uint32_t)i << rlog) + r) * 4u);
+    return v;
+  }
+  // a slot as {key', min', max', count} and {a, b} (block-synchronised paths)
+  __device__ __forceinline__ uint4 meta(int i) const {
+    const uint2 e = s_ld2(ext + 8u * i);
+    return make_uint4(s_ld(key + 4u * i), e.x, e.y, count(i));
+  }
+  __device__ __forceinline__ uint2 sums(int i) const { return make_uint2(sum_cols(a, i), sum_cols(b, i)); }
+  __device__ __forceinline__ uint32_t count(int i) const { return sum_cols(cnt, i); }
+  __device__ __forceinline__ void reset(int i, uint32_t k) const {
+    s_st(key + 4u * i, k);
+    s_st2(ext + 8u * i, make_uint2(0, 0));
+    for (uint32_t r = 0; r < (1u << rlog); ++r) {
+      const uint32_t o = (((uint32_t)i << rlog) + r) * 4u;
+      s_st(cnt + o, 0);
+      s_st(a + o, 0);
+      s_st(b + o, 0);
+    }
+  }
 };
+// shared bytes per slot with 2^rlog accumulator columns
+__host__ __device__ constexpr size_t slot_bytes(int rlog) { return 12 + ((size_t)12 << rlog); }
+// Shared bytes the table may take per CTA (two CTAs per SM).
+constexpr size_t kTableBudget = 96 * 1024;
 
 constexpr uint32_t kChunk = 32768;        // rows per step between bound checks
 constexpr uint32_t kCountLimit = 65535;   // rows a slot may take between flushes
@@ -135,11 +203,6 @@ constexpr uint32_t kHot = kCountLimit - kChunk;  // slots above go to level 2 at
 // earlier row's atomics: it only decides the claim path, which re-checks with
 // CAS, and whether a min/max atomic is worth issuing).
 __device__ __forceinline__ uint32_t s_addr(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
-__device__ __forceinline__ uint4 s_ld4(uint32_t a) {
-  uint4 r;
-  asm("ld.shared.v4.u32 {%0, %1, %2, %3}, [%4];" : "=r"(r.x), "=r"(r.y), "=r"(r.z), "=r"(r.w) : "r"(a));
-  return r;
-}
 __device__ __forceinline__ uint32_t s_ld_volatile(uint32_t a) {
   uint32_t r;
   asm volatile("ld.volatile.shared.u32 %0, [%1];" : "=r"(r) : "r"(a) : "memory");
@@ -163,8 +226,11 @@ __device__ __forceinline__ uint32_t s_cas(uint32_t a, uint32_t cmp, uint32_t v) 
 
 // Home slot: Fibonacci hashing, top bits.  Independent of the fmix32 low bits
 // that pick a key's partition, so it also spreads the keys of one partition.
+// The home is a bucket of two slots (an even slot and the next): one 8-byte
+// load checks both, so a key displaced by one collision still takes the
+// fast path.  Insertion claims the first empty slot from the bucket on.
 __device__ __forceinline__ uint32_t l1_home(const L1 &t, int32_t k) {
-  return ((uint32_t)k * 0x9E3779B1u) >> t.shift;
+  return (((uint32_t)k * 0x9E3779B1u) >> (t.shift + 1)) << 1;
 }
 
 __device__ __forceinline__ int64_t l1_sum(uint2 ab, uint32_t c) {
@@ -179,9 +245,9 @@ __device__ __forceinline__ int l1_find(const L1 &t, const GTable &g, int32_t k, 
   const uint32_t u = (uint32_t)v ^ kFlip;
   if (k != INT32_MIN) {
     const uint32_t kk = (uint32_t)k ^ kFlip;
-    const uint32_t base = s_addr(t.meta);
+    const uint32_t base = t.key;
     for (int step = 0; step < kProbeL1; ++step) {
-      const uint32_t a = base + h * (uint32_t)sizeof(uint4);
+      const uint32_t a = base + h * 4u;
       uint32_t cur = s_ld_volatile(a);
       if (cur == 0) cur = s_cas(a, 0u, kk);
       if (cur == 0 || cur == kk) return (int)h;
@@ -197,24 +263,35 @@ __device__ __forceinline__ void l1_row(const L1 &t, const GTable &g, int32_t k, 
                                        uint32_t *status) {
   const uint32_t u = (uint32_t)v ^ kFlip;  // biased value = max' encoding; ~u = min'
   uint32_t h = l1_home(t, k);
-  const uint32_t mb = s_addr(t.meta), sb = s_addr(t.sums);
-  uint4 m = s_ld4(mb + h * (uint32_t)sizeof(uint4));
+  const uint32_t kk = (uint32_t)k ^ kFlip;
+  uint2 pair = s_ld2(t.key + h * 4u);
   // INT32_MIN's key' is 0 (the empty mark), so it always takes the slow path
-  if (m.x != ((uint32_t)k ^ kFlip) || k == INT32_MIN) {
+  bool found = k != INT32_MIN && (pair.x == kk || pair.y == kk);
+  if (found) {
+    h += pair.x != kk;
+  } else if (k != INT32_MIN) {
+    // the next bucket holds most keys displaced from their home
+    const uint32_t h2 = (h + 2) & t.mask;
+    pair = s_ld2(t.key + h2 * 4u);
+    found = pair.x == kk || pair.y == kk;
+    if (found) h = h2 + (pair.x != kk);
+  }
+  if (!found) {
     const int f = l1_find(t, g, k, v, h, status);
     if (f < 0) {
       spill = true;
       return;
     }
     h = (uint32_t)f;
-    m = s_ld4(mb + h * (uint32_t)sizeof(uint4));
   }
-  const uint32_t ma = mb + h * (uint32_t)sizeof(uint4), sa = sb + h * (uint32_t)sizeof(uint2);
-  s_red_add(ma + 12, 1u);
-  s_red_add(sa, u & 0xffffu);
-  s_red_add(sa + 4, u >> 16);
-  s_red_max_above(ma + 4, ~u, m.y);
-  s_red_max_above(ma + 8, u, m.z);
+  const uint32_t ea = t.ext + h * 8u;
+  const uint2 e = s_ld2(ea);
+  const uint32_t c = t.col(h);
+  s_red_add(t.cnt + c, 1u);
+  s_red_add(t.a + c, u & 0xffffu);
+  s_red_add(t.b + c, u >> 16);
+  s_red_max_above(ea, ~u, e.x);
+  s_red_max_above(ea + 4, u, e.y);
 }
 
 // Moves one level-1 slot to level 2.
@@ -222,6 +299,50 @@ __device__ __forceinline__ void slot_to_l2(const GTable &g, uint4 m, uint2 ab, u
   if (m.w == 0) return;
   const int32_t k = (int32_t)(m.x ^ kFlip);
   g_update(g, g_slot(g, k, status), m.w, l1_sum(ab, m.w), m.y, m.z);
+}
+
+// Block-wide helpers (every thread of the CTA calls them).
+__device__ __forceinline__ void l1_clear(const L1 &t, int tab, uint32_t &s_bound) {
+  for (int i = threadIdx.x; i < tab; i += kThreads) t.reset(i, 0);
+  if (threadIdx.x == 0) s_bound = 0;
+}
+
+// level 1 -> level 2 (every occupied slot)
+__device__ __forceinline__ void l1_flush(const L1 &t, int tab, const GTable &g, uint32_t *status) {
+  for (int i = threadIdx.x; i < tab; i += kThreads) slot_to_l2(g, t.meta(i), t.sums(i), status);
+}
+
+// Before adding `rows` rows: if the bound on every slot's count could pass
+// kCountLimit, move the hot slots to level 2 and recompute the bound.  Ends
+// with s_bound updated by thread 0; the caller's next __syncthreads
+// publishes it.
+__device__ __forceinline__ void l1_make_room(const L1 &t, int tab, const GTable &g, uint32_t rows, bool &spill,
+                                             uint32_t *status, uint32_t &s_bound, uint32_t *s_warp) {
+  if (s_bound + rows <= kCountLimit) {
+    __syncthreads();
+    if (threadIdx.x == 0) s_bound += rows;
+    return;
+  }
+  __syncthreads();
+  uint32_t mx = 0;
+  for (int i = threadIdx.x; i < tab; i += kThreads) {
+    const uint4 m = t.meta(i);
+    if (m.w > kHot) {
+      slot_to_l2(g, m, t.sums(i), status);
+      t.reset(i, m.x);
+      spill = true;
+    } else {
+      mx = max(mx, m.w);
+    }
+  }
+  mx = __reduce_max_sync(0xffffffffu, mx);
+  if ((threadIdx.x & 31) == 0) s_warp[threadIdx.x >> 5] = mx;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    uint32_t b = 0;
+    for (int w2 = 0; w2 < kWarps; ++w2) b = max(b, s_warp[w2]);
+    s_bound = b + rows;
+  }
 }
 
 // Reads keys/values rows [i, i+4) with 16-byte loads.
@@ -238,17 +359,17 @@ __device__ __forceinline__ void load4(const int32_t *__restrict__ keys, const in
 // item and a whole partition is emitted directly).  kVec: the raw columns
 // are 16-byte aligned and read 4 rows per thread per load.
 template <bool kPairs, bool kVec>
-__global__ void __launch_bounds__(kThreads)
+__global__ void __launch_bounds__(kThreads, 2)
     k_groupby(const int32_t *__restrict__ keys, const int32_t *__restrict__ vals,
               const int2 *__restrict__ pairs, uint64_t n, uint64_t w,
               const uint64_t *__restrict__ poff, const uint64_t *__restrict__ item_off, uint32_t P,
-              uint32_t tslots, GTable g, Out o, unsigned long long *item_ctr, uint32_t *status) {
+              uint32_t tslots, uint32_t rlog, GTable g, Out o, unsigned long long *item_ctr, uint32_t *status) {
   extern __shared__ __align__(16) unsigned char smem[];
   // shared-table size: a power of two <= kSlots chosen by the host from the
   // expected groups per item
   const int kTab = (int)tslots;
-  L1 t{reinterpret_cast<uint4 *>(smem), reinterpret_cast<uint2 *>(smem + (size_t)kTab * sizeof(uint4)),
-       tslots - 1, 32u - (uint32_t)__popc(tslots - 1)};
+  L1 t;
+  t.place(s_addr(smem), tslots, rlog);
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   __shared__ unsigned long long s_item;
   __shared__ int s_spill;
@@ -257,49 +378,7 @@ __global__ void __launch_bounds__(kThreads)
   __shared__ uint32_t s_bound;  // >= every slot's count
   const uint64_t total_items = kPairs ? item_off[P] : (n + w - 1) / w;
 
-  auto clear = [&]() {
-    for (int i = threadIdx.x; i < kTab; i += kThreads) {
-      t.meta[i] = make_uint4(0, 0, 0, 0);
-      t.sums[i] = make_uint2(0, 0);
-    }
-    if (threadIdx.x == 0) s_bound = 0;
-  };
-  // level 1 -> level 2 (every occupied slot)
-  auto flush = [&]() {
-    for (int i = threadIdx.x; i < kTab; i += kThreads) slot_to_l2(g, t.meta[i], t.sums[i], status);
-  };
-  // Before adding `rows` rows: if the bound could pass kCountLimit, move the
-  // hot slots to level 2 and recompute the bound.  Called by the whole CTA.
-  auto make_room = [&](uint32_t rows, bool &spill) {
-    if (s_bound + rows <= kCountLimit) {
-      __syncthreads();
-      if (threadIdx.x == 0) s_bound += rows;
-      return;
-    }
-    __syncthreads();
-    uint32_t mx = 0;
-    for (int i = threadIdx.x; i < kTab; i += kThreads) {
-      const uint4 m = t.meta[i];
-      if (m.w > kHot) {
-        slot_to_l2(g, m, t.sums[i], status);
-        t.meta[i] = make_uint4(m.x, 0, 0, 0);
-        t.sums[i] = make_uint2(0, 0);
-        spill = true;
-      } else {
-        mx = max(mx, m.w);
-      }
-    }
-    mx = __reduce_max_sync(0xffffffffu, mx);
-    if (lane == 0) s_warp[warp] = mx;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-      uint32_t b = 0;
-      for (int w2 = 0; w2 < kWarps; ++w2) b = max(b, s_warp[w2]);
-      s_bound = b + rows;
-    }
-  };
-
-  clear();
+  l1_clear(t, kTab, s_bound);
   for (;;) {
     __syncthreads();
     if (threadIdx.x == 0) {
@@ -328,7 +407,7 @@ __global__ void __launch_bounds__(kThreads)
     bool spill = false;
     for (uint64_t c0 = lo; c0 < hi; c0 += kChunk) {
       const uint64_t c1 = c0 + kChunk < hi ? c0 + kChunk : hi;
-      make_room((uint32_t)(c1 - c0), spill);
+      l1_make_room(t, kTab, g, (uint32_t)(c1 - c0), spill, status, s_bound, s_warp);
       __syncthreads();
       if (!kPairs && kVec) {
         // 4 rows per thread per step; the loads of the next two steps are
@@ -386,7 +465,7 @@ __global__ void __launch_bounds__(kThreads)
       if (whole && !s_spill) {
         // final groups of a whole partition: compact straight to the output
         uint32_t mine = 0;
-        for (int i = threadIdx.x; i < kTab; i += kThreads) mine += t.meta[i].w != 0;
+        for (int i = threadIdx.x; i < kTab; i += kThreads) mine += t.count(i) != 0;
         mine = __reduce_add_sync(0xffffffffu, mine);
         if (lane == 0) s_warp[warp] = mine;
         __syncthreads();
@@ -400,24 +479,24 @@ __global__ void __launch_bounds__(kThreads)
         for (int w2 = 0; w2 < warp; ++w2) pos += s_warp[w2];
         for (int i0 = warp * 32; i0 < kTab; i0 += kThreads) {
           const int i = i0 + lane;
-          const uint4 m = i < kTab ? t.meta[i] : make_uint4(0, 0, 0, 0);
+          const uint4 m = i < kTab ? t.meta(i) : make_uint4(0, 0, 0, 0);
           const bool occ = m.w != 0;
           const unsigned b = __ballot_sync(0xffffffffu, occ);
           if (occ)
-            emit(o, pos + __popc(b & ((1u << lane) - 1)), (int32_t)(m.x ^ kFlip), m.w, l1_sum(t.sums[i], m.w),
+            emit(o, pos + __popc(b & ((1u << lane) - 1)), (int32_t)(m.x ^ kFlip), m.w, l1_sum(t.sums(i), m.w),
                  dec_min(m.y), dec_max(m.z), status);
           pos += __popc(b);
         }
       } else {
-        flush();
+        l1_flush(t, kTab, g, status);
       }
       __syncthreads();
-      clear();
+      l1_clear(t, kTab, s_bound);
     }
   }
   if (!kPairs) {
     __syncthreads();
-    flush();
+    l1_flush(t, kTab, g, status);
   }
 }
 
@@ -512,16 +591,21 @@ extern "C" int gbj_groupby(gbj_ctx *ctx, const int32_t *d_keys, const int32_t *d
   GBJ_TRY(scratch.get(1, &ctr));
   GBJ_CHECK_CUDA(ctx, cudaMemsetAsync(ctr, 0, sizeof(unsigned long long), s));
 
-  uint32_t tslots_arg = kSlots;
+  uint32_t tslots_arg = kSlots, rlog_arg = 0;
+  // as many accumulator columns (up to 32) as the table budget allows
+  auto pick_rlog = [&]() {
+    rlog_arg = 0;
+    while (rlog_arg < 5 && (size_t)tslots_arg * slot_bytes(rlog_arg + 1) <= kTableBudget) ++rlog_arg;
+  };
   auto launch = [&](auto kern, int tab, const int2 *pairs, uint64_t w, const uint64_t *poff,
                     const uint64_t *items, uint32_t P) -> int {
-    const size_t smem = (size_t)tab * (sizeof(uint4) + sizeof(uint2));
+    const size_t smem = (size_t)tab * slot_bytes(rlog_arg);
     GBJ_CHECK_CUDA(ctx, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     int per_sm = 1;
     GBJ_CHECK_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kThreads, smem));
     per_sm = std::max(per_sm, 1);
     kern<<<ctx->sm_count * per_sm, kThreads, smem, s>>>(d_keys, d_values, pairs, n, w, poff, items,
-                                                        P, tslots_arg, g, o, ctr, ctx->d_status);
+                                                        P, tslots_arg, rlog_arg, g, o, ctr, ctx->d_status);
     return after_launch(ctx, "k_groupby", s);
   };
 
@@ -529,9 +613,10 @@ extern "C" int gbj_groupby(gbj_ctx *ctx, const int32_t *d_keys, const int32_t *d
     // raw input in items of w rows; level 1 persists for the CTA's lifetime
     const uint64_t w = std::max<uint64_t>(1u << 16, (n + ctx->sm_count * 8 - 1) / (ctx->sm_count * 8));
     const uint64_t wq = (w + 3) / 4 * 4;
-    tslots_arg = (uint32_t)std::min<uint64_t>(kSlots, std::max<uint64_t>(64, next_pow2(4 * (hint ? hint : groups_cap))));
-    const bool vec = (reinterpret_cast<uintptr_t>(d_keys) | reinterpret_cast<uintptr_t>(d_values)) % 16 == 0;
-    if (vec) GBJ_TRY(launch(k_groupby<false, true>, (int)tslots_arg, nullptr, wq, nullptr, nullptr, 0));
+    tslots_arg = (uint32_t)std::min<uint64_t>(kSlots, std::max<uint64_t>(64, next_pow2(16 * (hint ? hint : groups_cap))));
+    pick_rlog();
+    const bool aligned = (reinterpret_cast<uintptr_t>(d_keys) | reinterpret_cast<uintptr_t>(d_values)) % 16 == 0;
+    if (aligned) GBJ_TRY(launch(k_groupby<false, true>, (int)tslots_arg, nullptr, wq, nullptr, nullptr, 0));
     else GBJ_TRY(launch(k_groupby<false, false>, (int)tslots_arg, nullptr, wq, nullptr, nullptr, 0));
   } else {
     // partition so each partition holds ~kSlots/4 groups; add bits (without
@@ -548,6 +633,7 @@ extern "C" int gbj_groupby(gbj_ctx *ctx, const int32_t *d_keys, const int32_t *d
     const uint32_t P = 1u << bits;
     tslots_arg = (uint32_t)std::min<uint64_t>(
         kSlots, std::max<uint64_t>(64, next_pow2(4 * ((groups_cap + P - 1) >> bits))));
+    pick_rlog();
     int2 *pairs;
     uint64_t *poff, *items;
     GBJ_TRY(scratch.get(n, &pairs));
