@@ -322,10 +322,12 @@ __device__ __forceinline__ uint32_t item_partition(const uint64_t *__restrict__ 
 
 enum : int { kAggGeneric = 0, kAggCountXor = 1, kAggCountProduct = 2 };
 
-// Table slot of key k: multiply-shift of the fmix32 bits above the partition
-// bits onto [0, cap).
+// Table slot of key k: Fibonacci hashing onto [0, cap) (multiply, then the
+// high word of hash * cap).  The keys of one partition share the low fmix32
+// bits that chose it; the multiplicative hash is independent of those.
 __device__ __forceinline__ uint32_t table_slot(int32_t k, int bits, uint32_t cap) {
-  return (uint32_t)(((uint64_t)(gbjd::fmix32((uint32_t)k) >> bits) * cap) >> (32 - bits));
+  (void)bits;
+  return __umulhi((uint32_t)k * 0x9E3779B1u, cap);
 }
 
 template <int kAgg>
