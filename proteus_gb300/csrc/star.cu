@@ -54,6 +54,7 @@ struct DimDev {
 struct Dims {
   DimDev d[kMaxDims];
   int32_t nd;
+  int32_t late;  // dimension whose mask is gathered only for rows still alive, -1 none
   uint64_t total_rows;
 };
 
@@ -229,11 +230,22 @@ __global__ void __launch_bounds__(kFactThreads)
       uint64_t m[4] = {active, active, active, active};
 #pragma unroll
       for (int d = 0; d < kMaxDims; ++d) {
-        if (d < dims.nd) {
+        if (d < dims.nd && d != dims.late) {
           m[0] &= dim_mask(dims.d[d], s_mask, k4[d].x, nojoin[d]);
           m[1] &= dim_mask(dims.d[d], s_mask, k4[d].y, nojoin[d]);
           m[2] &= dim_mask(dims.d[d], s_mask, k4[d].z, nojoin[d]);
           m[3] &= dim_mask(dims.d[d], s_mask, k4[d].w, nojoin[d]);
+        }
+      }
+      // the largest gathered dimension last, only for rows some query still
+      // passes (most rows have failed every query by then)
+#pragma unroll
+      for (int d = 0; d < kMaxDims; ++d) {
+        if (d < dims.nd && d == dims.late) {
+          if (m[0]) m[0] &= dim_mask(dims.d[d], s_mask, k4[d].x, nojoin[d]);
+          if (m[1]) m[1] &= dim_mask(dims.d[d], s_mask, k4[d].y, nojoin[d]);
+          if (m[2]) m[2] &= dim_mask(dims.d[d], s_mask, k4[d].z, nojoin[d]);
+          if (m[3]) m[3] &= dim_mask(dims.d[d], s_mask, k4[d].w, nojoin[d]);
         }
       }
       if (m[0]) {
@@ -494,6 +506,18 @@ extern "C" int gbj_star_plan_create(gbj_ctx *ctx, const gbj_star_fact *fact,
     }
   }
   p->dims.total_rows = rows;
+  // the late dimension: the largest one gathered from L2, when another
+  // gathered dimension is checked before it
+  p->dims.late = -1;
+  {
+    int gathered = 0, big = -1;
+    for (int d = 0; d < fact->n_dims; ++d) {
+      if (p->dims.d[d].smem_off >= 0) continue;
+      ++gathered;
+      if (big < 0 || p->dims.d[d].n > p->dims.d[big].n) big = d;
+    }
+    if (gathered >= 2) p->dims.late = big;
+  }
   p->vec = aligned;
   cudaStream_t s = ctx->stream;
   int rc = pool_alloc(ctx, rows * sizeof(uint64_t) + 16, s, reinterpret_cast<void **>(&p->masks));
