@@ -235,16 +235,25 @@ __global__ void __launch_bounds__(kThreads) k_serve_build(const SBatch *__restri
 // Probe + group-by.  With at most kL1 group slots the matches of an item
 // accumulate in shared memory indexed by group slot and are flushed once
 // per item; otherwise each match adds to the global group slot directly.
+// The shared accumulators use 32-bit atomics only (64-bit shared atomics
+// have no native form): a count, and the low / high 16 bits of the biased
+// value v + 2^31 in l1_a / l1_b, exact for the first 65535 matches of a slot
+// in an item; later matches (duplicate-heavy builds) add their value to the
+// global 64-bit sum directly.
+constexpr uint32_t kL1Exact = 65535;
+
 __global__ void __launch_bounds__(kProbeThreads) k_serve_probe(const SBatch *__restrict__ d, SlotDev *slot) {
   __shared__ uint64_t s_item0[kMaxB];
   __shared__ unsigned long long s_it;
   __shared__ uint32_t l1_cnt[kL1];
-  __shared__ unsigned long long l1_sum[kL1];
+  __shared__ uint32_t l1_a[kL1];
+  __shared__ uint32_t l1_b[kL1];
   const int nq = load_item0(d, kPhProbe, s_item0);
   const uint64_t total = d->items[kPhProbe];
   for (int i = threadIdx.x; i < kL1; i += blockDim.x) {
     l1_cnt[i] = 0;
-    l1_sum[i] = 0;
+    l1_a[i] = 0;
+    l1_b[i] = 0;
   }
   for (;;) {
     const uint64_t it = next_item(&slot->ctr[kPhProbe], &s_it);
@@ -256,8 +265,13 @@ __global__ void __launch_bounds__(kProbeThreads) k_serve_probe(const SBatch *__r
     const unsigned long long side_n = *q.side_n;
     auto add = [&](uint32_t gs, int32_t v) {
       if (use_l1) {
-        atomicAdd(&l1_cnt[gs], 1u);
-        atomicAdd(&l1_sum[gs], (unsigned long long)(int64_t)v);
+        if (atomicAdd(&l1_cnt[gs], 1u) < kL1Exact) {
+          const uint32_t u = (uint32_t)v ^ kFlip;
+          atomicAdd(&l1_a[gs], u & 0xffffu);
+          atomicAdd(&l1_b[gs], u >> 16);
+        } else {
+          atomicAdd(&q.gsum[gs], (unsigned long long)(int64_t)v);
+        }
       } else {
         atomicAdd(&q.gcnt[gs], 1ull);
         atomicAdd(&q.gsum[gs], (unsigned long long)(int64_t)v);
@@ -296,10 +310,13 @@ __global__ void __launch_bounds__(kProbeThreads) k_serve_probe(const SBatch *__r
       for (uint64_t i = threadIdx.x; i <= q.gmask + 1; i += blockDim.x) {
         const uint32_t c = l1_cnt[i];
         if (c) {
+          const uint64_t in_ab = c < kL1Exact ? c : kL1Exact;  // matches summed in a / b
+          const int64_t sum = (int64_t)(((uint64_t)l1_b[i] << 16) + l1_a[i]) - (int64_t)in_ab * (int64_t)kFlip;
           atomicAdd(&q.gcnt[i], (unsigned long long)c);
-          atomicAdd(&q.gsum[i], l1_sum[i]);
+          atomicAdd(&q.gsum[i], (unsigned long long)sum);
           l1_cnt[i] = 0;
-          l1_sum[i] = 0;
+          l1_a[i] = 0;
+          l1_b[i] = 0;
         }
       }
     }

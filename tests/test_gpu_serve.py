@@ -225,3 +225,27 @@ def test_serve_resident_table_budget(ctx):
         srv.register_table(bk, bk, 1 << 16)
     assert e.value.code == abi.ERR_BUDGET
     srv.close()
+
+
+def test_serve_duplicate_heavy_groups(ctx, oracle):
+    """Every probe row matches thousands of build rows of two groups, so a
+    group slot takes far more than 65535 matches within one work item; values
+    at both int32 extremes."""
+    i32 = np.iinfo(np.int32)
+    rng = np.random.default_rng(17)
+    bk = np.full(4000, 7, dtype=np.int32)
+    bg = rng.integers(0, 2, 4000).astype(np.int32)
+    pk = np.full(40000, 7, dtype=np.int32)
+    pk[::9] = 8  # misses
+    pv = np.where(rng.random(40000) < 0.5, i32.max, i32.min).astype(np.int32)
+    for srv in (serve.Server(ctx, max_batch=4), serve.Server.plain(ctx)):
+        o = serve.Output(8)
+        t = srv.submit(dev(bk), dev(bg), dev(pk), dev(pv), 4, o)
+        assert srv.wait(t, timeout=120.0) == abi.OK
+        same(o.sorted(), expected(oracle, (bk, bg, pk, pv)))
+        tid = srv.register_table(dev(bk), dev(bg), 4)
+        o2 = serve.Output(8)
+        t = srv.submit(None, None, dev(pk), dev(pv), 4, o2, table=tid)
+        assert srv.wait(t, timeout=120.0) == abi.OK
+        same(o2.sorted(), expected(oracle, (bk, bg, pk, pv)))
+        srv.close()
