@@ -110,9 +110,8 @@ __global__ void __launch_bounds__(1024)
 struct TileSmem {
   uint32_t whist[kTileWarps][kMaxDigits];  // per-warp digit counts, then run offsets
   int2 sorted[kTile];
-  uint16_t sdig[kTile];
   uint32_t dstart[kMaxDigits];
-  uint32_t gpos[kMaxDigits];
+  uint32_t gdelta[kMaxDigits];  // output position of sorted[i] = gdelta[digit] + i
   uint32_t wsum[8];
 };
 
@@ -211,10 +210,12 @@ __global__ void __launch_bounds__(kTileThreads, kTileCtas)
       if (lane == 31) S.wsum[warp] = incl;
     }
     __syncthreads();
+    uint32_t my_start = 0;
     if ((uint32_t)tid < ndig) {
       uint32_t add = 0;
       for (int w = 0; w < warp; ++w) add += S.wsum[w];
-      S.dstart[tid] = add + incl - tot;
+      my_start = add + incl - tot;
+      S.dstart[tid] = my_start;
     }
     __syncthreads();
 #pragma unroll
@@ -222,10 +223,11 @@ __global__ void __launch_bounds__(kTileThreads, kTileCtas)
       if (lo + tid + j * kTileThreads < hi) {
         const uint32_t pos = S.dstart[dg[j]] + S.whist[warp][dg[j]] + rk[j];
         S.sorted[pos] = tup[j];
-        S.sdig[pos] = (uint16_t)dg[j];
       }
     }
-    if ((uint32_t)tid < ndig) S.gpos[tid] = gpos;
+    // written after the scatter, so the cursor atomic's round trip overlaps it
+    // (modulo 2^32: gdelta + i is the output position)
+    if ((uint32_t)tid < ndig) S.gdelta[tid] = gpos - my_start;
     const uint32_t cnt = (uint32_t)(hi - lo);
     const uint64_t tn = t + gridDim.x;
     if (tn < ntiles) {
@@ -237,9 +239,10 @@ __global__ void __launch_bounds__(kTileThreads, kTileCtas)
     for (int j = 0; j < kTilePer; ++j) {
       const uint32_t i = tid + j * kTileThreads;
       if (i < cnt) {
-        const uint32_t d = S.sdig[i];
-        const uint32_t g = S.gpos[d] + (i - S.dstart[d]);
+        // the digit again from the key: cheaper than storing it beside the
+        // tuple at the scatter (a bank-conflicting shared store) and loading it
         const int2 v = S.sorted[i];
+        const uint32_t g = S.gdelta[digit_of<kDigit>(v.x, dshift, dmask)] + i;
         if (kAoSOut) {
           out_pairs[g] = v;
         } else {
