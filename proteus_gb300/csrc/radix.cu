@@ -108,9 +108,8 @@ __global__ void __launch_bounds__(1024)
 }
 
 struct TileSmem {
-  uint32_t whist[kTileWarps][kMaxDigits];  // per-warp digit counts, then run offsets
+  uint32_t whist[kTileWarps][kMaxDigits];  // per-warp digit counts, then each warp's run start
   int2 sorted[kTile];
-  uint32_t dstart[kMaxDigits];
   uint32_t gdelta[kMaxDigits];  // output position of sorted[i] = gdelta[digit] + i
   uint32_t wsum[8];
 };
@@ -215,13 +214,15 @@ __global__ void __launch_bounds__(kTileThreads, kTileCtas)
       uint32_t add = 0;
       for (int w = 0; w < warp; ++w) add += S.wsum[w];
       my_start = add + incl - tot;
-      S.dstart[tid] = my_start;
+      // absolute start of each warp's run of this digit in the tile
+#pragma unroll
+      for (int w = 0; w < kTileWarps; ++w) S.whist[w][tid] += my_start;
     }
     __syncthreads();
 #pragma unroll
     for (int j = 0; j < kTilePer; ++j) {
       if (lo + tid + j * kTileThreads < hi) {
-        const uint32_t pos = S.dstart[dg[j]] + S.whist[warp][dg[j]] + rk[j];
+        const uint32_t pos = S.whist[warp][dg[j]] + rk[j];
         S.sorted[pos] = tup[j];
       }
     }
