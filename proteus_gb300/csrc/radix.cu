@@ -184,15 +184,11 @@ __global__ void __launch_bounds__(kTileThreads, kTileCtas)
       }
     }
     __syncthreads();
-    // per digit: prefix over warps (in place) and the tile total
+    // per digit: the tile total (the per-warp starts follow the digit scan)
     uint32_t tot = 0;
     if ((uint32_t)tid < ndig) {
 #pragma unroll
-      for (int w = 0; w < kTileWarps; ++w) {
-        const uint32_t c = S.whist[w][tid];
-        S.whist[w][tid] = tot;
-        tot += c;
-      }
+      for (int w = 0; w < kTileWarps; ++w) tot += S.whist[w][tid];
     }
     // this tile's run of each digit in the output (consumed after the scatter)
     uint32_t gpos = 0;
@@ -215,8 +211,13 @@ __global__ void __launch_bounds__(kTileThreads, kTileCtas)
       for (int w = 0; w < warp; ++w) add += S.wsum[w];
       my_start = add + incl - tot;
       // absolute start of each warp's run of this digit in the tile
+      uint32_t run = my_start;
 #pragma unroll
-      for (int w = 0; w < kTileWarps; ++w) S.whist[w][tid] += my_start;
+      for (int w = 0; w < kTileWarps; ++w) {
+        const uint32_t c = S.whist[w][tid];
+        S.whist[w][tid] = run;
+        run += c;
+      }
     }
     __syncthreads();
 #pragma unroll
