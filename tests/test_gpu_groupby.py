@@ -104,3 +104,12 @@ def test_groupby_unaligned_columns(ctx, oracle):
     got = sort_groups(*[host(t) for t in res[:5]], host(res[5])[0])
     for a, b in zip(got, exp):
         assert (a == b).all()
+
+
+@pytest.mark.parametrize("card", [4, 12, 30, 60, 100, 300])
+@pytest.mark.parametrize("theta", [0.0, 1.0])
+def test_groupby_accumulator_columns(ctx, oracle, card, theta):
+    """Group counts whose on-chip tables (16 x groups: 64 .. 4096 slots) take
+    32, 16, 8, 4, 2 and 1 lane-indexed accumulator columns."""
+    k, v = engine.gen_groupby(4000 + card + int(theta), (1 << 20) + 7, card, theta)
+    check(ctx, oracle, k, v, expected_groups=card, strategy=1)
