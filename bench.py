@@ -10,6 +10,10 @@ Other workloads (same JSON contract):
                       COUNT and int64 SUM(R.payload * S.payload)
   --workload groupby  2^29 rows, --card C groups (--theta 0 uniform or Zipf),
                       COUNT / int64 SUM / MIN / MAX per key
+  --workload star     64 star-join queries sharing one 2^28-row fact scan
+  --workload serve    served stream of join + group-by queries (p50/p99)
+  --workload nest     RadixNest over int64 keys: 2^27 rows, --card C keys,
+                      COUNT / SUM / MIN / MAX of an int64 value
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
 
@@ -45,7 +49,7 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default="radix",
-                    choices=["radix", "plain", "groupby", "star", "serve"])
+                    choices=["radix", "plain", "groupby", "star", "serve", "nest"])
     ap.add_argument("--serve-queries", type=int, default=3000, help="queries per open-loop rate")
     ap.add_argument("--log-r", type=int, default=None, help="log2 build rows (joins)")
     ap.add_argument("--log-s", type=int, default=None, help="log2 probe / input rows")
@@ -387,6 +391,90 @@ class GroupBy:
                        f"(hash-partitioned per thread), {threads} threads")
 
 
+class Nest:
+    """RadixNest over int64 keys (the aggregation twin): per distinct key
+    COUNT, SUM, MIN, MAX of an int64 value."""
+    metric, unit, dtype = "nest Gtuples/s", "Gtuples/s", "int64"
+
+    def __init__(self, args):
+        self.ls = args.log_s or 27
+        self.n = 1 << self.ls
+        self.card = args.card
+
+    def describe(self):
+        return {"workload": f"RadixNest int64 group-by 2^{self.ls} rows, {self.card} distinct int64 keys "
+                            f"(uniform), int64 value: COUNT, SUM int64, MIN, MAX",
+                "rows": self.n, "cardinality": self.card, "l2": "inputs (2 GiB) larger than L2"}
+
+    def generate(self):
+        import numpy as np
+
+        rng = np.random.default_rng(SEED)
+        base = rng.integers(np.iinfo(np.int64).min, np.iinfo(np.int64).max, self.card, dtype=np.int64)
+        self.k = base[rng.integers(0, self.card, self.n)]
+        self.v = rng.integers(-(1 << 40), 1 << 40, self.n, dtype=np.int64)
+
+    def device(self, ctx):
+        import torch
+
+        self.ctx = ctx
+        self.dk, self.dv = torch.from_numpy(self.k).cuda(), torch.from_numpy(self.v).cuda()
+        self.cap = self.card + 16
+        self.res = None
+
+    def step(self):
+        self.res = self.ctx.nest_i64(self.dk, self.dv, self.cap, expected_groups=self.card)
+
+    def results(self):
+        return int(self.res[5].cpu()[0])
+
+    def pin(self):
+        import torch
+
+        self.hk = torch.from_numpy(self.k).pin_memory()
+        self.hv = torch.from_numpy(self.v).pin_memory()
+        self.h_out = [torch.empty(self.cap, dtype=torch.int64).pin_memory() for _ in range(5)]
+        self.h_n = torch.empty(1, dtype=torch.int64).pin_memory()
+
+    def e2e_step(self):
+        self.dk.copy_(self.hk, non_blocking=True)
+        self.dv.copy_(self.hv, non_blocking=True)
+        self.step()
+        for h, d in zip(self.h_out, self.res[:5]):
+            h.copy_(d, non_blocking=True)
+        self.h_n.copy_(self.res[5], non_blocking=True)
+
+    def e2e_results(self):
+        return int(self.h_n[0])
+
+    def h2d_bytes(self):
+        return 16 * self.n
+
+    def d2h_bytes(self):
+        return 40 * self.cap + 8
+
+    def units_per_step(self):
+        return self.n
+
+    def kernel_bytes(self, name):
+        return {"k_nest_build": 16 * self.n}.get(name)  # (int64 key, int64 value) per row
+
+    def extra(self, ms, steps, peak):
+        comp = 16 * self.n * steps
+        return {"job_hbm_gbs_compulsory": round(comp / (ms / 1e3) / 1e9, 1),
+                "job_frac_compulsory": round(comp / (ms / 1e3) / 1e9 / peak, 4)}
+
+    def cpu(self, threads, sample_log):
+        from oracle import oracle as O
+
+        n = 1 << min(sample_log - 2, self.ls)
+        t0 = time.perf_counter()
+        O.nest_i64(self.k[:n], self.v[:n])
+        dt = time.perf_counter() - t0
+        return n, dt, (f"first {n} rows; oracle C port of RadixNest over the int64 twin's partitionHT "
+                       f"and bucket chains, 1 thread")
+
+
 class StarBatch:
     """64 star-join query variants over a 2^28-row fact table, all in one
     graph replay sharing the fact scan (one step = one batch)."""
@@ -705,7 +793,7 @@ class Serve:
 
 
 WORKLOADS = {"radix": RadixJoin, "plain": PlainJoin, "groupby": GroupBy, "star": StarBatch,
-             "serve": Serve}
+             "serve": Serve, "nest": Nest}
 
 
 # ------------------------------------------------------------- helpers
@@ -802,7 +890,7 @@ def run_reference(args):
         "impl": "reference", "metric": wl.metric, "value": value, "unit": wl.unit,
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": 1e3 * secs / args.steps, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "int32", "data": "synthetic (seeded generator)",
+        "vs_baseline": None, "dtype": getattr(wl, "dtype", "int32"), "data": "synthetic (seeded generator)",
         "config": wl.describe(),
         "cpu_baseline": {"value": value, "unit": wl.unit, "cores": threads, "kind": "port",
                          "sample": sample},
@@ -909,7 +997,7 @@ def run_gpu(args):
         line = {
             "metric": wl.metric, "value": round(value, 3), "unit": wl.unit, "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
-            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32",
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": getattr(wl, "dtype", "int32"),
             "data": "synthetic (seeded generator)", "config": cfg,
             "e2e": e2e, "roofline": roof, "cpu_baseline": cpu, "clocks": clk,
             "gpu_launches": launches, **wl.extra(ms, args.steps, peak),
@@ -946,7 +1034,7 @@ def run_custom(args, wl, ctx, rank, world):
         line = {
             "metric": wl.metric, "value": round(world * value, 1), "unit": wl.unit, "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": None,
-            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32",
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": getattr(wl, "dtype", "int32"),
             "data": "synthetic (seeded generator)", "config": cfg,
             "e2e": {"value": round(world * value, 1), "unit": wl.unit, "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": None,

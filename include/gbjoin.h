@@ -201,6 +201,24 @@ int gbj_partition_i64(gbj_ctx *ctx, const int64_t *d_keys,
                       int32_t bits, int64_t *d_out_keys,
                       int64_t *d_out_payload, uint64_t *d_offsets,
                       void *stream);
+/* RadixNest over int64 keys (Nest, core/olap/lib/operators/radix-nest.cpp:
+ * 326-700, on the aggregation twin's clusters and bucket chains,
+ * radix-aggr.cpp:163-259): one output row per distinct key with COUNT and,
+ * for d_vals not NULL, SUM (int64, two's-complement wrap), MIN and MAX of
+ * the value column (0 when d_vals is NULL).  Groups come out unordered;
+ * *d_n_groups (device) gets their number even when it exceeds out_capacity
+ * (then GBJ_ERR_CAPACITY at the next sync).  expected_groups sizes the
+ * table (0: min(n, 2^24)); more distinct keys than the table holds also
+ * give GBJ_ERR_CAPACITY. */
+int gbj_nest_i64(gbj_ctx *ctx, const int64_t *d_keys, const int64_t *d_vals, uint64_t n,
+                 uint64_t expected_groups, int64_t *d_out_keys, int64_t *d_out_count,
+                 int64_t *d_out_sum, int64_t *d_out_min, int64_t *d_out_max,
+                 uint64_t out_capacity, uint64_t *d_n_groups, void *stream);
+/* RJStepwise of the aggregation twin (radix-aggr.cpp:261-358): the number of
+ * (R, S) pairs with equal int64 keys into *d_count (device). */
+int gbj_radix_join_count_i64(gbj_ctx *ctx, const int64_t *d_r_keys, uint64_t nr,
+                             const int64_t *d_s_keys, uint64_t ns, int64_t *d_count,
+                             void *stream);
 
 typedef struct gbj_radix_params {
   int32_t bits;       /* radix bits, 0 = autotuned                        */

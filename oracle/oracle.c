@@ -1181,3 +1181,137 @@ void orc_partition_ht_agg(const int64_t *keys, uint64_t n, int32_t *counts, int6
   free(tk);
   free(tp);
 }
+
+/* Bucket chains over one cluster of int64-key tuples, as the twin's
+ * bucket_chaining_agg_prepare (radix-agg: radix-aggr.cpp:181-204):
+ * N = next power of two >= n, MASK = (N - 1) << 14, bucket index
+ * (key & MASK) >> 14, chains 1-based through next[]. */
+typedef struct {
+  int *bucket, *next;
+  uint64_t mask;
+} orc_chain_ht;
+
+static void orc_chain_prepare(const int64_t *keys, uint32_t n, orc_chain_ht *ht) {
+  uint32_t N = 1;
+  while (N < n) N <<= 1;
+  ht->mask = (uint64_t)(N - 1) << ORC_RADIX_BITS;
+  ht->next = (int *)malloc((n ? n : 1) * sizeof(int));
+  ht->bucket = (int *)calloc(N, sizeof(int));
+  for (uint32_t i = 0; i < n;) {
+    const uint64_t idx = ((uint64_t)keys[i] & ht->mask) >> ORC_RADIX_BITS;
+    ht->next[i] = ht->bucket[idx];
+    ht->bucket[idx] = (int)++i;
+  }
+}
+
+static void orc_chain_free(orc_chain_ht *ht) {
+  free(ht->bucket);
+  free(ht->next);
+}
+
+/* RJStepwise of the int64-key twin (radix-aggr.cpp:261-358): both sides
+ * clustered by partitionHT, then per cluster present on both sides, the
+ * bucket chains of R probed by every S tuple (bucket_chaining_agg_probe,
+ * :206-223); returns the number of (R, S) pairs with equal keys. */
+int64_t orc_join_count_i64(const int64_t *rk, uint64_t nr, const int64_t *sk, uint64_t ns) {
+  const uint32_t C = 1u << ORC_RADIX_BITS;
+  int32_t *rc = (int32_t *)malloc(C * sizeof(int32_t)), *sc = (int32_t *)malloc(C * sizeof(int32_t));
+  int64_t *rkk = (int64_t *)malloc((nr ? nr : 1) * sizeof(int64_t)), *rp = (int64_t *)malloc((nr ? nr : 1) * sizeof(int64_t));
+  int64_t *skk = (int64_t *)malloc((ns ? ns : 1) * sizeof(int64_t)), *sp = (int64_t *)malloc((ns ? ns : 1) * sizeof(int64_t));
+  orc_partition_ht_agg(rk, nr, rc, rkk, rp);
+  orc_partition_ht_agg(sk, ns, sc, skk, sp);
+  int64_t result = 0;
+  uint64_t r = 0, s = 0;
+  for (uint32_t c = 0; c < C; ++c) {
+    if (rc[c] > 0 && sc[c] > 0) {
+      orc_chain_ht ht;
+      orc_chain_prepare(rkk + r, (uint32_t)rc[c], &ht);
+      for (int32_t j = 0; j < sc[c]; ++j) {
+        const int64_t key = skk[s + j];
+        const uint64_t idx = ((uint64_t)key & ht.mask) >> ORC_RADIX_BITS;
+        for (int hit = ht.bucket[idx]; hit > 0; hit = ht.next[hit - 1])
+          if (rkk[r + hit - 1] == key) result++;
+      }
+      orc_chain_free(&ht);
+    }
+    r += rc[c];
+    s += sc[c];
+  }
+  free(rc);
+  free(sc);
+  free(rkk);
+  free(rp);
+  free(skk);
+  free(sp);
+  return result;
+}
+
+static int orc_cmp_i64_first(const void *a, const void *b) {
+  const int64_t x = ((const int64_t *)a)[0], y = ((const int64_t *)b)[0];
+  return x < y ? -1 : x > y;
+}
+
+/* RadixNest over int64-key tuples (radix-nest.cpp:326-700 with the twin's
+ * partitionHT and bucket chains): tuples are clustered, each cluster gets
+ * its bucket chains, and every tuple not yet marked starts a group, walks
+ * its chain, folds every tuple of equal key into the group (COUNT, SUM with
+ * int64 wrap-around, MIN, MAX of the value column) and marks it.  Groups are
+ * returned sorted by key.  Returns the number of groups; with out_cap below
+ * it only that many are written. */
+int64_t orc_nest_i64(const int64_t *keys, const int64_t *vals, uint64_t n, int64_t *out_keys, int64_t *out_cnt,
+                     int64_t *out_sum, int64_t *out_min, int64_t *out_max, uint64_t out_cap) {
+  const uint32_t C = 1u << ORC_RADIX_BITS;
+  int32_t *cnt = (int32_t *)malloc(C * sizeof(int32_t));
+  int64_t *ck = (int64_t *)malloc((n ? n : 1) * sizeof(int64_t)), *crow = (int64_t *)malloc((n ? n : 1) * sizeof(int64_t));
+  orc_partition_ht_agg(keys, n, cnt, ck, crow);
+  /* groups as rows of {key, count, sum, min, max} */
+  int64_t *g = (int64_t *)malloc((n ? n : 1) * 5 * sizeof(int64_t));
+  uint64_t ng = 0, r = 0;
+  unsigned char *marked = (unsigned char *)calloc(n ? n : 1, 1);
+  for (uint32_t c = 0; c < C; ++c) {
+    const uint32_t m = (uint32_t)cnt[c];
+    if (m > 0) {
+      orc_chain_ht ht;
+      orc_chain_prepare(ck + r, m, &ht);
+      for (uint32_t j = 0; j < m; ++j) {
+        if (marked[r + j]) continue;
+        const int64_t key = ck[r + j];
+        uint64_t count = 0, sum = 0;
+        int64_t mn = INT64_MAX, mx = INT64_MIN;
+        const uint64_t idx = ((uint64_t)key & ht.mask) >> ORC_RADIX_BITS;
+        for (int hit = ht.bucket[idx]; hit > 0; hit = ht.next[hit - 1]) {
+          const uint64_t t = r + (uint64_t)(hit - 1);
+          if (ck[t] != key) continue;
+          const int64_t v = vals ? vals[crow[t]] : 0;
+          count++;
+          sum += (uint64_t)v;
+          if (v < mn) mn = v;
+          if (v > mx) mx = v;
+          marked[t] = 1;
+        }
+        int64_t *o = g + 5 * ng++;
+        o[0] = key;
+        o[1] = (int64_t)count;
+        o[2] = (int64_t)sum;
+        o[3] = mn;
+        o[4] = mx;
+      }
+      orc_chain_free(&ht);
+    }
+    r += m;
+  }
+  qsort(g, ng, 5 * sizeof(int64_t), orc_cmp_i64_first);
+  for (uint64_t i = 0; i < ng && i < out_cap; ++i) {
+    if (out_keys) out_keys[i] = g[5 * i];
+    if (out_cnt) out_cnt[i] = g[5 * i + 1];
+    if (out_sum) out_sum[i] = g[5 * i + 2];
+    if (out_min) out_min[i] = g[5 * i + 3];
+    if (out_max) out_max[i] = g[5 * i + 4];
+  }
+  free(cnt);
+  free(ck);
+  free(crow);
+  free(g);
+  free(marked);
+  return (int64_t)ng;
+}

@@ -169,6 +169,14 @@ void orc_radix_cluster_i64(const int64_t *keys, const int64_t *payload,
 void orc_partition_ht_agg(const int64_t *keys, uint64_t n, int32_t *counts,
                           int64_t *out_keys, int64_t *out_payload);
 
+/* RJStepwise of the int64-key twin: number of (R, S) pairs with equal keys. */
+int64_t orc_join_count_i64(const int64_t *rk, uint64_t nr, const int64_t *sk, uint64_t ns);
+
+/* RadixNest over int64 keys: per distinct key COUNT, SUM (int64, wrapping),
+ * MIN, MAX of vals (NULL: 0), sorted by key; returns the number of groups. */
+int64_t orc_nest_i64(const int64_t *keys, const int64_t *vals, uint64_t n, int64_t *out_keys, int64_t *out_cnt,
+                     int64_t *out_sum, int64_t *out_min, int64_t *out_max, uint64_t out_cap);
+
 #ifdef __cplusplus
 }
 #endif

@@ -72,6 +72,10 @@ def lib():
         L.orc_radix_cluster_i64.argtypes = [vp, vp, u64, i32, i32, vp, vp, vp]
         L.orc_partition_ht_agg.restype = None
         L.orc_partition_ht_agg.argtypes = [vp, u64, vp, vp, vp]
+        L.orc_join_count_i64.restype = i64
+        L.orc_join_count_i64.argtypes = [vp, u64, vp, u64]
+        L.orc_nest_i64.restype = i64
+        L.orc_nest_i64.argtypes = [vp, vp, u64, vp, vp, vp, vp, vp, u64]
         L.orc_bloom_semijoin.restype = i64
         L.orc_bloom_semijoin.argtypes = [vp, u64, vp, u64, u64, vp, u64]
         L.orc_join_groupby.restype = i64
@@ -93,6 +97,10 @@ def ref_lib():
         R.ref_partition_ht.argtypes = [vp, C.c_uint32, vp, vp, vp]
         R.ref_partition_ht_agg.restype = None
         R.ref_partition_ht_agg.argtypes = [vp, C.c_uint32, vp, vp, vp]
+        R.ref_rj_stepwise_agg.restype = i64
+        R.ref_rj_stepwise_agg.argtypes = [vp, C.c_uint32, vp, C.c_uint32]
+        R.ref_nest_counts.restype = None
+        R.ref_nest_counts.argtypes = [vp, C.c_uint32, vp, C.c_uint32, vp]
         R.ref_num_radix_bits.restype = i32
         _ref = R
     return _ref
@@ -231,6 +239,25 @@ def partition_ht_agg(keys):
     return c, ok[:n], op[:n]
 
 
+def join_count_i64(r_keys, s_keys):
+    """RJStepwise of the int64-key twin: matching (R, S) pairs."""
+    L = lib()
+    r = np.ascontiguousarray(r_keys, dtype=np.int64)
+    s = np.ascontiguousarray(s_keys, dtype=np.int64)
+    return int(L.orc_join_count_i64(_p(r), len(r), _p(s), len(s)))
+
+
+def nest_i64(keys, vals=None):
+    """RadixNest over int64 keys -> (keys, count, sum, min, max) sorted by key."""
+    L = lib()
+    keys = np.ascontiguousarray(keys, dtype=np.int64)
+    v = None if vals is None else np.ascontiguousarray(vals, dtype=np.int64)
+    n = len(keys)
+    out = [np.empty(max(n, 1), np.int64) for _ in range(5)]
+    ng = int(L.orc_nest_i64(_p(keys), _p(v), n, *[_p(a) for a in out], max(n, 1)))
+    return tuple(a[:ng] for a in out)
+
+
 def bloom_semijoin(build, probe, filter_size):
     """Positions of the probe rows the reference's bloom filter passes."""
     L = lib()
@@ -320,6 +347,29 @@ def ref_partition_ht_agg(keys):
     ok, op = np.empty(max(n, 1), np.int64), np.empty(max(n, 1), np.int64)
     R.ref_partition_ht_agg(_p(keys), n, _p(c), _p(ok), _p(op))
     return c, ok[:n], op[:n]
+
+
+def ref_rj_stepwise_agg(rkeys, skeys):
+    """The reference's own int64-key RJStepwise (oracle/_ref): match count."""
+    R = ref_lib()
+    if R is None:
+        return None
+    r = np.ascontiguousarray(rkeys, dtype=np.int64)
+    s = np.ascontiguousarray(skeys, dtype=np.int64)
+    return int(R.ref_rj_stepwise_agg(_p(r), len(r), _p(s), len(s)))
+
+
+def ref_nest_counts(keys, query):
+    """Group size of each query key from the reference's own partitionHT and
+    bucket chains (oracle/_ref)."""
+    R = ref_lib()
+    if R is None:
+        return None
+    keys = np.ascontiguousarray(keys, dtype=np.int64)
+    query = np.ascontiguousarray(query, dtype=np.int64)
+    out = np.empty(max(len(query), 1), np.int64)
+    R.ref_nest_counts(_p(keys), len(keys), _p(query), len(query), _p(out))
+    return out[:len(query)]
 
 
 def ref_partition_ht(keys):

@@ -141,6 +141,8 @@ SIGNATURES = {
     "gbj_bloom_probe": (C.c_int, [vp, vp, vp, u64, vp, vp, vp]),
     "gbj_bloom_destroy": (C.c_int, [vp, vp]),
     "gbj_partition_i64": (C.c_int, [vp, vp, vp, u64, i32, i32, vp, vp, vp, vp]),
+    "gbj_nest_i64": (C.c_int, [vp, vp, vp, u64, u64, vp, vp, vp, vp, vp, u64, vp, vp]),
+    "gbj_radix_join_count_i64": (C.c_int, [vp, vp, u64, vp, u64, vp, vp]),
     "gbj_sort_by_key": (C.c_int, [vp, P(vp), i32, u64, i32, i32, P(vp), vp]),
     "gbj_hash_rearrange": (C.c_int, [vp, P(vp), i32, u64, i32, C.c_uint32, P(vp), vp, vp]),
     "gbj_catalog_create": (C.c_int, [vp, P(vp)]),

@@ -1,0 +1,226 @@
+// The int64-key twins of the radix path: RadixNest's grouping and the
+// int64 RJStepwise match count.
+//
+// Stand in for Nest (RadixNest, core/olap/lib/operators/radix-nest.cpp:
+// 326-700), which clusters {int64 key, int64 payload} tuples with the
+// aggregation twin's partitionHT, builds bucket chains per cluster and folds
+// every tuple of a key into that key's group (core/platform/lib/util/radix/
+// aggregations/radix-aggr.cpp:163-259), and for the twin's RJStepwise
+// (radix-aggr.cpp:261-358), which counts the (R, S) pairs with equal keys.
+//
+// GB300 design: one global open-addressing table per call, 2^k slots of
+// 64-bit keys (key ^ 2^63, so all-zero = empty; INT64_MIN, whose stored form
+// is 0, has a dedicated slot), updated with native 64-bit global atomics
+// (the table of up to ~2^22 groups stays in the 126 MB L2).  The nest keeps
+// COUNT, SUM (two's-complement wrap, as int64 addition), and MIN / MAX in
+// order-preserving unsigned encodings combined with atomicMax, issued only
+// when the value improves the stored extreme.  The join count stores each
+// R key's multiplicity and every S row adds the multiplicity of its key.
+#include <algorithm>
+
+#include "gbj_internal.cuh"
+
+using namespace gbj;
+
+namespace {
+
+constexpr int kThreads = 256;
+constexpr uint64_t kFlip64 = 0x8000000000000000ull;
+
+__device__ __forceinline__ uint64_t fmix64(uint64_t k) {  // murmur3 64-bit finaliser
+  k ^= k >> 33;
+  k *= 0xff51afd7ed558ccdull;
+  k ^= k >> 33;
+  k *= 0xc4ceb9fe1a85ec53ull;
+  k ^= k >> 33;
+  return k;
+}
+
+struct Table64 {
+  unsigned long long *key;  // key ^ 2^63; 0 = empty
+  unsigned long long *cnt;
+  unsigned long long *sum;
+  unsigned long long *mn;   // ~(value ^ 2^63), combined with max
+  unsigned long long *mx;   // value ^ 2^63
+  uint64_t mask;            // slots - 1; slot mask + 1 is INT64_MIN's
+};
+
+// Slot of key k (claimed when new), or -1 when the table is full.
+__device__ __forceinline__ int64_t slot_of(const Table64 &t, int64_t k, uint32_t *status) {
+  if (k == INT64_MIN) return (int64_t)(t.mask + 1);
+  const unsigned long long kk = (unsigned long long)k ^ kFlip64;
+  uint64_t h = fmix64((uint64_t)k) & t.mask;
+  for (uint64_t step = 0; step <= t.mask; ++step) {
+    unsigned long long cur = *(volatile unsigned long long *)&t.key[h];
+    if (cur == kk) return (int64_t)h;
+    if (cur == 0) {
+      cur = atomicCAS(&t.key[h], 0ull, kk);
+      if (cur == 0 || cur == kk) return (int64_t)h;
+    }
+    h = (h + 1) & t.mask;
+  }
+  gbjd::latch(status, GBJ_DEV_CAPACITY);
+  return -1;
+}
+
+// Slot of key k when present, else -1 (read only).
+__device__ __forceinline__ int64_t find(const Table64 &t, int64_t k) {
+  if (k == INT64_MIN) return (int64_t)(t.mask + 1);
+  const unsigned long long kk = (unsigned long long)k ^ kFlip64;
+  uint64_t h = fmix64((uint64_t)k) & t.mask;
+  for (uint64_t step = 0; step <= t.mask; ++step) {
+    const unsigned long long cur = __ldg(&t.key[h]);
+    if (cur == kk) return (int64_t)h;
+    if (cur == 0) return -1;
+    h = (h + 1) & t.mask;
+  }
+  return -1;
+}
+
+__device__ __forceinline__ void add_row(const Table64 &t, int64_t k, const int64_t *vals, uint64_t i,
+                                        uint32_t *status) {
+  const int64_t s = slot_of(t, k, status);
+  if (s < 0) return;
+  atomicAdd(&t.cnt[s], 1ull);
+  if (vals) {
+    const int64_t v = __ldcs(vals + i);
+    atomicAdd(&t.sum[s], (unsigned long long)v);
+    const unsigned long long emx = (unsigned long long)v ^ kFlip64, emn = ~emx;
+    if (emn > *(volatile unsigned long long *)&t.mn[s]) atomicMax(&t.mn[s], emn);
+    if (emx > *(volatile unsigned long long *)&t.mx[s]) atomicMax(&t.mx[s], emx);
+  }
+}
+
+// Every row into its group (vals null: counts only).
+__global__ void __launch_bounds__(kThreads)
+    k_nest_build(const int64_t *__restrict__ keys, const int64_t *__restrict__ vals, uint64_t n, Table64 t,
+                 uint32_t *status) {
+  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += stride)
+    add_row(t, __ldcs(keys + i), vals, i, status);
+}
+
+// The occupied slots (and INT64_MIN's) to the output; one output
+// reservation per warp.
+__global__ void __launch_bounds__(kThreads)
+    k_nest_emit(Table64 t, bool with_vals, int64_t *__restrict__ ok, int64_t *__restrict__ oc,
+                int64_t *__restrict__ os, int64_t *__restrict__ omn, int64_t *__restrict__ omx, uint64_t cap,
+                unsigned long long *__restrict__ n_out, uint32_t *status) {
+  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  const uint64_t slots = t.mask + 2;
+  const int lane = threadIdx.x & 31;
+  for (uint64_t b0 = blockIdx.x * (uint64_t)blockDim.x; b0 < slots; b0 += stride) {
+    const uint64_t i = b0 + threadIdx.x;
+    bool occ = false;
+    int64_t key = INT64_MIN;
+    if (i <= t.mask) {
+      occ = t.key[i] != 0;
+      key = (int64_t)(t.key[i] ^ kFlip64);
+    } else if (i == t.mask + 1) {
+      occ = t.cnt[i] != 0;
+    }
+    const unsigned bal = __ballot_sync(0xffffffffu, occ);
+    unsigned long long base = 0;
+    if (lane == 0 && bal) base = atomicAdd(n_out, (unsigned long long)__popc(bal));
+    base = __shfl_sync(0xffffffffu, base, 0);
+    if (!occ) continue;
+    const uint64_t pos = base + __popc(bal & ((1u << lane) - 1));
+    if (pos >= cap) {
+      gbjd::latch(status, GBJ_DEV_CAPACITY);
+      continue;
+    }
+    if (ok) ok[pos] = key;
+    if (oc) oc[pos] = (int64_t)t.cnt[i];
+    if (os) os[pos] = with_vals ? (int64_t)t.sum[i] : 0;
+    if (omn) omn[pos] = with_vals ? (int64_t)(~t.mn[i] ^ kFlip64) : 0;
+    if (omx) omx[pos] = with_vals ? (int64_t)(t.mx[i] ^ kFlip64) : 0;
+  }
+}
+
+// S rows add the multiplicity of their key in R; one atomic per block.
+__global__ void __launch_bounds__(kThreads)
+    k_join_count_probe(const int64_t *__restrict__ keys, uint64_t n, Table64 t,
+                       unsigned long long *__restrict__ out) {
+  __shared__ unsigned long long red[kThreads / 32];
+  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  unsigned long long acc = 0;
+  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += stride) {
+    const int64_t s = find(t, __ldcs(keys + i));
+    if (s >= 0) acc += __ldg(&t.cnt[s]);
+  }
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    unsigned long long tot = 0;
+    for (int w = 0; w < kThreads / 32; ++w) tot += red[w];
+    if (tot) atomicAdd(out, tot);
+  }
+}
+
+// Table64 with `slots` slots (+ the INT64_MIN slot), zeroed, from scratch.
+int make_table(gbj_ctx *ctx, Scratch &scratch, uint64_t slots, bool with_vals, cudaStream_t s, Table64 *t) {
+  const uint64_t cols = with_vals ? 5 : 2;
+  unsigned long long *mem;
+  GBJ_TRY(scratch.get(cols * (slots + 1), &mem));
+  GBJ_CHECK_CUDA(ctx, cudaMemsetAsync(mem, 0, sizeof(unsigned long long) * cols * (slots + 1), s));
+  t->key = mem;
+  t->cnt = mem + (slots + 1);
+  t->sum = with_vals ? mem + 2 * (slots + 1) : nullptr;
+  t->mn = with_vals ? mem + 3 * (slots + 1) : nullptr;
+  t->mx = with_vals ? mem + 4 * (slots + 1) : nullptr;
+  t->mask = slots - 1;
+  return GBJ_OK;
+}
+
+unsigned grid_for(gbj_ctx *ctx, uint64_t n) {
+  return (unsigned)std::max<uint64_t>(1, std::min<uint64_t>((n + kThreads - 1) / kThreads,
+                                                            (uint64_t)ctx->sm_count * 8));
+}
+
+}  // namespace
+
+extern "C" int gbj_nest_i64(gbj_ctx *ctx, const int64_t *d_keys, const int64_t *d_vals, uint64_t n,
+                            uint64_t expected_groups, int64_t *d_out_keys, int64_t *d_out_count,
+                            int64_t *d_out_sum, int64_t *d_out_min, int64_t *d_out_max, uint64_t out_capacity,
+                            uint64_t *d_n_groups, void *stream) {
+  if (!ctx) return GBJ_ERR_INVALID;
+  if (!d_n_groups) return set_error(ctx, GBJ_ERR_INVALID, "nest_i64: null group count");
+  if (n && !d_keys) return set_error(ctx, GBJ_ERR_INVALID, "nest_i64: null key column");
+  if (n >= (1ull << 40)) return set_error(ctx, GBJ_ERR_INVALID, "nest_i64: n >= 2^40");
+  cudaStream_t s = pick_stream(ctx, stream);
+  prof_mark(ctx, s);
+  GBJ_CHECK_CUDA(ctx, cudaMemsetAsync(d_n_groups, 0, sizeof(uint64_t), s));
+  if (n == 0) return GBJ_OK;
+  const uint64_t groups = std::max<uint64_t>(1024, expected_groups ? std::min(expected_groups, n)
+                                                                   : std::min<uint64_t>(n, 1ull << 24));
+  Scratch scratch(ctx, s);
+  Table64 t;
+  GBJ_TRY(make_table(ctx, scratch, next_pow2(2 * groups), d_vals != nullptr, s, &t));
+  k_nest_build<<<grid_for(ctx, n), kThreads, 0, s>>>(d_keys, d_vals, n, t, ctx->d_status);
+  GBJ_TRY(after_launch(ctx, "k_nest_build", s));
+  k_nest_emit<<<grid_for(ctx, t.mask + 2), kThreads, 0, s>>>(
+      t, d_vals != nullptr, d_out_keys, d_out_count, d_out_sum, d_out_min, d_out_max, out_capacity,
+      reinterpret_cast<unsigned long long *>(d_n_groups), ctx->d_status);
+  return after_launch(ctx, "k_nest_emit", s);
+}
+
+extern "C" int gbj_radix_join_count_i64(gbj_ctx *ctx, const int64_t *d_r_keys, uint64_t nr,
+                                        const int64_t *d_s_keys, uint64_t ns, int64_t *d_count, void *stream) {
+  if (!ctx) return GBJ_ERR_INVALID;
+  if (!d_count) return set_error(ctx, GBJ_ERR_INVALID, "join_count_i64: null output");
+  if ((nr && !d_r_keys) || (ns && !d_s_keys)) return set_error(ctx, GBJ_ERR_INVALID, "join_count_i64: null key column");
+  if (nr >= (1ull << 40) || ns >= (1ull << 40)) return set_error(ctx, GBJ_ERR_INVALID, "join_count_i64: n >= 2^40");
+  cudaStream_t s = pick_stream(ctx, stream);
+  prof_mark(ctx, s);
+  GBJ_CHECK_CUDA(ctx, cudaMemsetAsync(d_count, 0, sizeof(int64_t), s));
+  if (nr == 0 || ns == 0) return GBJ_OK;
+  Scratch scratch(ctx, s);
+  Table64 t;
+  GBJ_TRY(make_table(ctx, scratch, next_pow2(std::max<uint64_t>(2 * nr, 1024)), false, s, &t));
+  k_nest_build<<<grid_for(ctx, nr), kThreads, 0, s>>>(d_r_keys, nullptr, nr, t, ctx->d_status);
+  GBJ_TRY(after_launch(ctx, "k_nest_build", s));
+  k_join_count_probe<<<grid_for(ctx, ns), kThreads, 0, s>>>(d_s_keys, ns, t,
+                                                            reinterpret_cast<unsigned long long *>(d_count));
+  return after_launch(ctx, "k_join_count_probe", s);
+}

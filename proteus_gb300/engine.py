@@ -243,6 +243,28 @@ class Context:
                                               _ptr(ok), _ptr(op), _ptr(off), self._s(stream)))
         return ok, op, off
 
+    def nest_i64(self, keys, vals, out_capacity, expected_groups=0, stream=None):
+        """RadixNest over int64 keys -> (keys, count, sum, min, max, n_groups) device tensors."""
+        import torch
+
+        if vals is not None and vals.numel() != keys.numel():
+            raise ValueError("nest_i64: keys and values differ in length")
+        cap = max(out_capacity, 1)
+        outs = [torch.empty(cap, dtype=torch.int64, device=keys.device) for _ in range(5)]
+        ng = torch.zeros(1, dtype=torch.int64, device=keys.device)
+        self.check(self.lib.gbj_nest_i64(self.handle, _ptr(keys), _ptr(vals), keys.numel(), expected_groups,
+                                         *[_ptr(o) for o in outs], out_capacity, _ptr(ng), self._s(stream)))
+        return (*outs, ng)
+
+    def radix_join_count_i64(self, r_keys, s_keys, stream=None):
+        """RJStepwise of the int64 twin -> device int64[1] match count."""
+        import torch
+
+        out = torch.zeros(1, dtype=torch.int64, device=r_keys.device)
+        self.check(self.lib.gbj_radix_join_count_i64(self.handle, _ptr(r_keys), r_keys.numel(), _ptr(s_keys),
+                                                     s_keys.numel(), _ptr(out), self._s(stream)))
+        return out
+
     # ----------------------------------------------------------------- sort
     def sort_by_key(self, cols, key_col: int, descending=False, stream=None):
         """-> the columns with rows ordered by cols[key_col] (stable)."""

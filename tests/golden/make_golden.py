@@ -194,6 +194,51 @@ def partition_ht_agg_cases():
     }
 
 
+def _i64_keys(lib, seed, n, span, salt):
+    keys = np.array([int(lib.gbj_gen_rand(seed, salt, i)) % span for i in range(n)], dtype=np.uint64)
+    return keys.view(np.int64) - (np.int64(span // 2) if span < (1 << 63) else 0)
+
+
+def nest_i64_cases():
+    """The reference's int64-key RJStepwise match counts and RadixNest group
+    sizes (bucket_chaining_agg_prepare / _probe over partitionHT clusters)."""
+    from oracle import oracle as O
+    from proteus_gb300 import abi
+
+    O.build()
+    if not O.build_ref(REF):
+        raise SystemExit("reference tree not found; cannot build oracle/_ref")
+    lib = abi.load()
+    joins, nests = [], []
+    for seed, nr, ns, span in ((31, 1 << 12, 1 << 14, 1 << 13), (32, 40000, 90001, 1 << 18),
+                               (33, 1 << 16, 1 << 16, 1 << 62), (34, 3000, 200000, 1 << 11)):
+        rk = _i64_keys(lib, seed, nr, span, 0x6B00)
+        sk = _i64_keys(lib, seed, ns, span, 0x6B01)
+        joins.append({"seed": seed, "nr": nr, "ns": ns, "span": str(span),
+                      "r_sha": hashlib.sha256(rk.tobytes()).hexdigest()[:16],
+                      "s_sha": hashlib.sha256(sk.tobytes()).hexdigest()[:16],
+                      "matches": O.ref_rj_stepwise_agg(rk, sk)})
+    for seed, n, span in ((41, 1 << 14, 1 << 10), (42, 100003, 1 << 16), (43, 1 << 16, 1 << 63),
+                          (44, 50000, 1 << 40)):
+        keys = _i64_keys(lib, seed, n, span, 0x6B02)
+        uk = np.unique(keys)
+        counts = O.ref_nest_counts(keys, uk)
+        nests.append({"seed": seed, "n": n, "span": str(span),
+                      "keys_sha": hashlib.sha256(keys.tobytes()).hexdigest()[:16],
+                      "groups": int(len(uk)),
+                      "counts_sha": hashlib.sha256(counts.astype(np.int64).tobytes()).hexdigest()[:16],
+                      "max_count": int(counts.max())})
+    return {
+        "about": "the reference's int64-key twins (core/platform/lib/util/radix/aggregations/"
+                 "radix-aggr.cpp), compiled from source by oracle/Makefile (target ref): RJStepwise match "
+                 "counts, and per distinct key (ascending) the group size bucket_chaining_agg_probe finds in "
+                 "its partitionHT cluster; keys = gbj_gen_rand(seed, salt, i) mod span, shifted to be signed "
+                 "(salts 0x6B00 R, 0x6B01 S, 0x6B02 nest).",
+        "joins": joins,
+        "nests": nests,
+    }
+
+
 def main():
     with open(os.path.join(OUT, "reference_cases.json"), "w") as f:
         json.dump(reference_cases(), f, indent=1)
@@ -201,6 +246,8 @@ def main():
         json.dump(rjstepwise_cases(), f, indent=1)
     with open(os.path.join(OUT, "partition_ht_agg_cases.json"), "w") as f:
         json.dump(partition_ht_agg_cases(), f, indent=1)
+    with open(os.path.join(OUT, "nest_i64_cases.json"), "w") as f:
+        json.dump(nest_i64_cases(), f, indent=1)
     print("wrote", OUT)
 
 
