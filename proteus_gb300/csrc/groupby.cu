@@ -433,29 +433,29 @@ __global__ void __launch_bounds__(kThreads, 2)
           }
         }
       } else {
-        for (uint64_t base = c0; base < c1; base += 4 * kThreads) {
-          int32_t k[4], v[4];
-          bool ok[4];
+        // 4 rows per thread per step (stride kThreads); the next step's
+        // loads are issued before this step's rows are applied
+        auto load = [&](uint64_t base, int2 (&r)[4]) {
 #pragma unroll
           for (int u = 0; u < 4; ++u) {
             const uint64_t i = base + threadIdx.x + (uint64_t)u * kThreads;
-            ok[u] = i < c1;
-            k[u] = 0;
-            v[u] = 0;
-            if (ok[u]) {
-              if (kPairs) {
-                const int2 pv = __ldcs(pairs + i);
-                k[u] = pv.x;
-                v[u] = pv.y;
-              } else {
-                k[u] = __ldcs(keys + i);
-                v[u] = __ldcs(vals + i);
-              }
+            r[u] = make_int2(0, 0);
+            if (i < c1) {
+              if (kPairs) r[u] = __ldcs(pairs + i);
+              else r[u] = make_int2(__ldcs(keys + i), __ldcs(vals + i));
             }
           }
+        };
+        int2 nx[4];
+        load(c0, nx);
+        for (uint64_t base = c0; base < c1; base += 4 * kThreads) {
+          int2 cur[4];
+#pragma unroll
+          for (int u = 0; u < 4; ++u) cur[u] = nx[u];
+          if (base + 4 * kThreads < c1) load(base + 4 * kThreads, nx);
 #pragma unroll
           for (int u = 0; u < 4; ++u)
-            if (ok[u]) l1_row(t, g, k[u], v[u], spill, status);
+            if (base + threadIdx.x + (uint64_t)u * kThreads < c1) l1_row(t, g, cur[u].x, cur[u].y, spill, status);
         }
       }
     }
