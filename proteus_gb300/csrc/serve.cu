@@ -869,6 +869,9 @@ extern "C" int gbj_server_destroy(gbj_server *sv) {
   if (sv->th.joinable()) sv->th.join();
   for (int i = 0; i < sv->nslots; ++i) cudaStreamSynchronize(sv->slots[i].stream);
   free_slots(sv);
+  // resident tables still registered go back to the pool
+  for (auto &kv : sv->tables) pool_release(sv->ctx, kv.second.mem, sv->ctx->stream);
+  sv->tables.clear();
   delete sv;
   return GBJ_OK;
 }

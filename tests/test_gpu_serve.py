@@ -249,3 +249,19 @@ def test_serve_duplicate_heavy_groups(ctx, oracle):
         assert srv.wait(t, timeout=120.0) == abi.OK
         same(o2.sorted(), expected(oracle, (bk, bg, pk, pv)))
         srv.close()
+
+
+def test_serve_resident_tables_released(ctx):
+    """Tables still registered when the server is destroyed go back to the
+    pool; so does an unregistered one."""
+    bk = dev(np.arange(1 << 16, dtype=np.int32))
+    ctx.sync()
+    before = ctx.pool_stats()["in_use"]
+    srv = serve.Server(ctx)
+    a = srv.register_table(bk, bk, 1 << 16)
+    srv.register_table(bk, bk, 1 << 16)
+    assert ctx.pool_stats()["in_use"] > before
+    srv.unregister_table(a)
+    srv.close()
+    ctx.sync()
+    assert ctx.pool_stats()["in_use"] == before
