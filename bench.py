@@ -457,7 +457,8 @@ class Nest:
         return self.n
 
     def kernel_bytes(self, name):
-        return {"k_nest_build": 16 * self.n}.get(name)  # (int64 key, int64 value) per row
+        # (int64 key, int64 value) per row: on-chip level for few groups, else the global table
+        return {"k_nest_l1": 16 * self.n, "k_nest_build": 16 * self.n}.get(name)
 
     def extra(self, ms, steps, peak):
         comp = 16 * self.n * steps

@@ -8,7 +8,9 @@
 // aggregations/radix-aggr.cpp:163-259), and for the twin's RJStepwise
 // (radix-aggr.cpp:261-358), which counts the (R, S) pairs with equal keys.
 //
-// GB300 design: one global open-addressing table per call, 2^k slots of
+// GB300 design: for few groups an on-chip level per CTA (32-bit shared
+// reductions only) in front of the global table; otherwise one global
+// open-addressing table per call, 2^k slots of
 // 64-bit keys (key ^ 2^63, so all-zero = empty; INT64_MIN, whose stored form
 // is 0, has a dedicated slot), updated with native 64-bit global atomics
 // (the table of up to ~2^22 groups stays in the 126 MB L2).  The nest keeps
@@ -77,18 +79,22 @@ __device__ __forceinline__ int64_t find(const Table64 &t, int64_t k) {
   return -1;
 }
 
-__device__ __forceinline__ void add_row(const Table64 &t, int64_t k, const int64_t *vals, uint64_t i,
-                                        uint32_t *status) {
+// One row (key k, value v when has_v) into the global table.
+__device__ __forceinline__ void add_kv(const Table64 &t, int64_t k, int64_t v, bool has_v, uint32_t *status) {
   const int64_t s = slot_of(t, k, status);
   if (s < 0) return;
   atomicAdd(&t.cnt[s], 1ull);
-  if (vals) {
-    const int64_t v = __ldcs(vals + i);
+  if (has_v) {
     atomicAdd(&t.sum[s], (unsigned long long)v);
     const unsigned long long emx = (unsigned long long)v ^ kFlip64, emn = ~emx;
     if (emn > *(volatile unsigned long long *)&t.mn[s]) atomicMax(&t.mn[s], emn);
     if (emx > *(volatile unsigned long long *)&t.mx[s]) atomicMax(&t.mx[s], emx);
   }
+}
+
+__device__ __forceinline__ void add_row(const Table64 &t, int64_t k, const int64_t *vals, uint64_t i,
+                                        uint32_t *status) {
+  add_kv(t, k, vals ? __ldcs(vals + i) : 0, vals != nullptr, status);
 }
 
 // Every row into its group (vals null: counts only).
@@ -98,6 +104,214 @@ __global__ void __launch_bounds__(kThreads)
   const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
   for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += stride)
     add_row(t, __ldcs(keys + i), vals, i, status);
+}
+
+// ---------------------------------------------------------------------------
+// On-chip level for few groups (expected groups <= kL1MaxGroups): one table
+// per CTA in shared memory, updated with 32-bit reductions only (64-bit
+// shared atomics have no native form): the count, and the value as four
+// 16-bit chunk sums (SUM = sum of chunk_i << 16 i, modulo 2^64 like int64
+// addition), exact while a slot takes at most kL1Limit rows between flushes.
+// The CTA keeps a bound on every slot's count and moves slots above kL1Hot
+// rows to the global table before the bound could pass kL1Limit.  Min and
+// max keep 64-bit encodings whose (emulated) atomics are issued only when a
+// value improves the stored extreme.  The global table is level 2.
+constexpr int kL1Threads = 512;
+constexpr int kL1Warps = kL1Threads / 32;
+constexpr uint64_t kL1MaxGroups = 2048;
+constexpr uint32_t kL1MaxSlots = 4096;
+constexpr uint32_t kL1Chunk = 32768;                 // rows per item (one bound check each)
+constexpr uint32_t kL1Limit = 65535;                 // rows a slot may take between flushes
+constexpr uint32_t kL1Hot = kL1Limit - kL1Chunk;     // slots above go to level 2 at a check
+constexpr int kL1Probe = 32;
+constexpr uint32_t kL1SlotBytes = 8 + 16 + 4 + 16;  // key, {min', max'}, count, 4 chunk sums
+
+__device__ __forceinline__ uint32_t s_addr(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+__device__ __forceinline__ unsigned long long s_ld64(uint32_t a) {
+  unsigned long long r;
+  asm volatile("ld.volatile.shared.u64 %0, [%1];" : "=l"(r) : "r"(a) : "memory");
+  return r;
+}
+__device__ __forceinline__ uint32_t s_ld32(uint32_t a) {
+  uint32_t r;
+  asm volatile("ld.volatile.shared.u32 %0, [%1];" : "=r"(r) : "r"(a) : "memory");
+  return r;
+}
+__device__ __forceinline__ ulonglong2 s_ld128(uint32_t a) {
+  ulonglong2 r;
+  asm volatile("ld.volatile.shared.v2.u64 {%0, %1}, [%2];" : "=l"(r.x), "=l"(r.y) : "r"(a) : "memory");
+  return r;
+}
+__device__ __forceinline__ void s_st64(uint32_t a, unsigned long long v) {
+  asm volatile("st.shared.u64 [%0], %1;" ::"r"(a), "l"(v) : "memory");
+}
+__device__ __forceinline__ void s_st32(uint32_t a, uint32_t v) {
+  asm volatile("st.shared.u32 [%0], %1;" ::"r"(a), "r"(v) : "memory");
+}
+__device__ __forceinline__ unsigned long long s_cas64(uint32_t a, unsigned long long c, unsigned long long v) {
+  unsigned long long r;
+  asm volatile("atom.shared.cas.b64 %0, [%1], %2, %3;" : "=l"(r) : "r"(a), "l"(c), "l"(v) : "memory");
+  return r;
+}
+__device__ __forceinline__ void s_red32(uint32_t a, uint32_t v) {
+  asm volatile("red.shared.add.u32 [%0], %1;" ::"r"(a), "r"(v) : "memory");
+}
+__device__ __forceinline__ void s_redmax64(uint32_t a, unsigned long long v) {
+  asm volatile("red.shared.max.u64 [%0], %1;" ::"r"(a), "l"(v) : "memory");
+}
+
+// The table's arrays by shared-state-space address.
+struct L1N {
+  uint32_t key;  // u64 [T]: key ^ 2^63, 0 = empty
+  uint32_t ext;  // u64 [2T]: {min', max'}
+  uint32_t cnt;  // u32 [T]
+  uint32_t sum;  // u32 [4T]: chunk sums of slot i at 16 i
+  uint32_t mask, shift;  // T - 1, 64 - log2 T
+};
+
+__device__ __forceinline__ void l1n_row(const L1N &t, const Table64 &g, int64_t k, int64_t v, bool has_v,
+                                        bool &spill, uint32_t *status) {
+  if (k == INT64_MIN) {  // its stored form is the empty mark
+    add_kv(g, k, v, has_v, status);
+    spill = true;
+    return;
+  }
+  const unsigned long long kk = (unsigned long long)k ^ kFlip64;
+  uint32_t h = (uint32_t)(((uint64_t)k * 0x9E3779B97F4A7C15ull) >> t.shift);
+  for (int step = 0;; ++step) {
+    unsigned long long cur = s_ld64(t.key + 8u * h);
+    if (cur == kk) break;
+    if (cur == 0) {
+      cur = s_cas64(t.key + 8u * h, 0ull, kk);
+      if (cur == 0 || cur == kk) break;
+    }
+    if (step + 1 == kL1Probe) {
+      add_kv(g, k, v, has_v, status);
+      spill = true;
+      return;
+    }
+    h = (h + 1) & t.mask;
+  }
+  s_red32(t.cnt + 4u * h, 1u);
+  if (has_v) {
+    const unsigned long long u = (unsigned long long)v;
+    const uint32_t sa = t.sum + 16u * h;
+    s_red32(sa, (uint32_t)(u & 0xffffu));
+    s_red32(sa + 4, (uint32_t)((u >> 16) & 0xffffu));
+    s_red32(sa + 8, (uint32_t)((u >> 32) & 0xffffu));
+    s_red32(sa + 12, (uint32_t)(u >> 48));
+    const unsigned long long emx = u ^ kFlip64, emn = ~emx;
+    const ulonglong2 e = s_ld128(t.ext + 16u * h);
+    if (emn > e.x) s_redmax64(t.ext + 16u * h, emn);
+    if (emx > e.y) s_redmax64(t.ext + 16u * h + 8, emx);
+  }
+}
+
+// Slot i of level 1 into the global table (and reset its accumulators).
+__device__ __forceinline__ void l1n_flush_slot(const L1N &t, const Table64 &g, uint32_t i, bool has_v,
+                                               uint32_t *status) {
+  const uint32_t c = s_ld32(t.cnt + 4u * i);
+  if (c == 0) return;
+  const int64_t k = (int64_t)(s_ld64(t.key + 8u * i) ^ kFlip64);
+  const int64_t s = slot_of(g, k, status);
+  if (s >= 0) {
+    atomicAdd(&g.cnt[s], (unsigned long long)c);
+    if (has_v) {
+      const uint32_t sa = t.sum + 16u * i;
+      const unsigned long long sum = (unsigned long long)s_ld32(sa) + ((unsigned long long)s_ld32(sa + 4) << 16) +
+                                     ((unsigned long long)s_ld32(sa + 8) << 32) +
+                                     ((unsigned long long)s_ld32(sa + 12) << 48);
+      atomicAdd(&g.sum[s], sum);
+      const ulonglong2 e = s_ld128(t.ext + 16u * i);
+      if (e.x) atomicMax(&g.mn[s], e.x);
+      if (e.y) atomicMax(&g.mx[s], e.y);
+    }
+  }
+  s_st32(t.cnt + 4u * i, 0);
+  for (int j = 0; j < 4; ++j) s_st32(t.sum + 16u * i + 4u * j, 0);
+  s_st64(t.ext + 16u * i, 0);
+  s_st64(t.ext + 16u * i + 8, 0);
+}
+
+// Raw int64 rows in items of kL1Chunk; level 1 persists for the CTA's
+// lifetime and goes to the global table when the CTA finishes.
+__global__ void __launch_bounds__(kL1Threads, 1)
+    k_nest_l1(const int64_t *__restrict__ keys, const int64_t *__restrict__ vals, uint64_t n, uint32_t tslots,
+              Table64 g, unsigned long long *item_ctr, uint32_t *status) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  __shared__ unsigned long long s_item;
+  __shared__ uint32_t s_bound;
+  __shared__ uint32_t s_warp[kL1Warps];
+  const uint32_t T = tslots;
+  const uint32_t base = s_addr(smem);
+  L1N t{base, base + 8u * T, base + 24u * T, base + 28u * T, T - 1, 64u - (uint32_t)__popc(T - 1)};
+  const bool has_v = vals != nullptr;
+  for (uint32_t i = threadIdx.x; i < T; i += kL1Threads) {
+    s_st64(t.key + 8u * i, 0);
+    s_st64(t.ext + 16u * i, 0);
+    s_st64(t.ext + 16u * i + 8, 0);
+    s_st32(t.cnt + 4u * i, 0);
+    for (int j = 0; j < 4; ++j) s_st32(t.sum + 16u * i + 4u * j, 0);
+  }
+  if (threadIdx.x == 0) s_bound = 0;
+  const uint64_t items = (n + kL1Chunk - 1) / kL1Chunk;
+  bool spill = false;
+  for (;;) {
+    __syncthreads();
+    if (threadIdx.x == 0) s_item = atomicAdd(item_ctr, 1ull);
+    __syncthreads();
+    const uint64_t item = s_item;
+    if (item >= items) break;
+    const uint64_t lo = item * kL1Chunk, hi = lo + kL1Chunk < n ? lo + kL1Chunk : n;
+    const uint32_t rows = (uint32_t)(hi - lo);
+    // room for this item's rows: every slot's count stays <= kL1Limit
+    if (s_bound + rows > kL1Limit) {
+      uint32_t mx = 0;
+      for (uint32_t i = threadIdx.x; i < T; i += kL1Threads) {
+        const uint32_t c = s_ld32(t.cnt + 4u * i);
+        if (c > kL1Hot) l1n_flush_slot(t, g, i, has_v, status);
+        else mx = max(mx, c);
+      }
+      mx = __reduce_max_sync(0xffffffffu, mx);
+      if ((threadIdx.x & 31) == 0) s_warp[threadIdx.x >> 5] = mx;
+      __syncthreads();
+      if (threadIdx.x == 0) {
+        uint32_t b = 0;
+        for (int w2 = 0; w2 < kL1Warps; ++w2) b = max(b, s_warp[w2]);
+        s_bound = b + rows;
+      }
+    } else {
+      __syncthreads();
+      if (threadIdx.x == 0) s_bound += rows;
+    }
+    __syncthreads();
+    // 4 rows per thread per step (stride kL1Threads), the next step's loads
+    // issued before this step's rows are applied
+    int64_t nk[4], nv[4];
+    auto load = [&](uint64_t b0) {
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        const uint64_t i = b0 + threadIdx.x + (uint64_t)u * kL1Threads;
+        nk[u] = i < hi ? __ldcs(keys + i) : 0;
+        nv[u] = (i < hi && has_v) ? __ldcs(vals + i) : 0;
+      }
+    };
+    load(lo);
+    for (uint64_t b0 = lo; b0 < hi; b0 += 4 * kL1Threads) {
+      int64_t ck[4], cv[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        ck[u] = nk[u];
+        cv[u] = nv[u];
+      }
+      if (b0 + 4 * kL1Threads < hi) load(b0 + 4 * kL1Threads);
+#pragma unroll
+      for (int u = 0; u < 4; ++u)
+        if (b0 + threadIdx.x + (uint64_t)u * kL1Threads < hi) l1n_row(t, g, ck[u], cv[u], has_v, spill, status);
+    }
+  }
+  __syncthreads();
+  for (uint32_t i = threadIdx.x; i < T; i += kL1Threads) l1n_flush_slot(t, g, i, has_v, status);
 }
 
 // The occupied slots (and INT64_MIN's) to the output; one output
@@ -197,8 +411,24 @@ extern "C" int gbj_nest_i64(gbj_ctx *ctx, const int64_t *d_keys, const int64_t *
   Scratch scratch(ctx, s);
   Table64 t;
   GBJ_TRY(make_table(ctx, scratch, next_pow2(2 * groups), d_vals != nullptr, s, &t));
-  k_nest_build<<<grid_for(ctx, n), kThreads, 0, s>>>(d_keys, d_vals, n, t, ctx->d_status);
-  GBJ_TRY(after_launch(ctx, "k_nest_build", s));
+  if (expected_groups && expected_groups <= kL1MaxGroups) {
+    // few groups: the on-chip level first (tables at 8 x groups)
+    const uint32_t tslots =
+        (uint32_t)std::min<uint64_t>(kL1MaxSlots, std::max<uint64_t>(64, next_pow2(8 * expected_groups)));
+    const size_t smem = (size_t)tslots * kL1SlotBytes;
+    unsigned long long *ctr;
+    GBJ_TRY(scratch.get(1, &ctr));
+    GBJ_CHECK_CUDA(ctx, cudaMemsetAsync(ctr, 0, sizeof(unsigned long long), s));
+    GBJ_CHECK_CUDA(ctx, cudaFuncSetAttribute(k_nest_l1, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    int per_sm = 1;
+    GBJ_CHECK_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_nest_l1, kL1Threads, smem));
+    per_sm = std::max(per_sm, 1);
+    k_nest_l1<<<ctx->sm_count * per_sm, kL1Threads, smem, s>>>(d_keys, d_vals, n, tslots, t, ctr, ctx->d_status);
+    GBJ_TRY(after_launch(ctx, "k_nest_l1", s));
+  } else {
+    k_nest_build<<<grid_for(ctx, n), kThreads, 0, s>>>(d_keys, d_vals, n, t, ctx->d_status);
+    GBJ_TRY(after_launch(ctx, "k_nest_build", s));
+  }
   k_nest_emit<<<grid_for(ctx, t.mask + 2), kThreads, 0, s>>>(
       t, d_vals != nullptr, d_out_keys, d_out_count, d_out_sum, d_out_min, d_out_max, out_capacity,
       reinterpret_cast<unsigned long long *>(d_n_groups), ctx->d_status);

@@ -78,3 +78,15 @@ def test_join_count_i64_parity(ctx, oracle, nr, ns, span):
     ctx.sync()
     assert got == oracle.join_count_i64(r, s)
     assert int(host(ctx.radix_join_count_i64(dev(r[:0]), dev(s)))[0]) == 0
+
+
+def test_nest_i64_hot_groups_wrap(ctx, oracle):
+    """Three keys over 2^24 rows: every CTA's on-chip slots pass the 65535-row
+    bound and move to the global table; values at both int64 extremes."""
+    rng = np.random.default_rng(12)
+    n = (1 << 24) + 3
+    k = np.array([-1, 0, 5], dtype=np.int64)[rng.integers(0, 3, n)]
+    k[rng.integers(0, n, 1000)] = I64.min
+    v = np.where(rng.random(n) < 0.5, I64.max, I64.min).astype(np.int64)
+    v[::7] = -1
+    check_nest(ctx, oracle, k, v, expected_groups=4)
