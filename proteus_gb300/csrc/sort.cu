@@ -9,8 +9,9 @@
 //
 // Each pass: a histogram per 2048-row tile (stored digit-major), one scan
 // over the (digit, tile) counts, and a stable scatter in which a warp ranks
-// its 32 consecutive rows among equal digits with __match_any_sync and the
-// warps of a tile combine their counts in shared memory.
+// its 32 consecutive rows among equal digits (the lanes with the same digit
+// found with one ballot per digit bit -- __match_any_sync costs far more on
+// this part) and the warps of a tile combine their counts in shared memory.
 #include <algorithm>
 
 #include "gbj_internal.cuh"
@@ -63,7 +64,14 @@ __global__ void __launch_bounds__(kSortThreads)
     const bool ok = i < n;
     const uint2 e = ok ? in[i] : make_uint2(0, 0);
     const uint32_t d = ok ? (e.x >> shift) & 0xffu : 256u;  // 256: no row
-    const unsigned peers = __match_any_sync(0xffffffffu, d);
+    // lanes with the same 9-bit value d (256 = no row): one ballot per bit
+    unsigned peers = 0xffffffffu;
+#pragma unroll
+    for (int bit = 0; bit < 9; ++bit) {
+      const bool set = (d >> bit) & 1u;
+      const unsigned bal = __ballot_sync(0xffffffffu, set);
+      peers &= set ? bal : ~bal;
+    }
     const uint32_t rank = __popc(peers & lt);  // equal digits before this lane
     if (ok && rank == 0) wcnt[warp][d] = __popc(peers);
     __syncthreads();
