@@ -1,6 +1,6 @@
 """Benchmark of the GB300 relational hot path.
 
-Default workload (the one the driver runs): radix-partitioned hash join,
+Default workload: radix-partitioned hash join,
 R = 2^27 unique keys, S = 2^29 keys (50% hits, hit keys Zipf theta in
 {0, 0.5, 1.0}), output match count and int64 SUM(R.rowid XOR S.rowid).  One
 step = the three joins (one per theta) over resident device columns.

@@ -34,7 +34,7 @@ typedef enum gbj_status {
   GBJ_ERR_CAPACITY = 3,    /* a table or output buffer was too small         */
   GBJ_ERR_TIMEOUT = 4,     /* a bounded device-side wait gave up             */
   GBJ_ERR_CUDA = 5,        /* a CUDA runtime call failed                     */
-  GBJ_ERR_UNSUPPORTED = 6, /* valid request this build does not implement    */
+  GBJ_ERR_UNSUPPORTED = 6, /* valid request the library does not implement  */
   GBJ_ERR_BUDGET = 7,      /* admission refused: HBM budget exhausted        */
   GBJ_ERR_CANCELLED = 8    /* request cancelled before it ran                */
 } gbj_status;
