@@ -304,7 +304,7 @@ int gbj_join_build(gbj_ctx *ctx, const int32_t *d_keys,
   cudaStream_t s = pick_stream(ctx, stream);
   prof_mark(ctx, s);
   uint64_t slots = next_pow2(2 * (n ? n : 1));
-  if (!hash_bits) {  // an autotuned table size for this build-side size, if any
+  if (!hash_bits) {  // an autotuned table size for build sides of this size, if any
     const int32_t tb = tuned_value(ctx, tune_key("join", n, 0));
     if (tb > 0) hash_bits = tb;
   }
