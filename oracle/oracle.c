@@ -1,7 +1,8 @@
 /*
  * oracle.c -- CPU restatement of chapeiro/proteus's hash-join, group-by and
- * radix-cluster semantics.  TEST INFRASTRUCTURE ONLY: the checker for the
- * CUDA path and the CPU baseline of the benchmark; never part of the product.
+ * radix-cluster semantics.  TEST INFRASTRUCTURE ONLY: the oracle the CUDA
+ * path's results are compared with, and the CPU baseline of the benchmark;
+ * never part of the product.
  * Every function names the reference file:line it restates.
  */
 #define _GNU_SOURCE

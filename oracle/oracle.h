@@ -1,8 +1,8 @@
 /*
  * oracle.h -- CPU restatement of chapeiro/proteus's join / group-by semantics.
  *
- * TEST INFRASTRUCTURE ONLY.  The oracle is the checker that the CUDA path is
- * compared with (bit-exact: every result is integer).  Only the test suite,
+ * TEST INFRASTRUCTURE ONLY.  The CUDA path's results are compared with the
+ * oracle's (bit-exact: every result is integer).  Only the test suite,
  * the smoke check and the benchmark's CPU-baseline leg may load it; the
  * product library never links or calls it.
  *

@@ -1,7 +1,7 @@
 """ctypes wrapper of the oracle (liboracle.so) and of oracle/_ref.
 
-TEST INFRASTRUCTURE ONLY: the checker for the CUDA path and the benchmark's
-CPU-baseline leg.  The product never imports this module.
+TEST INFRASTRUCTURE ONLY: the oracle the CUDA path's results are compared
+with, and the benchmark's CPU-baseline leg.  The product never imports this module.
 """
 from __future__ import annotations
 
