@@ -124,7 +124,9 @@ constexpr uint32_t kL1Chunk = 32768;                 // rows per item (one bound
 constexpr uint32_t kL1Limit = 65535;                 // rows a slot may take between flushes
 constexpr uint32_t kL1Hot = kL1Limit - kL1Chunk;     // slots above go to level 2 at a check
 constexpr int kL1Probe = 32;
-constexpr uint32_t kL1SlotBytes = 8 + 16 + 4 + 16;  // key, {min', max'}, count, 4 chunk sums
+// key and {min', max'} per slot; count and 4 chunk sums per slot and column
+__host__ __device__ constexpr uint32_t l1_slot_bytes(uint32_t rlog) { return 24 + (20u << rlog); }
+constexpr size_t kL1Budget = 200 * 1024;  // shared bytes of the one CTA per SM
 
 __device__ __forceinline__ uint32_t s_addr(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
 __device__ __forceinline__ unsigned long long s_ld64(uint32_t a) {
@@ -161,12 +163,36 @@ __device__ __forceinline__ void s_redmax64(uint32_t a, unsigned long long v) {
 }
 
 // The table's arrays by shared-state-space address.
+// count and chunk sums have 2^rlog columns per slot, column = lane mod 2^rlog,
+// so the reductions of a warp's lanes on one hot slot fall on different
+// addresses and banks; a slot's value is the sum of its columns.
 struct L1N {
   uint32_t key;  // u64 [T]: key ^ 2^63, 0 = empty
   uint32_t ext;  // u64 [2T]: {min', max'}
-  uint32_t cnt;  // u32 [T]
-  uint32_t sum;  // u32 [4T]: chunk sums of slot i at 16 i
+  uint32_t cnt;  // u32 [T << rlog]
+  uint32_t sum;  // u32 [4 (T << rlog)]: the 4 chunk sums of column c at 16 c
   uint32_t mask, shift;  // T - 1, 64 - log2 T
+  uint32_t rlog;
+  __device__ __forceinline__ uint32_t col(uint32_t h) const {
+    return (h << rlog) + ((threadIdx.x & 31) & ((1u << rlog) - 1));
+  }
+  __device__ __forceinline__ uint32_t count(uint32_t i) const {
+    uint32_t c = 0;
+    for (uint32_t r = 0; r < (1u << rlog); ++r) c += s_ld32(cnt + 4u * ((i << rlog) + r));
+    return c;
+  }
+  __device__ __forceinline__ uint32_t chunk(uint32_t i, int j) const {
+    uint32_t c = 0;
+    for (uint32_t r = 0; r < (1u << rlog); ++r) c += s_ld32(sum + 16u * ((i << rlog) + r) + 4u * j);
+    return c;
+  }
+  __device__ __forceinline__ void reset_acc(uint32_t i) const {
+    for (uint32_t r = 0; r < (1u << rlog); ++r) {
+      const uint32_t c = (i << rlog) + r;
+      s_st32(cnt + 4u * c, 0);
+      for (int j = 0; j < 4; ++j) s_st32(sum + 16u * c + 4u * j, 0);
+    }
+  }
 };
 
 __device__ __forceinline__ void l1n_row(const L1N &t, const Table64 &g, int64_t k, int64_t v, bool has_v,
@@ -192,10 +218,11 @@ __device__ __forceinline__ void l1n_row(const L1N &t, const Table64 &g, int64_t 
     }
     h = (h + 1) & t.mask;
   }
-  s_red32(t.cnt + 4u * h, 1u);
+  const uint32_t c = t.col(h);
+  s_red32(t.cnt + 4u * c, 1u);
   if (has_v) {
     const unsigned long long u = (unsigned long long)v;
-    const uint32_t sa = t.sum + 16u * h;
+    const uint32_t sa = t.sum + 16u * c;
     s_red32(sa, (uint32_t)(u & 0xffffu));
     s_red32(sa + 4, (uint32_t)((u >> 16) & 0xffffu));
     s_red32(sa + 8, (uint32_t)((u >> 32) & 0xffffu));
@@ -210,25 +237,23 @@ __device__ __forceinline__ void l1n_row(const L1N &t, const Table64 &g, int64_t 
 // Slot i of level 1 into the global table (and reset its accumulators).
 __device__ __forceinline__ void l1n_flush_slot(const L1N &t, const Table64 &g, uint32_t i, bool has_v,
                                                uint32_t *status) {
-  const uint32_t c = s_ld32(t.cnt + 4u * i);
+  const uint32_t c = t.count(i);
   if (c == 0) return;
   const int64_t k = (int64_t)(s_ld64(t.key + 8u * i) ^ kFlip64);
   const int64_t s = slot_of(g, k, status);
   if (s >= 0) {
     atomicAdd(&g.cnt[s], (unsigned long long)c);
     if (has_v) {
-      const uint32_t sa = t.sum + 16u * i;
-      const unsigned long long sum = (unsigned long long)s_ld32(sa) + ((unsigned long long)s_ld32(sa + 4) << 16) +
-                                     ((unsigned long long)s_ld32(sa + 8) << 32) +
-                                     ((unsigned long long)s_ld32(sa + 12) << 48);
+      const unsigned long long sum = (unsigned long long)t.chunk(i, 0) + ((unsigned long long)t.chunk(i, 1) << 16) +
+                                     ((unsigned long long)t.chunk(i, 2) << 32) +
+                                     ((unsigned long long)t.chunk(i, 3) << 48);
       atomicAdd(&g.sum[s], sum);
       const ulonglong2 e = s_ld128(t.ext + 16u * i);
       if (e.x) atomicMax(&g.mn[s], e.x);
       if (e.y) atomicMax(&g.mx[s], e.y);
     }
   }
-  s_st32(t.cnt + 4u * i, 0);
-  for (int j = 0; j < 4; ++j) s_st32(t.sum + 16u * i + 4u * j, 0);
+  t.reset_acc(i);
   s_st64(t.ext + 16u * i, 0);
   s_st64(t.ext + 16u * i + 8, 0);
 }
@@ -237,21 +262,21 @@ __device__ __forceinline__ void l1n_flush_slot(const L1N &t, const Table64 &g, u
 // lifetime and goes to the global table when the CTA finishes.
 __global__ void __launch_bounds__(kL1Threads, 1)
     k_nest_l1(const int64_t *__restrict__ keys, const int64_t *__restrict__ vals, uint64_t n, uint32_t tslots,
-              Table64 g, unsigned long long *item_ctr, uint32_t *status) {
+              uint32_t rlog, Table64 g, unsigned long long *item_ctr, uint32_t *status) {
   extern __shared__ __align__(16) unsigned char smem[];
   __shared__ unsigned long long s_item;
   __shared__ uint32_t s_bound;
   __shared__ uint32_t s_warp[kL1Warps];
   const uint32_t T = tslots;
   const uint32_t base = s_addr(smem);
-  L1N t{base, base + 8u * T, base + 24u * T, base + 28u * T, T - 1, 64u - (uint32_t)__popc(T - 1)};
+  L1N t{base, base + 8u * T, base + 24u * T, base + 24u * T + ((4u * T) << rlog),
+        T - 1, 64u - (uint32_t)__popc(T - 1), rlog};
   const bool has_v = vals != nullptr;
   for (uint32_t i = threadIdx.x; i < T; i += kL1Threads) {
     s_st64(t.key + 8u * i, 0);
     s_st64(t.ext + 16u * i, 0);
     s_st64(t.ext + 16u * i + 8, 0);
-    s_st32(t.cnt + 4u * i, 0);
-    for (int j = 0; j < 4; ++j) s_st32(t.sum + 16u * i + 4u * j, 0);
+    t.reset_acc(i);
   }
   if (threadIdx.x == 0) s_bound = 0;
   const uint64_t items = (n + kL1Chunk - 1) / kL1Chunk;
@@ -268,7 +293,7 @@ __global__ void __launch_bounds__(kL1Threads, 1)
     if (s_bound + rows > kL1Limit) {
       uint32_t mx = 0;
       for (uint32_t i = threadIdx.x; i < T; i += kL1Threads) {
-        const uint32_t c = s_ld32(t.cnt + 4u * i);
+        const uint32_t c = t.count(i);
         if (c > kL1Hot) l1n_flush_slot(t, g, i, has_v, status);
         else mx = max(mx, c);
       }
@@ -415,7 +440,9 @@ extern "C" int gbj_nest_i64(gbj_ctx *ctx, const int64_t *d_keys, const int64_t *
     // few groups: the on-chip level first (tables at 8 x groups)
     const uint32_t tslots =
         (uint32_t)std::min<uint64_t>(kL1MaxSlots, std::max<uint64_t>(64, next_pow2(8 * expected_groups)));
-    const size_t smem = (size_t)tslots * kL1SlotBytes;
+    uint32_t rlog = 0;  // as many accumulator columns (<= 32) as the budget allows
+    while (rlog < 5 && (size_t)tslots * l1_slot_bytes(rlog + 1) <= kL1Budget) ++rlog;
+    const size_t smem = (size_t)tslots * l1_slot_bytes(rlog);
     unsigned long long *ctr;
     GBJ_TRY(scratch.get(1, &ctr));
     GBJ_CHECK_CUDA(ctx, cudaMemsetAsync(ctr, 0, sizeof(unsigned long long), s));
@@ -423,7 +450,8 @@ extern "C" int gbj_nest_i64(gbj_ctx *ctx, const int64_t *d_keys, const int64_t *
     int per_sm = 1;
     GBJ_CHECK_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_nest_l1, kL1Threads, smem));
     per_sm = std::max(per_sm, 1);
-    k_nest_l1<<<ctx->sm_count * per_sm, kL1Threads, smem, s>>>(d_keys, d_vals, n, tslots, t, ctr, ctx->d_status);
+    k_nest_l1<<<ctx->sm_count * per_sm, kL1Threads, smem, s>>>(d_keys, d_vals, n, tslots, rlog, t, ctr,
+                                                              ctx->d_status);
     GBJ_TRY(after_launch(ctx, "k_nest_l1", s));
   } else {
     k_nest_build<<<grid_for(ctx, n), kThreads, 0, s>>>(d_keys, d_vals, n, t, ctx->d_status);
