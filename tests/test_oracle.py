@@ -222,3 +222,24 @@ def test_nest_i64_aggregates_against_numpy(oracle):
     assert (gs == s.view(np.int64)).all() and (gmn == mn).all() and (gmx == mx).all()
     assert oracle.nest_i64(np.zeros(0, np.int64))[0].size == 0
     assert oracle.join_count_i64(np.zeros(0, np.int64), k) == 0
+
+
+@pytest.mark.parametrize("seed", [1, 2, 3])
+def test_int64_twins_equal_reference_live(oracle, seed):
+    """Fresh seeded int64 inputs (duplicates, keys sharing their low cluster
+    bits, negative and extreme keys): the oracle's RJStepwise count and
+    RadixNest group sizes equal the reference's own, run here."""
+    if oracle.ref_lib() is None and not oracle.build_ref():
+        pytest.skip("reference tree not present (oracle/_ref cannot be built here)")
+    rng = np.random.default_rng(seed)
+    i64 = np.iinfo(np.int64)
+    base = rng.integers(i64.min, i64.max, 3000, dtype=np.int64)
+    base[:40] = (base[:40] >> 14) << 14  # same low 14 bits: one cluster, long chains
+    base[40] = i64.max
+    r = base[rng.integers(0, len(base), 20000)]
+    s = np.concatenate([base[rng.integers(0, len(base), 30000)],
+                        rng.integers(i64.min, i64.max, 5000, dtype=np.int64)])
+    assert oracle.join_count_i64(r, s) == oracle.ref_rj_stepwise_agg(r, s)
+    k, cnt, _, _, _ = oracle.nest_i64(r)
+    assert (cnt == oracle.ref_nest_counts(r, k)).all()
+    assert int(cnt.sum()) == len(r)
