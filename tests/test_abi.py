@@ -34,6 +34,8 @@ def test_binding_covers_header(lib):
     names = declared_symbols()
     unbound = sorted(n for n in names if n not in abi.SIGNATURES)
     assert not unbound, unbound
+    stale = sorted(n for n in abi.SIGNATURES if n not in names)
+    assert not stale, stale
 
 
 def test_ctx_create_without_gpu_fails_cleanly(lib):
