@@ -104,15 +104,13 @@ class RadixJoin:
                             f"S=2^{self.ls} int32 keys (50% hits, Zipf theta 0/0.5/1.0), "
                             f"COUNT + SUM(rowid xor)",
                 "n_build": self.nr, "n_probe": self.ns, "thetas": list(self.THETAS),
-                "hit_rate": 0.5, "l2": "inputs larger than L2 (2 GiB probe keys per join)",
-                "radix_bits": getattr(self, "tuned_bits", None),
-                "radix_bits_from": "fixed" if self.fixed_bits else "autotuner"}
+                "hit_rate": 0.5, "l2": "inputs larger than L2 (2 GiB probe keys per join)"}
 
     def generate(self):
-        from proteus_gb300 import engine
+        import datagen
 
-        self.rk, _ = engine.gen_build_side(SEED, self.nr, payload=False)
-        self.sks = [engine.gen_probe_zipf(SEED + i, self.ns, self.nr, th, 0.5)[0]
+        self.rk, _ = datagen.gen_build_side(SEED, self.nr, payload=False)
+        self.sks = [datagen.gen_probe_zipf(SEED + i, self.ns, self.nr, th, 0.5)[0]
                     for i, th in enumerate(self.THETAS)]
 
     def device(self, ctx):
@@ -210,7 +208,9 @@ class RadixJoin:
         return {"job_hbm_gbs_compulsory": round(comp / (ms / 1e3) / 1e9, 1),
                 "job_frac_compulsory": round(comp / (ms / 1e3) / 1e9 / peak, 4),
                 "build_plus_probe_gtuples_s": round(len(self.THETAS) * (self.nr + self.ns) * steps
-                                                    / (ms / 1e3) / 1e9, 3)}
+                                                    / (ms / 1e3) / 1e9, 3),
+                "radix_bits": self.tuned_bits,
+                "radix_bits_from": "fixed" if self.fixed_bits else "autotuner"}
 
     def cpu(self, threads, sample_log):
         from oracle import oracle as O
@@ -241,10 +241,10 @@ class PlainJoin:
                 "l2": "probe columns (128 MiB) larger than L2"}
 
     def generate(self):
-        from proteus_gb300 import engine
+        import datagen
 
-        self.rk, self.rp = engine.gen_build_side(SEED, self.nr)
-        self.sk, self.sp = engine.gen_probe_uniform(SEED, self.ns, self.nr)
+        self.rk, self.rp = datagen.gen_build_side(SEED, self.nr)
+        self.sk, self.sp = datagen.gen_probe_uniform(SEED, self.ns, self.nr)
 
     def device(self, ctx):
         import torch
@@ -323,9 +323,9 @@ class GroupBy:
                 "l2": "inputs (4 GiB) larger than L2"}
 
     def generate(self):
-        from proteus_gb300 import engine
+        import datagen
 
-        self.k, self.v = engine.gen_groupby(SEED, self.n, self.card, self.theta)
+        self.k, self.v = datagen.gen_groupby(SEED, self.n, self.card, self.theta)
 
     def device(self, ctx):
         import torch
@@ -650,10 +650,9 @@ class Serve:
         torch.cuda.synchronize()
 
     def _order(self, n, salt):
-        from proteus_gb300 import abi
+        import datagen
 
-        lib = abi.load()
-        return [int(lib.gbj_gen_rand(SEED, 0x6000 + salt, i)) % self.nt for i in range(n)]
+        return [int(datagen.load().gbj_gen_rand(SEED, 0x6000 + salt, i)) % self.nt for i in range(n)]
 
     def _submit(self, srv, t, out, tables):
         """Template t's query; with `tables`, against its resident build table."""
@@ -887,12 +886,15 @@ def run_reference(args):
         units += u
         secs += dt
     value = units / secs / getattr(wl, "scale", 1e9)
+    cfg = wl.describe()  # the GPU arm's config, key for key
+    cfg["parallelism"] = f"replicas x{world}"
     line = {
         "impl": "reference", "metric": wl.metric, "value": value, "unit": wl.unit,
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": 1e3 * secs / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": getattr(wl, "dtype", "int32"), "data": "synthetic (seeded generator)",
-        "config": wl.describe(),
+        "config": cfg,
+        "sample": sample,
         "cpu_baseline": {"value": value, "unit": wl.unit, "cores": threads, "kind": "port",
                          "sample": sample},
         "e2e": {"value": value, "unit": wl.unit, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},

@@ -14,6 +14,7 @@
 //                permutation, misses = U{nR+1..2nR}.
 //   groupby    : key = bijection32(g), g = U{0..C-1} or Zipf(theta) rank - 1,
 //                value = U[-2^20, 2^20).
+#include "gbj_datagen.h"
 #include "gbjoin.h"
 
 #include <cmath>

@@ -90,13 +90,19 @@ int gbj_pool_stats(gbj_ctx *ctx, uint64_t *capacity, uint64_t *in_use,
  * with gpu::Monoid update semantics (core/olap/lib/operators/gpu/
  * gmonoids.cpp:122-360).  SUM accumulates in int64, as the reference does
  * after a CastExpression (core/olap/include/olap/expressions/
- * expressions.hpp:1162).  On an empty input COUNT/SUM give 0, MIN gives
- * INT64_MAX and MAX gives INT64_MIN. */
+ * expressions.hpp:1162).  OR and AND are the logical monoids of the
+ * reference's GPU path (LogOrMonoid / LogAndMonoid, gmonoids.cpp:286-290,
+ * 363-376, parsed from "or" / "and" at expression-parser.cpp:790-793): the
+ * operand counts as true when it is not zero and the result is 0 or 1.  On
+ * an empty input COUNT/SUM/OR give 0, AND gives 1, MIN gives INT64_MAX and
+ * MAX gives INT64_MIN. */
 typedef enum gbj_agg_op {
   GBJ_AGG_COUNT = 0,
   GBJ_AGG_SUM = 1,
   GBJ_AGG_MIN = 2,
-  GBJ_AGG_MAX = 3
+  GBJ_AGG_MAX = 3,
+  GBJ_AGG_OR = 4,
+  GBJ_AGG_AND = 5
 } gbj_agg_op;
 
 /* Value a join aggregate reads for one matching (build row, probe row). */
@@ -186,8 +192,9 @@ int gbj_partition(gbj_ctx *ctx, const int32_t *d_keys,
  * then build and probe per partition with the aggregate fused in.  Each side
  * carries ONE 32-bit value into the partitions: its payload if an aggregate
  * reads GBJ_VAL_BUILD/PROBE/PRODUCT, its row position if one reads a rowid
- * operand (mixing both on one side gives GBJ_ERR_UNSUPPORTED).  Work items
- * are sized on the device, so the call never synchronises with the host. */
+ * operand; when one side needs both, both sides carry row positions and
+ * matches read the payloads by row.  Work items are sized on the device, so
+ * the call never synchronises with the host. */
 /* Radix clustering of {int64 key, int64 payload} tuples: the aggregation
  * twins radix_cluster_nopadding / partitionHT of core/platform/lib/util/
  * radix/aggregations/radix-aggr.cpp:82-155,237-259 (agg::tuple_t, KEY_8B).
@@ -220,9 +227,13 @@ int gbj_radix_join_count_i64(gbj_ctx *ctx, const int64_t *d_r_keys, uint64_t nr,
                              const int64_t *d_s_keys, uint64_t ns, int64_t *d_count,
                              void *stream);
 
+/* Every field is honoured or the call fails with GBJ_ERR_UNSUPPORTED: bits
+ * and log_parts in [0, 15]; passes 1 needs bits <= 8 and passes 2 bits >= 2
+ * (with bits unset, a pinned pass count bounds the automatic choice); block
+ * is 0 or the join kernel's 1024 threads. */
 typedef struct gbj_radix_params {
   int32_t bits;       /* radix bits, 0 = autotuned                        */
-  int32_t passes;     /* 1 or 2, 0 = autotuned                            */
+  int32_t passes;     /* 1 or 2, 0 = one pass up to 8 bits, two above     */
   int32_t block;      /* threads per block of the join kernel, 0 = auto   */
   int32_t log_parts;  /* plan field log_parts (reference: 13), 0 = unset  */
 } gbj_radix_params;
@@ -233,6 +244,24 @@ int gbj_radix_join_agg(gbj_ctx *ctx, const int32_t *d_build_keys,
                        const int32_t *d_probe_payload, uint64_t n_probe,
                        const gbj_radix_params *params, const gbj_agg *aggs,
                        int32_t n_aggs, int64_t *d_out, void *stream);
+
+/* The partitioned join with a minor key: GpuPartitionedHashJoinChained built
+ * with build_k_minor / probe_k_minor (core/olap/lib/plan/plan-parser.cpp:
+ * 872-880), which after the key compare of a chain match also requires the
+ * build and probe minor keys to be equal (core/olap/lib/operators/gpu/
+ * gpu-partitioned-hash-join-chained.cpp:1284-1333).  Partitions are on the
+ * (major) key's hash; both sides carry their row positions and a match reads
+ * the minor keys and payloads by row, so any operand mix is allowed.  Both
+ * minor columns are required (GBJ_ERR_INVALID otherwise). */
+int gbj_radix_join_agg_minor(gbj_ctx *ctx, const int32_t *d_build_keys,
+                             const int32_t *d_build_minor,
+                             const int32_t *d_build_payload, uint64_t n_build,
+                             const int32_t *d_probe_keys,
+                             const int32_t *d_probe_minor,
+                             const int32_t *d_probe_payload, uint64_t n_probe,
+                             const gbj_radix_params *params,
+                             const gbj_agg *aggs, int32_t n_aggs,
+                             int64_t *d_out, void *stream);
 
 /* ------------------------------------------------------ hash group-by */
 /* GpuHashGroupByChained (core/olap/lib/operators/gpu/
@@ -608,7 +637,8 @@ void gbj_result_destroy(gbj_result *r);
  * Runs on `stream` (NULL = the legacy default stream) of the current device.
  * The first call on a device looks up the array's device address for that
  * device (cudaGetSymbolAddress); make that first call before any stream
- * capture.  All calls share the one array and it keeps the previous call's
+ * capture.  After cudaDeviceReset the next call on that device looks the
+ * address up again, in the new context.  All calls share the one array and it keeps the previous call's
  * contents: each call clears the part it uses first, and calls whose work
  * overlaps on the GPU (other streams, other host threads) race on the table,
  * so the caller must order them.  On failure the message is available from
@@ -621,40 +651,6 @@ int gbj_join_agg_noalloc(const int32_t *d_build_keys,
                          const int32_t *d_probe_payload, uint64_t n_probe,
                          const gbj_agg *aggs, int32_t n_aggs, int64_t *d_out,
                          void *stream);
-
-/* ------------------------------------------ seeded synthetic input (host) */
-/* Deterministic, thread-parallel generators for the workload shapes; pure
- * functions of (seed, row), identical on every host.  threads <= 0 uses all
- * hardware threads. */
-int gbj_gen_build_side(uint64_t seed, uint64_t n, int32_t *h_keys,
-                       int32_t *h_payload, int threads);
-int gbj_gen_probe_uniform(uint64_t seed, uint64_t n, uint64_t n_build,
-                          int32_t *h_keys, int32_t *h_payload, int threads);
-int gbj_gen_probe_zipf(uint64_t seed, uint64_t n, uint64_t n_build,
-                       double theta, double hit_rate, int32_t *h_keys,
-                       int32_t *h_payload, int threads);
-int gbj_gen_groupby(uint64_t seed, uint64_t n, uint64_t cardinality,
-                    double theta, int32_t *h_keys, int32_t *h_values,
-                    int threads);
-/* out[i] = lo + a uniform draw from {0 .. hi - lo} of column stream
- * `stream` (independent streams for independent columns). */
-int gbj_gen_uniform_i32(uint64_t seed, uint64_t stream, uint64_t n,
-                        int32_t lo, int32_t hi, int32_t *h_out, int threads);
-/* One served join + group-by query (gbj_serve_query inputs): build keys a
- * seeded permutation of 1..n_build, build groups `cardinality` distinct
- * int32 values, probe keys hitting a uniform build key with probability
- * match_rate (else a key above every build key), probe values U[0, 1000). */
-int gbj_gen_serve_query(uint64_t seed, uint64_t n_build, uint64_t n_probe,
-                        double match_rate, uint64_t cardinality,
-                        int32_t *h_build_keys, int32_t *h_build_group,
-                        int32_t *h_probe_keys, int32_t *h_probe_vals,
-                        int threads);
-uint64_t gbj_gen_rand(uint64_t seed, uint64_t stream, uint64_t i);
-uint64_t gbj_gen_perm(uint64_t seed, uint64_t stream, uint64_t n, uint64_t i);
-uint64_t gbj_gen_zipf(uint64_t seed, uint64_t stream, uint64_t n, double theta,
-                      uint64_t i);
-double gbj_gen_det_log(double x);
-double gbj_gen_det_exp(double x);
 
 #ifdef __cplusplus
 }

@@ -14,7 +14,7 @@
 #include <string.h>
 
 /* Codes of gbjoin.h (kept numerically identical). */
-enum { A_COUNT = 0, A_SUM = 1, A_MIN = 2, A_MAX = 3 };
+enum { A_COUNT = 0, A_SUM = 1, A_MIN = 2, A_MAX = 3, A_OR = 4, A_AND = 5 };
 enum {
   V_ONE = 0,
   V_BUILD = 1,
@@ -155,12 +155,17 @@ typedef struct {
   int64_t v[8];
 } acc8;
 
+/* Identities: MIN/MAX of nothing as int64 extremes; the logical AND of
+ * nothing is true (LogAndMonoid, gmonoids.cpp:286-290; its atomic form only
+ * ever stores false, :292-321), the logical OR of nothing false. */
 static void acc_init(acc8 *a, const int32_t *ops, int n_aggs) {
   for (int j = 0; j < n_aggs; ++j) {
     if (ops[j] == A_MIN)
       a->v[j] = INT64_MAX;
     else if (ops[j] == A_MAX)
       a->v[j] = INT64_MIN;
+    else if (ops[j] == A_AND)
+      a->v[j] = 1;
     else
       a->v[j] = 0;
   }
@@ -192,6 +197,10 @@ static inline void acc_update(acc8 *a, const int32_t *ops,
       case A_SUM: a->v[j] += x; break;
       case A_MIN: if (x < a->v[j]) a->v[j] = x; break;
       case A_MAX: if (x > a->v[j]) a->v[j] = x; break;
+      /* LogOrMonoid / LogAndMonoid (gmonoids.cpp:286-290, 363-376): the
+       * operand is a truth value, any non-zero value is true */
+      case A_OR: a->v[j] = a->v[j] | (x != 0); break;
+      case A_AND: a->v[j] = a->v[j] & (x != 0); break;
     }
   }
 }
@@ -203,6 +212,10 @@ static void acc_merge(acc8 *dst, const acc8 *src, const int32_t *ops,
       if (src->v[j] < dst->v[j]) dst->v[j] = src->v[j];
     } else if (ops[j] == A_MAX) {
       if (src->v[j] > dst->v[j]) dst->v[j] = src->v[j];
+    } else if (ops[j] == A_OR) {
+      dst->v[j] |= src->v[j];
+    } else if (ops[j] == A_AND) {
+      dst->v[j] &= src->v[j];
     } else {
       dst->v[j] += src->v[j];
     }
@@ -212,7 +225,7 @@ static void acc_merge(acc8 *dst, const acc8 *src, const int32_t *ops,
 static int check_aggs(const int32_t *ops, const int32_t *operands, int n) {
   if (n < 0 || n > 8 || (n && (!ops || !operands))) return -1;
   for (int j = 0; j < n; ++j) {
-    if (ops[j] < A_COUNT || ops[j] > A_MAX) return -1;
+    if (ops[j] < A_COUNT || ops[j] > A_AND) return -1;
     if (operands[j] < V_ONE || operands[j] > V_BUILD_KEY) return -1;
   }
   return 0;
@@ -493,6 +506,10 @@ typedef struct {
   volatile int64_t *next_part;
   const int32_t *ops, *operands;
   int n_aggs;
+  /* rv / sv carry row positions; the minor keys and payloads are read
+   * through them (orc_radix_join_agg_minor) */
+  int by_rows;
+  const int32_t *minor_r, *minor_s, *pay_r, *pay_s;
   acc8 acc;
 } rjoin_arg;
 
@@ -527,9 +544,18 @@ static void *rjoin_worker(void *p) {
       uint32_t idx = (orc_hashd(k) >> a->bits) & (N - 1);
       for (int32_t hit = bucket[idx]; hit > 0; hit = next[hit - 1]) {
         uint64_t r = r0 + (uint64_t)(hit - 1);
-        if (a->rk[r] == k)
+        if (a->rk[r] != k) continue;
+        if (a->by_rows) {
+          const int32_t br = a->rv[r], pr = a->sv[j];
+          /* gpu-partitioned-hash-join-chained.cpp:1284-1333: after the key
+           * compare, the build and probe minor keys must be equal too */
+          if (a->minor_r && a->minor_r[br] != a->minor_s[pr]) continue;
+          acc_update(&a->acc, a->ops, a->operands, a->n_aggs, k,
+                     a->pay_r ? a->pay_r[br] : 0, a->pay_s ? a->pay_s[pr] : 0, br, pr);
+        } else {
           acc_update(&a->acc, a->ops, a->operands, a->n_aggs, k, a->rv[r],
                      a->sv[j], a->rv[r], a->sv[j]);
+        }
       }
     }
   }
@@ -548,11 +574,13 @@ static int side_carries_rowid(const int32_t *operands, int n, int build) {
   return 0;
 }
 
-int orc_radix_join_agg(const int32_t *keys_r, const int32_t *pay_r,
-                       uint64_t nr, const int32_t *keys_s,
-                       const int32_t *pay_s, uint64_t ns, int32_t bits,
-                       const int32_t *ops, const int32_t *operands,
-                       int32_t n_aggs, int64_t *out, int threads) {
+static int radix_join_impl(const int32_t *keys_r, const int32_t *minor_r,
+                           const int32_t *pay_r, uint64_t nr,
+                           const int32_t *keys_s, const int32_t *minor_s,
+                           const int32_t *pay_s, uint64_t ns, int32_t bits,
+                           int by_rows, const int32_t *ops,
+                           const int32_t *operands, int32_t n_aggs,
+                           int64_t *out, int threads) {
   if (check_aggs(ops, operands, n_aggs) || !out) return -1;
   if (threads < 1) threads = 1;
   if (bits <= 0) {
@@ -569,8 +597,8 @@ int orc_radix_join_agg(const int32_t *keys_r, const int32_t *pay_r,
   /* the value carried through the partitions is the rowid when an
    * aggregate reads one, else the payload (operand_value then reads it as
    * "bval"/"pval" and as the rowid consistently). */
-  int r_rowid = side_carries_rowid(operands, n_aggs, 1);
-  int s_rowid = side_carries_rowid(operands, n_aggs, 0);
+  int r_rowid = by_rows || side_carries_rowid(operands, n_aggs, 1);
+  int s_rowid = by_rows || side_carries_rowid(operands, n_aggs, 0);
   parallel_partition(keys_r, pay_r, nr, bits, threads, r_rowid, rk, rv, ro);
   parallel_partition(keys_s, pay_s, ns, bits, threads, s_rowid, sk, sv, so);
   volatile int64_t next_part = 0;
@@ -590,6 +618,11 @@ int orc_radix_join_agg(const int32_t *keys_r, const int32_t *pay_r,
     a->ops = ops;
     a->operands = operands;
     a->n_aggs = n_aggs;
+    a->by_rows = by_rows;
+    a->minor_r = minor_r;
+    a->minor_s = minor_s;
+    a->pay_r = pay_r;
+    a->pay_s = pay_s;
     acc_init(&a->acc, ops, n_aggs);
     pthread_create(&th[t], 0, rjoin_worker, a);
   }
@@ -609,6 +642,33 @@ int orc_radix_join_agg(const int32_t *keys_r, const int32_t *pay_r,
   free(ro);
   free(so);
   return 0;
+}
+
+int orc_radix_join_agg(const int32_t *keys_r, const int32_t *pay_r,
+                       uint64_t nr, const int32_t *keys_s,
+                       const int32_t *pay_s, uint64_t ns, int32_t bits,
+                       const int32_t *ops, const int32_t *operands,
+                       int32_t n_aggs, int64_t *out, int threads) {
+  return radix_join_impl(keys_r, 0, pay_r, nr, keys_s, 0, pay_s, ns, bits, 0,
+                         ops, operands, n_aggs, out, threads);
+}
+
+/* GpuPartitionedHashJoinChained with build_k_minor / probe_k_minor
+ * (plan-parser.cpp:872-880; the check at
+ * gpu-partitioned-hash-join-chained.cpp:1284-1333): a pair matches when the
+ * keys are equal and the minor keys are equal.  Both sides carry their row
+ * positions through the partitions; minor keys and payloads are read by
+ * row.  minor_r / minor_s: both given, or both 0 (then this is the plain
+ * partitioned join). */
+int orc_radix_join_agg_minor(const int32_t *keys_r, const int32_t *minor_r,
+                             const int32_t *pay_r, uint64_t nr,
+                             const int32_t *keys_s, const int32_t *minor_s,
+                             const int32_t *pay_s, uint64_t ns, int32_t bits,
+                             const int32_t *ops, const int32_t *operands,
+                             int32_t n_aggs, int64_t *out, int threads) {
+  if (!minor_r != !minor_s) return -1;
+  return radix_join_impl(keys_r, minor_r, pay_r, nr, keys_s, minor_s, pay_s, ns,
+                         bits, 1, ops, operands, n_aggs, out, threads);
 }
 
 /* ------------------------------------------------------------ group-by */

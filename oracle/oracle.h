@@ -90,6 +90,15 @@ int orc_radix_join_agg(const int32_t *keys_r, const int32_t *pay_r,
                        const int32_t *pay_s, uint64_t ns, int32_t bits,
                        const int32_t *ops, const int32_t *operands,
                        int32_t n_aggs, int64_t *out, int threads);
+/* Composite-key form (build_k_minor / probe_k_minor of the reference's
+ * partitioned join): a pair also needs equal minor keys; minor columns both
+ * given or both 0.  Row ids and payloads are read by row position. */
+int orc_radix_join_agg_minor(const int32_t *keys_r, const int32_t *minor_r,
+                             const int32_t *pay_r, uint64_t nr,
+                             const int32_t *keys_s, const int32_t *minor_s,
+                             const int32_t *pay_s, uint64_t ns, int32_t bits,
+                             const int32_t *ops, const int32_t *operands,
+                             int32_t n_aggs, int64_t *out, int threads);
 
 /* ---- chained hash group-by (core/olap/lib/operators/
  *      hash-group-by-chained.cpp:267-633 build, :638-853 emit scan) ---- */

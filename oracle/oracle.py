@@ -31,9 +31,11 @@ def build():
     subprocess.run(["make", "-s", "-C", HERE, "all"], check=True)
 
 
-def build_ref(ref_root="/root/reference"):
-    """Compiles oracle/_ref from the reference sources, when they are present."""
-    if not os.path.isdir(os.path.join(ref_root, "core", "platform")):
+def build_ref(ref_root=None):
+    """Compiles oracle/_ref from the reference sources (the tree named by
+    `ref_root` or $PROTEUS_REF), when they are present."""
+    ref_root = ref_root or os.environ.get("PROTEUS_REF")
+    if not ref_root or not os.path.isdir(os.path.join(ref_root, "core", "platform")):
         return False
     subprocess.run(["make", "-s", "-C", HERE, "ref", f"REF={ref_root}"], check=True)
     return True
@@ -64,6 +66,9 @@ def lib():
         L.orc_partition_ht_counts.argtypes = [vp, u64, vp]
         L.orc_radix_join_agg.restype = C.c_int
         L.orc_radix_join_agg.argtypes = [vp, vp, u64, vp, vp, u64, i32, vp, vp, i32, vp, C.c_int]
+        L.orc_radix_join_agg_minor.restype = C.c_int
+        L.orc_radix_join_agg_minor.argtypes = [vp, vp, vp, u64, vp, vp, vp, u64, i32, vp, vp, i32,
+                                               vp, C.c_int]
         L.orc_groupby.restype = i64
         L.orc_groupby.argtypes = [vp, vp, u64, i32, C.c_int, vp, vp, vp, vp, vp, u64]
         L.orc_reduce.restype = None
@@ -184,6 +189,21 @@ def radix_join_agg(bkeys, bpay, pkeys, ppay, aggs, bits=0, threads=1):
     out = np.zeros(len(aggs), dtype=np.int64)
     rc = L.orc_radix_join_agg(_p(bkeys), _p(bpay), len(bkeys), _p(pkeys), _p(ppay), len(pkeys),
                               bits, _p(ops), _p(opd), len(aggs), _p(out), threads)
+    assert rc == 0
+    return [int(x) for x in out]
+
+
+def radix_join_agg_minor(bkeys, bminor, bpay, pkeys, pminor, ppay, aggs, bits=0, threads=1):
+    """Partitioned join whose pairs also need equal minor keys (both minor
+    columns given, or both None); payloads and row ids read by row."""
+    L = lib()
+    bkeys, bminor, bpay = _i32(bkeys), _i32(bminor), _i32(bpay)
+    pkeys, pminor, ppay = _i32(pkeys), _i32(pminor), _i32(ppay)
+    ops, opd = _aggs(aggs)
+    out = np.zeros(len(aggs), dtype=np.int64)
+    rc = L.orc_radix_join_agg_minor(_p(bkeys), _p(bminor), _p(bpay), len(bkeys), _p(pkeys),
+                                    _p(pminor), _p(ppay), len(pkeys), bits, _p(ops), _p(opd),
+                                    len(aggs), _p(out), threads)
     assert rc == 0
     return [int(x) for x in out]
 

@@ -17,7 +17,7 @@ OK, ERR_INVALID, ERR_OOM, ERR_CAPACITY, ERR_TIMEOUT, ERR_CUDA, ERR_UNSUPPORTED, 
 STATUS_NAMES = {0: "OK", 1: "INVALID", 2: "OOM", 3: "CAPACITY", 4: "TIMEOUT", 5: "CUDA",
                 6: "UNSUPPORTED", 7: "BUDGET", 8: "CANCELLED"}
 
-AGG_COUNT, AGG_SUM, AGG_MIN, AGG_MAX = range(4)
+AGG_COUNT, AGG_SUM, AGG_MIN, AGG_MAX, AGG_OR, AGG_AND = range(6)
 (VAL_ONE, VAL_BUILD, VAL_PROBE, VAL_PRODUCT, VAL_BUILD_ROWID, VAL_PROBE_ROWID,
  VAL_ROWID_XOR, VAL_BUILD_KEY) = range(8)
 DIGIT_KEY, DIGIT_HASH = 0, 1
@@ -107,16 +107,14 @@ SIGNATURES = {
     "gbj_partition": (C.c_int, [vp, vp, vp, u64, i32, i32, i32, vp, vp, vp, vp]),
     "gbj_radix_join_agg": (C.c_int, [vp, vp, vp, u64, vp, vp, u64, P(RadixParams), P(Agg), i32,
                                      vp, vp]),
+    "gbj_radix_join_agg_minor": (C.c_int, [vp, vp, vp, vp, u64, vp, vp, vp, u64, P(RadixParams),
+                                           P(Agg), i32, vp, vp]),
     "gbj_groupby": (C.c_int, [vp, vp, vp, u64, P(GroupbyParams), vp, vp, vp, vp, vp, u64, vp,
                               vp]),
     "gbj_reduce": (C.c_int, [vp, vp, vp, u64, P(Agg), i32, vp, vp]),
     "gbj_gather": (C.c_int, [vp, vp, vp, u64, vp, vp]),
     "gbj_select_range": (C.c_int, [vp, vp, u64, i32, i32, vp, vp, vp]),
     "gbj_join_agg_noalloc": (C.c_int, [vp, vp, u64, vp, vp, u64, P(Agg), i32, vp, vp]),
-    "gbj_gen_build_side": (C.c_int, [u64, u64, vp, vp, C.c_int]),
-    "gbj_gen_probe_uniform": (C.c_int, [u64, u64, u64, vp, vp, C.c_int]),
-    "gbj_gen_probe_zipf": (C.c_int, [u64, u64, u64, dbl, dbl, vp, vp, C.c_int]),
-    "gbj_gen_groupby": (C.c_int, [u64, u64, u64, dbl, vp, vp, C.c_int]),
     "gbj_star_plan_create": (C.c_int, [vp, P(StarFact), P(StarDim), P(vp)]),
     "gbj_star_run": (C.c_int, [vp, P(StarQuery), i32, P(StarOut), i32, vp]),
     "gbj_star_plan_destroy": (None, [vp]),
@@ -155,13 +153,6 @@ SIGNATURES = {
     "gbj_result_name": (C.c_char_p, [vp, i32]),
     "gbj_result_column": (C.c_int, [vp, i32, vp]),
     "gbj_result_destroy": (None, [vp]),
-    "gbj_gen_serve_query": (C.c_int, [u64, u64, u64, dbl, u64, vp, vp, vp, vp, C.c_int]),
-    "gbj_gen_uniform_i32": (C.c_int, [u64, u64, u64, i32, i32, vp, C.c_int]),
-    "gbj_gen_rand": (u64, [u64, u64, u64]),
-    "gbj_gen_perm": (u64, [u64, u64, u64, u64]),
-    "gbj_gen_zipf": (u64, [u64, u64, u64, dbl, u64]),
-    "gbj_gen_det_log": (dbl, [dbl]),
-    "gbj_gen_det_exp": (dbl, [dbl]),
 }
 
 _lib = None

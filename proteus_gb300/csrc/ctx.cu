@@ -194,7 +194,7 @@ int validate_aggs(gbj_ctx *ctx, const gbj_agg *aggs, int32_t n_aggs) {
   if (n_aggs < 1 || n_aggs > GBJ_MAX_AGGS || !aggs)
     return set_error(ctx, GBJ_ERR_INVALID, "n_aggs must be in [1, 8]");
   for (int j = 0; j < n_aggs; ++j) {
-    if (aggs[j].op < GBJ_AGG_COUNT || aggs[j].op > GBJ_AGG_MAX)
+    if (aggs[j].op < GBJ_AGG_COUNT || aggs[j].op > GBJ_AGG_AND)
       return set_error(ctx, GBJ_ERR_INVALID, "bad aggregate op");
     if (aggs[j].operand < GBJ_VAL_ONE || aggs[j].operand > GBJ_VAL_BUILD_KEY)
       return set_error(ctx, GBJ_ERR_INVALID, "bad aggregate operand");

@@ -184,8 +184,11 @@ __device__ __forceinline__ int64_t operand_value(int operand, int32_t key,
   }
 }
 
+// Identity of each aggregate: 0 for COUNT / SUM / OR, the int64 extremes for
+// MIN / MAX, true (1) for AND.
 __device__ __forceinline__ int64_t agg_identity(int op) {
-  return op == GBJ_AGG_MIN ? INT64_MAX : (op == GBJ_AGG_MAX ? INT64_MIN : 0);
+  return op == GBJ_AGG_MIN ? INT64_MAX
+                           : (op == GBJ_AGG_MAX ? INT64_MIN : (op == GBJ_AGG_AND ? 1 : 0));
 }
 
 struct Acc {
@@ -214,7 +217,10 @@ struct Acc {
         const int op = s.op[j];
         const int64_t add = v[j] + (op == GBJ_AGG_COUNT ? 1 : x);
         const int64_t mm = op == GBJ_AGG_MIN ? (x < v[j] ? x : v[j]) : (x > v[j] ? x : v[j]);
-        v[j] = op <= GBJ_AGG_SUM ? add : mm;
+        // OR / AND are logical: the operand is true when it is not zero
+        const int64_t tv = (int64_t)(x != 0);
+        const int64_t lg = op == GBJ_AGG_OR ? (v[j] | tv) : (v[j] & tv);
+        v[j] = op <= GBJ_AGG_SUM ? add : (op <= GBJ_AGG_MAX ? mm : lg);
       }
     }
   }
@@ -223,6 +229,8 @@ struct Acc {
 __device__ __forceinline__ int64_t combine(int op, int64_t a, int64_t b) {
   if (op == GBJ_AGG_MIN) return a < b ? a : b;
   if (op == GBJ_AGG_MAX) return a > b ? a : b;
+  if (op == GBJ_AGG_OR) return a | b;
+  if (op == GBJ_AGG_AND) return a & b;
   return a + b;
 }
 
@@ -251,6 +259,10 @@ __device__ __forceinline__ void block_flush(const gbj::AggSpec &s, Acc &a,
       if (x != INT64_MAX) atomicMin((long long *)&d_out[j], (long long)x);
     } else if (s.op[j] == GBJ_AGG_MAX) {
       if (x != INT64_MIN) atomicMax((long long *)&d_out[j], (long long)x);
+    } else if (s.op[j] == GBJ_AGG_OR) {
+      if (x) atomicOr((unsigned long long *)&d_out[j], 1ull);
+    } else if (s.op[j] == GBJ_AGG_AND) {
+      if (!x) atomicAnd((unsigned long long *)&d_out[j], 0ull);
     } else {
       atomicAdd((unsigned long long *)&d_out[j], (unsigned long long)x);
     }

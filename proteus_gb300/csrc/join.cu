@@ -31,7 +31,9 @@ __device__ __forceinline__ int32_t slot_key(uint64_t e) { return (int32_t)(uint3
 __device__ __forceinline__ uint32_t slot_row(uint64_t e) { return (uint32_t)(e >> 32) - 1; }
 
 // meta[0] = 1 once a duplicate build key was seen (probes may then not stop
-// at the first match).
+// at the first match).  A row that finds no free slot latches
+// GBJ_DEV_CAPACITY into *status (status may be null where the table has 2n
+// slots and cannot fill).
 __global__ void __launch_bounds__(kThreads)
     k_join_build(const int32_t *__restrict__ keys, uint64_t n,
                  uint64_t *__restrict__ slots, uint64_t mask,
@@ -55,7 +57,7 @@ __global__ void __launch_bounds__(kThreads)
       h = (h + 1) & mask;
     }
     if (dup) meta[0] = 1;
-    if (!placed) gbjd::latch(status, GBJ_DEV_CAPACITY);
+    if (!placed && status) gbjd::latch(status, GBJ_DEV_CAPACITY);
   }
 }
 
@@ -256,7 +258,8 @@ void launch_probe(int sm_count, const int32_t *keys, const int32_t *pay, uint64_
 // Hash table of gbj_join_agg_noalloc: a fixed array in the module's device
 // memory, so that entry point never allocates.  Slots for build sides of up
 // to GBJ_NOALLOC_MAX_BUILD rows at load factor 1/2, then 32 words of table
-// metadata (duplicate flag) and status.
+// metadata (the duplicate-key flag).  The table always has at least 2n
+// slots, so its build cannot run out of room and needs no status word.
 constexpr uint64_t kNoAllocSlots = 2ull * GBJ_NOALLOC_MAX_BUILD;
 static __device__ __align__(256) uint64_t g_noalloc_scratch[kNoAllocSlots + 32];
 
@@ -267,13 +270,42 @@ __global__ void k_noalloc_init_out(gbj::AggSpec s, int64_t *out) {
 
 // Per-device set-up of the allocation-free entry point: the device address
 // of g_noalloc_scratch (host code cannot use the symbol itself) and the SM
-// count, looked up once per device with that device current.
+// count, looked up once per device and CUDA context with that device current.
+// The context is part of the key because cudaDeviceReset ends the context
+// that address belongs to; the next call then looks it up again.
 struct NoAllocDevice {
   uint64_t *scratch = nullptr;
   int sm_count = 0;
 };
 std::mutex g_noalloc_mu;
-std::unordered_map<int, NoAllocDevice> g_noalloc_devices;
+std::map<std::pair<int, unsigned long long>, NoAllocDevice> g_noalloc_devices;
+
+// Unique id of the calling thread's current CUDA context (0 when there is
+// none yet), through the driver entry points the runtime hands out, so the
+// library needs no link against the driver library.
+unsigned long long current_context_id() {
+  typedef int (*GetCurrent)(void **);
+  typedef int (*GetId)(void *, unsigned long long *);
+  static GetCurrent get_current = nullptr;
+  static GetId get_id = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    void *f = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      get_current = reinterpret_cast<GetCurrent>(f);
+    f = nullptr;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      get_id = reinterpret_cast<GetId>(f);
+    (void)cudaGetLastError();
+  });
+  void *c = nullptr;
+  unsigned long long id = 0;
+  if (!get_current || !get_id || get_current(&c) != 0 || !c || get_id(c, &id) != 0) return 0;
+  return id;
+}
 thread_local std::string g_noalloc_error;
 
 int noalloc_fail(int code, const char *msg) {
@@ -451,7 +483,7 @@ int gbj_join_agg_noalloc(const int32_t *d_build_keys, const int32_t *d_build_pay
   if (n_probe >= (1ULL << 32))
     return noalloc_fail(GBJ_ERR_INVALID, "join_agg_noalloc: probe side must have < 2^32 rows");
   for (int j = 0; j < n_aggs; ++j) {
-    if (aggs[j].op < GBJ_AGG_COUNT || aggs[j].op > GBJ_AGG_MAX || aggs[j].operand < GBJ_VAL_ONE ||
+    if (aggs[j].op < GBJ_AGG_COUNT || aggs[j].op > GBJ_AGG_AND || aggs[j].operand < GBJ_VAL_ONE ||
         aggs[j].operand > GBJ_VAL_BUILD_KEY)
       return noalloc_fail(GBJ_ERR_INVALID, "join_agg_noalloc: bad aggregate");
     const int o = aggs[j].operand;
@@ -468,9 +500,10 @@ int gbj_join_agg_noalloc(const int32_t *d_build_keys, const int32_t *d_build_pay
   NoAllocDevice d;
   {
     std::lock_guard<std::mutex> g(g_noalloc_mu);
-    auto it = g_noalloc_devices.find(dev);
+    auto it = g_noalloc_devices.find({dev, current_context_id()});
     if (it == g_noalloc_devices.end()) {
-      // first call on this device: resolve the array's device address
+      // first call on this device in this context: resolve the array's
+      // device address (this also makes the runtime's context current)
       void *ptr = nullptr;
       cudaError_t e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
       if (e != cudaSuccess || !ptr) {
@@ -483,7 +516,7 @@ int gbj_join_agg_noalloc(const int32_t *d_build_keys, const int32_t *d_build_pay
         (void)cudaGetLastError();
         return noalloc_fail(GBJ_ERR_CUDA, "join_agg_noalloc: device query failed");
       }
-      it = g_noalloc_devices.emplace(dev, nd).first;
+      it = g_noalloc_devices.insert_or_assign({dev, current_context_id()}, nd).first;
     }
     d = it->second;
   }
@@ -493,17 +526,16 @@ int gbj_join_agg_noalloc(const int32_t *d_build_keys, const int32_t *d_build_pay
   if (slots < 64) slots = 64;
   uint64_t *table = d.scratch;
   uint32_t *meta = reinterpret_cast<uint32_t *>(d.scratch + kNoAllocSlots);
-  uint32_t *status = meta + 1;
   // the array keeps the previous call's table: clear the part this call uses
   if (cudaMemsetAsync(table, 0, slots * sizeof(uint64_t), s) != cudaSuccess ||
-      cudaMemsetAsync(meta, 0, 2 * sizeof(uint32_t), s) != cudaSuccess) {
+      cudaMemsetAsync(meta, 0, sizeof(uint32_t), s) != cudaSuccess) {
     (void)cudaGetLastError();
     return noalloc_fail(GBJ_ERR_CUDA, "join_agg_noalloc: cudaMemsetAsync failed");
   }
   k_noalloc_init_out<<<1, 32, 0, s>>>(spec, d_out);
   if (n_build)
     k_join_build<<<grid_for_sms(d.sm_count, n_build, kThreads), kThreads, 0, s>>>(
-        d_build_keys, n_build, table, slots - 1, meta, status);
+        d_build_keys, n_build, table, slots - 1, meta, nullptr);
   if (n_probe)
     launch_probe(d.sm_count, d_probe_keys, d_probe_payload, n_probe, table, slots - 1,
                  d_build_payload, meta, spec, d_out, s);

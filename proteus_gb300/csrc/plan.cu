@@ -10,10 +10,21 @@
 // partitioned-hashjoin-chained (:851-976) and join (radix; p{eq},
 // leftInput, rightInput; :1007-1139), groupby / hashgroupby-chained (input,
 // k, e[{e, m, packet, offset}], hash_bits, maxInputSize; :479-530) and
-// reduce (e, accumulator, p; :248-286).  Expressions (expression-parser.cpp):
-// recordProjection, argument, int, int64, bool, cast, eq, lt, le, gt, ge,
-// and, multiply.  Accumulators: sum, max, min.  Anything else is rejected
-// with GBJ_ERR_UNSUPPORTED and a message naming it.
+// reduce (e, accumulator, p; :248-286), nest (RadixNest: f, p, e,
+// accumulator, aggrLabels, g, fields; :1140-1268), print / project /
+// materializer over a result, and the data-movement operators that leave a
+// relation unchanged on one GPU (block-to-tuples, unpack, pack,
+// tuples-to-block, cpu-to-gpu, gpu-to-cpu, mem-move-device,
+// mem-broadcast-device, mem-move-local-to, router, exchange).  Expressions
+// (expression-parser.cpp): recordProjection, argument, int, int64, bool,
+// cast, eq, lt, le, gt, ge, and, multiply.  Accumulators: sum, max, min, or,
+// and.  Every field of an operator is either honoured or rejected: an
+// operator or field the façade does not know (or a value it cannot honour)
+// fails with GBJ_ERR_UNSUPPORTED and a message naming it.  Placement and
+// layout fields (gpu, blockwise, output, build_w / build_e packets, ...)
+// select where and in which packed layout the reference runs an operator;
+// here every operator runs on this GPU over columns, so they do not change
+// a result and are accepted.
 //
 // Lowering: reduce over a join whose output expressions read at most one
 // build column and one probe column runs as one fused probe + aggregate
@@ -224,17 +235,102 @@ bool is_const(const JVal &e, int64_t *v) {
   return true;
 }
 
+// expression-parser.cpp:781-800 (parseAccumulator); or / and are the
+// logical monoids (gmonoids.cpp:363-376).
 int monoid(const std::string &m) {
   if (m == "sum") return GBJ_AGG_SUM;
   if (m == "max") return GBJ_AGG_MAX;
   if (m == "min") return GBJ_AGG_MIN;
-  fail(GBJ_ERR_UNSUPPORTED, "plan: accumulator '" + m + "' is not supported (sum, max, min are)");
+  if (m == "or") return GBJ_AGG_OR;
+  if (m == "and") return GBJ_AGG_AND;
+  fail(GBJ_ERR_UNSUPPORTED,
+       "plan: accumulator '" + m + "' is not supported (sum, max, min, or, and are)");
 }
 
-// Walks a plan checking operator names and required fields (no GPU work).
+// Operators that move or re-route a relation without changing it (the
+// reference's device crossings, packers and routers): on one GPU over
+// resident columns they are the identity.
+bool passthrough(const std::string &op) {
+  static const std::set<std::string> k = {"block-to-tuples", "unpack", "pack", "tuples-to-block",
+                                          "cpu-to-gpu", "gpu-to-cpu", "mem-move-device",
+                                          "mem-broadcast-device", "mem-move-local-to", "router",
+                                          "exchange"};
+  return k.count(op) != 0;
+}
+
+// The fields each operator may carry: the ones plan-parser.cpp reads for it,
+// plus the placement / layout fields its plans carry.  Anything else is
+// refused, so no field is ever silently ignored.
+void check_fields(const JVal &v, const std::string &op) {
+  static const std::set<std::string> placement = {"operator", "gpu", "blockwise", "output",
+                                                  "max_line_estimate", "jumpTo"};
+  static const std::map<std::string, std::set<std::string>> fields = {
+      {"scan", {"plugin"}},
+      {"select", {"input", "p"}},
+      {"project", {"input", "e", "relName"}},
+      {"print", {"input", "e", "plugin"}},
+      {"materializer", {"input", "e", "w"}},
+      {"sort", {"input", "e", "granularity", "rowType"}},
+      {"hashjoin-chained",
+       {"build_input", "probe_input", "build_k", "probe_k", "hash_bits", "maxBuildInputSize", "build_e",
+        "build_w", "probe_e", "probe_w"}},
+      {"partitioned-hashjoin-chained",
+       {"build_input", "probe_input", "build_k", "probe_k", "build_k_minor", "probe_k_minor", "hash_bits",
+        "maxBuildInputSize", "maxProbeInputSize", "build_e", "build_w", "probe_e", "probe_w"}},
+      {"join",
+       {"p", "leftInput", "rightInput", "leftFields", "rightFields", "build_e", "build_w", "probe_e",
+        "probe_w"}},
+      {"groupby", {"input", "k", "e", "hash_bits", "maxInputSize", "w"}},
+      {"hashgroupby-chained", {"input", "k", "e", "hash_bits", "maxInputSize", "w"}},
+      {"reduce", {"input", "e", "accumulator", "p"}},
+      {"nest", {"input", "accumulator", "aggrLabels", "e", "p", "f", "g", "fields"}},
+      {"hash-rearrange", {"input", "e", "projections", "buckets", "hashProject"}},
+      {"hash-pack", {"input", "e", "projections", "buckets", "hashProject"}},
+      {"block-to-tuples", {"input", "projections"}},
+      {"unpack", {"input", "projections"}},
+      {"pack", {"input", "projections", "trait"}},
+      {"tuples-to-block", {"input", "projections", "trait"}},
+      {"cpu-to-gpu", {"input", "projections", "queueSize", "granularity"}},
+      {"gpu-to-cpu", {"input", "projections", "queueSize", "granularity"}},
+      {"mem-move-device", {"input", "projections", "do_transfer", "split_id", "to_cpu", "slack"}},
+      {"mem-broadcast-device", {"input", "projections", "always_share", "num_of_targets", "to_cpu"}},
+      {"mem-move-local-to", {"input", "projections", "slack"}},
+      {"router",
+       {"input", "numOfParents", "num_of_targets", "slack", "target", "cpu_targets", "numa_local",
+        "rand_local_cpu", "producers", "projections", "split_id"}},
+      {"exchange",
+       {"input", "numOfParents", "num_of_targets", "slack", "target", "cpu_targets", "numa_local",
+        "rand_local_cpu", "producers", "projections", "split_id"}},
+  };
+  auto it = fields.find(op);
+  if (it == fields.end()) return;
+  for (const auto &kv : v.o)
+    if (!placement.count(kv.first) && !it->second.count(kv.first))
+      fail(GBJ_ERR_UNSUPPORTED, "plan: field '" + kv.first + "' of operator '" + op + "' is not supported");
+}
+
+// Walks a plan checking operator names and fields (no GPU work).
 void validate(const JVal &v) {
   const std::string op = op_name(v);
-  if (op == "scan") {
+  check_fields(v, op);
+  if (passthrough(op)) {
+    validate(need(v, "input", op.c_str()));
+  } else if (op == "print") {
+    validate(need(v, "input", "print"));
+  } else if (op == "materializer") {
+    need(v, "e", "materializer");
+    validate(need(v, "input", "materializer"));
+  } else if (op == "nest") {
+    const JVal &acc = need(v, "accumulator", "nest");
+    const JVal &e = need(v, "e", "nest");
+    const JVal &labels = need(v, "aggrLabels", "nest");
+    if (acc.a.size() != e.a.size() || labels.a.size() != e.a.size())
+      fail(GBJ_ERR_INVALID, "plan: nest needs one accumulator and one label per expression");
+    for (const JVal &a : acc.a) monoid(a.s);
+    need(v, "f", "nest");
+    need(v, "p", "nest");
+    validate(need(v, "input", "nest"));
+  } else if (op == "scan") {
     const JVal &pl = need(v, "plugin", "scan");
     need(pl, "name", "scan plugin");
   } else if (op == "select") {
@@ -243,6 +339,9 @@ void validate(const JVal &v) {
   } else if (op == "hashjoin-chained" || op == "partitioned-hashjoin-chained") {
     need(v, "build_k", op.c_str());
     need(v, "probe_k", op.c_str());
+    if (!v.get("build_k_minor") != !v.get("probe_k_minor"))
+      fail(GBJ_ERR_INVALID, "plan: " + op + " needs build_k_minor and probe_k_minor together "
+                            "(the reference checks the minor key only when both are given)");
     validate(need(v, "build_input", op.c_str()));
     validate(need(v, "probe_input", op.c_str()));
   } else if (op == "join") {
@@ -280,10 +379,45 @@ void validate(const JVal &v) {
     validate(need(v, "input", op.c_str()));
   } else {
     fail(GBJ_ERR_UNSUPPORTED, "plan: operator '" + op +
-                                  "' is not supported (scan, select, project, sort, hashjoin-chained, "
-                                  "partitioned-hashjoin-chained, join, groupby, hashgroupby-chained, "
-                                  "reduce, hash-rearrange, hash-pack are)");
+                                  "' is not supported (scan, select, project, print, materializer, sort, "
+                                  "hashjoin-chained, partitioned-hashjoin-chained, join, groupby, "
+                                  "hashgroupby-chained, nest, reduce, hash-rearrange, hash-pack and the "
+                                  "data-movement operators are)");
   }
+}
+
+// Output name of an expression: its register_as attribute, else `dflt`.
+std::string out_name(const JVal &e, const std::string &dflt) {
+  if (const JVal *r = e.get("register_as"))
+    if (const JVal *a = r->get("attrName"))
+      if (a->t == JVal::Str) return a->s;
+  return dflt;
+}
+
+// ---------------------------------------------------------- kernels
+// truth[i] = lo <= col[i] <= hi (mode 0) or col[i] != 0 (mode 1); with
+// and_into the result is ANDed into truth.
+__global__ void k_truth(const int32_t *__restrict__ col, uint64_t n, int mode, int32_t lo, int32_t hi,
+                        int and_into, int32_t *__restrict__ truth) {
+  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+    const int32_t v = col[i];
+    const int32_t t = mode == 0 ? (v >= lo && v <= hi) : (v != 0);
+    truth[i] = and_into ? (truth[i] & t) : t;
+  }
+}
+
+__global__ void k_widen(const int32_t *__restrict__ col, uint64_t n, int64_t *__restrict__ out) {
+  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x)
+    out[i] = col[i];
+}
+
+// flag[i] = bminor[brow[i]] == pminor[prow[i]] (the minor-key check over
+// materialised join pairs).
+__global__ void k_pair_eq(const int32_t *__restrict__ bminor, const int32_t *__restrict__ pminor,
+                          const int32_t *__restrict__ brow, const int32_t *__restrict__ prow, uint64_t n,
+                          int32_t *__restrict__ flag) {
+  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x)
+    flag[i] = bminor[brow[i]] == pminor[prow[i]];
 }
 
 }  // namespace
@@ -330,35 +464,90 @@ class Exec {
     for (void *p : allocs_) gbj_pool_free(ctx_, p);
   }
 
+  static bool is_agg(const std::string &op) {
+    return op == "reduce" || op == "groupby" || op == "hashgroupby-chained" || op == "nest";
+  }
+  // Whether an aggregate sits below print / project / materializer / sort
+  // wrappers (their lists then select from the aggregate's result).
+  static bool agg_below(const JVal &v) {
+    const std::string op = op_name(v);
+    if (is_agg(op)) return true;
+    if (op == "print" || op == "project" || op == "materializer" || op == "sort")
+      return agg_below(need(v, "input", op.c_str()));
+    return false;
+  }
+
   gbj_result *run(const JVal &root) {
     auto res = std::make_unique<gbj_result>();
-    const std::string op = op_name(root);
-    const std::string iop = op == "sort" ? op_name(need(root, "input", "sort")) : std::string();
-    if (op == "reduce") {
-      reduce(root, res.get());
-    } else if (op == "groupby" || op == "hashgroupby-chained") {
-      groupby(root, res.get());
-    } else if (iop == "groupby" || iop == "hashgroupby-chained" || iop == "reduce") {
+    // print and, over an aggregate, project / materializer only choose and
+    // rename result columns: peel them, apply their lists at the end
+    std::vector<const JVal *> lists;  // outermost first
+    const JVal *node = &root;
+    for (;;) {
+      const std::string op = op_name(*node);
+      if (op != "print" && op != "project" && op != "materializer") break;
+      const JVal &in = need(*node, "input", op.c_str());
+      if (op != "print" && !agg_below(in)) break;
+      if (const JVal *e = node->get("e")) lists.push_back(e);
+      node = &in;
+    }
+    const std::string op = op_name(*node);
+    const std::string iop = op == "sort" ? op_name(need(*node, "input", "sort")) : std::string();
+    if (is_agg(op)) {
+      aggregate(*node, res.get());
+    } else if (op == "sort" && is_agg(iop)) {
       // ORDER BY over an aggregate's (small, int64) result: ordered on the host
-      const JVal &in = need(root, "input", "sort");
-      if (iop == "reduce") reduce(in, res.get());
-      else groupby(in, res.get());
-      host_sort(root, res.get());
+      aggregate(need(*node, "input", "sort"), res.get());
+      host_sort(*node, res.get());
     } else {
-      const Rel r = rel(root);
+      const Rel r = rel(*node);
       res->rows = r.n;
       for (const auto &c : r.cols) {
         res->names.push_back(c.rel.empty() ? c.attr : c.rel + "." + c.attr);
         res->cols.push_back(to_host32(c.d, r.n));
       }
     }
+    for (auto it = lists.rbegin(); it != lists.rend(); ++it) select_columns(**it, res.get());
     return res.release();
   }
 
  private:
+  void aggregate(const JVal &v, gbj_result *res) {
+    const std::string op = op_name(v);
+    if (op == "reduce") reduce(v, res);
+    else if (op == "nest") nest(v, res);
+    else groupby(v, res);
+  }
+
+  // A print / project list over a result: each entry names a result column
+  // (recordProjection) and may rename it (register_as).
+  void select_columns(const JVal &list, gbj_result *res) {
+    std::vector<std::string> names;
+    std::vector<std::vector<int64_t>> cols;
+    for (const JVal &e : list.a) {
+      const auto ra = projection(e);
+      int c = -1;
+      for (size_t j = 0; j < res->names.size() && c < 0; ++j) {
+        const std::string &n = res->names[j];
+        if (n == ra.second || n == ra.first + "." + ra.second ||
+            (n.size() > ra.second.size() && n.compare(n.size() - ra.second.size() - 1, std::string::npos,
+                                                       "." + ra.second) == 0))
+          c = (int)j;
+      }
+      if (c < 0) fail(GBJ_ERR_INVALID, "plan: output column " + ra.second + " is not in the result");
+      names.push_back(out_name(e, ra.second));
+      cols.push_back(res->cols[c]);
+    }
+    res->names.swap(names);
+    res->cols.swap(cols);
+  }
+
   gbj_catalog *cat_;
   gbj_ctx *ctx_;
   std::vector<void *> allocs_;
+  std::set<std::pair<std::string, std::string>> absent_;
+  int grid(uint64_t n) const { return (int)std::max<uint64_t>(1, std::min<uint64_t>((n + 255) / 256, 4096)); }
+  void launched(const char *name) { ck(after_launch(ctx_, name, ctx_->stream), name); }
 
   void ck(int rc, const char *what) {
     if (rc != GBJ_OK) fail(rc, std::string(what) + ": " + gbj_last_error(ctx_));
@@ -394,20 +583,26 @@ class Exec {
   const int32_t *column(const Rel &r, const JVal &e) {
     const auto ra = projection(e);
     const Rel::C *c = r.find(ra);
+    if (!c && absent_.count(ra))
+      fail(GBJ_ERR_UNSUPPORTED, "plan: column " + ra.first + "." + ra.second +
+                                    " is not an int32 column of the catalog (only int32 columns are loaded)");
     if (!c) fail(GBJ_ERR_INVALID, "plan: column " + ra.first + "." + ra.second + " is not in the operator's input");
     return c->d;
   }
 
   Rel rel(const JVal &v) {
     const std::string op = op_name(v);
+    if (passthrough(op) || op == "print") return rel(need(v, "input", op.c_str()));
+    if (op == "materializer") return project(v);
     if (op == "scan") return scan(v);
     if (op == "select") return select(v);
     if (op == "hashjoin-chained" || op == "partitioned-hashjoin-chained" || op == "join") return join(v);
     if (op == "sort") return sort(v);
     if (op == "project") return project(v);
     if (op == "hash-rearrange" || op == "hash-pack") return rearrange(v);
-    if (op == "groupby" || op == "hashgroupby-chained" || op == "reduce")
-      fail(GBJ_ERR_UNSUPPORTED, "plan: '" + op + "' is supported only as the plan's root");
+    if (is_agg(op))
+      fail(GBJ_ERR_UNSUPPORTED, "plan: '" + op + "' is supported only as the plan's root (under print, "
+                                "project or sort)");
     validate(v);  // raises the unsupported-operator error
     fail(GBJ_ERR_UNSUPPORTED, "plan: operator '" + op + "'");
   }
@@ -440,10 +635,11 @@ class Exec {
   }
 
   Rel project(const JVal &v) {
-    const Rel r = rel(need(v, "input", "project"));
+    const std::string op = op_name(v);
+    const Rel r = rel(need(v, "input", op.c_str()));
     Rel o;
     o.n = r.n;
-    for (const JVal &e : need(v, "e", "project").a) {
+    for (const JVal &e : need(v, "e", op.c_str()).a) {
       const auto ra = projection(e);
       const Rel::C *c = r.find(ra);
       if (!c) fail(GBJ_ERR_INVALID, "plan: project column " + ra.second + " is not in its input");
@@ -528,17 +724,20 @@ class Exec {
         attrs.push_back(an->s);
       }
     }
+    // the relation's row count, also for a scan that projects nothing
     Rel r;
-    bool first = true;
+    r.n = cat_->cols.at({name, it->second.front()}).n;
     for (const std::string &a : attrs) {
       auto c = cat_->cols.find({name, a});
-      if (c == cat_->cols.end()) fail(GBJ_ERR_INVALID, "plan: column " + name + "." + a + " is not in the catalog");
-      if (!first && c->second.n != r.n) fail(GBJ_ERR_INVALID, "plan: columns of " + name + " differ in length");
-      r.n = c->second.n;
-      first = false;
+      if (c == cat_->cols.end()) {
+        // a projected attribute the catalog does not hold (a string or float
+        // column of the reference's schema): an error only if an operator reads it
+        absent_.insert({name, a});
+        continue;
+      }
+      if (c->second.n != r.n) fail(GBJ_ERR_INVALID, "plan: columns of " + name + " differ in length");
       r.cols.push_back({name, a, c->second.d});
     }
-    if (first) r.n = 0;
     return r;
   }
 
@@ -595,10 +794,21 @@ class Exec {
     return o;
   }
 
-  Rel select(const JVal &v) {
-    Rel in = rel(need(v, "input", "select"));
+  Rel select(const JVal &v) { return filter(rel(need(v, "input", "select")), need(v, "p", "select")); }
+
+  // True for an absent predicate or the constant true.
+  static bool always_true(const JVal *p) {
+    if (!p) return true;
+    const JVal &x = uncast(*p);
+    if (expr_name(x) != "bool") return false;
+    const JVal *b = x.get("v");
+    return b && b->t == JVal::Bool && b->b;
+  }
+
+  // The rows of `in` a conjunction of column-vs-constant comparisons keeps.
+  Rel filter(Rel in, const JVal &p) {
     std::vector<std::tuple<std::pair<std::string, std::string>, int32_t, int32_t>> rg;
-    ranges(need(v, "p", "select"), rg);
+    ranges(p, rg);
     for (const auto &t : rg) {
       if (std::get<1>(t) > std::get<2>(t)) return gather(in, nullptr, 0);  // always false
       const Rel::C *c = in.find(std::get<0>(t));
@@ -614,6 +824,7 @@ class Exec {
 
   struct JoinSides {
     const JVal *build, *probe, *bk, *pk;
+    const JVal *bkm = nullptr, *pkm = nullptr;  // minor keys (partitioned join)
     int32_t hash_bits = 0;
     uint64_t max_build = 0;
     bool radix = false;
@@ -637,6 +848,9 @@ class Exec {
       if (const JVal *h = v.get("hash_bits")) s.hash_bits = (int32_t)h->i;
       if (const JVal *m = v.get("maxBuildInputSize")) s.max_build = (uint64_t)std::max<int64_t>(m->i, 0);
       s.radix = op == "partitioned-hashjoin-chained";
+      s.bkm = v.get("build_k_minor");
+      s.pkm = v.get("probe_k_minor");
+      if (!s.bkm != !s.pkm) fail(GBJ_ERR_INVALID, "plan: build_k_minor and probe_k_minor go together");
     }
     return s;
   }
@@ -661,9 +875,27 @@ class Exec {
     int32_t *br = alloc<int32_t>(m), *pr = alloc<int32_t>(m);
     uint64_t *dm = alloc<uint64_t>(1);
     ck(gbj_join_probe_pairs(ctx_, t, pk, nullptr, p.n, br, pr, m, dm, nullptr), "join pairs");
+    uint64_t k = m;
+    if (s.bkm && m) {
+      // the minor-key check (gpu-partitioned-hash-join-chained.cpp:1284-1333)
+      // over the key matches: keep the pairs whose minor keys are equal
+      const int32_t *bm = column(b, *s.bkm), *pm = column(p, *s.pkm);
+      int32_t *flag = alloc<int32_t>(m), *keep = alloc<int32_t>(m);
+      k_pair_eq<<<grid(m), 256, 0, ctx_->stream>>>(bm, pm, br, pr, m, flag);
+      launched("k_pair_eq");
+      uint64_t *kc = alloc<uint64_t>(1);
+      ck(gbj_select_range(ctx_, flag, m, 1, 1, keep, kc, nullptr), "minor key");
+      k = read1(kc);
+      int32_t *br2 = alloc<int32_t>(k), *pr2 = alloc<int32_t>(k);
+      if (k) {
+        ck(gbj_gather(ctx_, br, keep, k, br2, nullptr), "gather");
+        ck(gbj_gather(ctx_, pr, keep, k, pr2, nullptr), "gather");
+      }
+      br = br2, pr = pr2;
+    }
     sync();
-    Rel o = gather(b, br, m);
-    const Rel po = gather(p, pr, m);
+    Rel o = gather(b, br, k);
+    const Rel po = gather(p, pr, k);
     o.cols.insert(o.cols.end(), po.cols.begin(), po.cols.end());
     return o;
   }
@@ -725,15 +957,86 @@ class Exec {
     return false;
   }
 
+  // Aggregate of a constant operand over `n` rows (or `n` join matches).
+  static int64_t const_agg(int m, int64_t c, int64_t n) {
+    switch (m) {
+      case GBJ_AGG_SUM: return c * n;
+      case GBJ_AGG_OR: return (n && c) ? 1 : 0;
+      case GBJ_AGG_AND: return (!n || c) ? 1 : 0;
+      default: return n ? c : (m == GBJ_AGG_MAX ? INT64_MIN : INT64_MAX);
+    }
+  }
+
+  // A value operand of an aggregate: a column, a constant, or a
+  // column-vs-constant comparison (materialised as a 0/1 column).  With
+  // `truth`, a column is turned into its truth value (!= 0), as the logical
+  // accumulators read it.
+  struct Val {
+    const int32_t *d = nullptr;
+    bool is_const = false;
+    int64_t c = 0;
+  };
+  Val value(const Rel &r, const JVal &e, bool truth) {
+    Val out;
+    const JVal &x = uncast(e);
+    const std::string n = expr_name(x);
+    int64_t c = 0;
+    if (is_const(x, &c)) {
+      out.is_const = true;
+      out.c = truth ? (c != 0) : c;
+      return out;
+    }
+    if (n == "bool") {
+      out.is_const = true;
+      out.c = always_true(&x) ? 1 : 0;
+      return out;
+    }
+    if (n == "eq" || n == "lt" || n == "le" || n == "gt" || n == "ge" || n == "and") {
+      std::vector<std::tuple<std::pair<std::string, std::string>, int32_t, int32_t>> rg;
+      ranges(x, rg);
+      int32_t *t = alloc<int32_t>(r.n);
+      bool first = true;
+      for (const auto &q : rg) {
+        const bool never = std::get<1>(q) > std::get<2>(q);
+        const Rel::C *col = never ? nullptr : r.find(std::get<0>(q));
+        if (!never && !col) fail(GBJ_ERR_INVALID, "plan: column " + std::get<0>(q).second + " is not in the input");
+        if (r.n) {
+          // an always-false range: every row fails (a column compared with an empty range)
+          const int32_t *src = col ? col->d : t;
+          k_truth<<<grid(r.n), 256, 0, ctx_->stream>>>(src, r.n, 0, never ? 1 : std::get<1>(q),
+                                                       never ? 0 : std::get<2>(q), first ? 0 : 1, t);
+          launched("k_truth");
+        }
+        first = false;
+      }
+      out.d = t;
+      return out;
+    }
+    const int32_t *col = column(r, e);
+    if (!truth) {
+      out.d = col;
+      return out;
+    }
+    int32_t *t = alloc<int32_t>(r.n);
+    if (r.n) {
+      k_truth<<<grid(r.n), 256, 0, ctx_->stream>>>(col, r.n, 1, 0, 0, 0, t);
+      launched("k_truth");
+    }
+    out.d = t;
+    return out;
+  }
+
   void reduce(const JVal &v, gbj_result *res) {
     const JVal &es = need(v, "e", "reduce"), &acc = need(v, "accumulator", "reduce");
     if (es.a.size() != acc.a.size() || es.a.empty() || es.a.size() > GBJ_MAX_AGGS)
       fail(GBJ_ERR_INVALID, "plan: reduce needs 1..8 expressions, one accumulator each");
     const JVal &in = need(v, "input", "reduce");
+    const JVal *pred = v.get("p");
     const std::string iop = op_name(in);
     std::vector<int64_t> out(es.a.size());
     bool done = false;
-    if (iop == "hashjoin-chained" || iop == "partitioned-hashjoin-chained" || iop == "join") {
+    if (always_true(pred) &&
+        (iop == "hashjoin-chained" || iop == "partitioned-hashjoin-chained" || iop == "join")) {
       const JoinSides s = sides(in);
       const Rel b = rel(*s.build), p = rel(*s.probe);
       const int32_t *bcol = nullptr, *pcol = nullptr;
@@ -747,7 +1050,11 @@ class Exec {
           aggs[j] = {ops[j].operand == GBJ_VAL_ONE ? GBJ_AGG_COUNT : monoid(acc.a[j].s), ops[j].operand};
         int64_t *d = alloc<int64_t>(aggs.size());
         const int32_t *bk = column(b, *s.bk), *pk = column(p, *s.pk);
-        if (s.radix) {
+        if (s.bkm) {
+          ck(gbj_radix_join_agg_minor(ctx_, bk, column(b, *s.bkm), bcol, b.n, pk, column(p, *s.pkm), pcol, p.n,
+                                      nullptr, aggs.data(), (int32_t)aggs.size(), d, nullptr),
+             "radix join (minor key)");
+        } else if (s.radix) {
           ck(gbj_radix_join_agg(ctx_, bk, bcol, b.n, pk, pcol, p.n, nullptr, aggs.data(), (int32_t)aggs.size(), d,
                                 nullptr),
              "radix join");
@@ -760,38 +1067,66 @@ class Exec {
           ck(rc, "join probe");
         }
         const std::vector<int64_t> h = to_host64(d, aggs.size());
-        for (size_t j = 0; j < aggs.size(); ++j) {
-          int64_t x = h[j];
-          if (ops[j].operand == GBJ_VAL_ONE) {  // sum = v * count; max/min = v if any match
-            const int m = monoid(acc.a[j].s);
-            x = m == GBJ_AGG_SUM ? ops[j].scale * h[j]
-                                 : (h[j] ? ops[j].scale : (m == GBJ_AGG_MAX ? INT64_MIN : INT64_MAX));
-          }
-          out[j] = x;
-        }
+        for (size_t j = 0; j < aggs.size(); ++j)
+          out[j] = ops[j].operand == GBJ_VAL_ONE ? const_agg(monoid(acc.a[j].s), ops[j].scale, h[j]) : h[j];
         done = true;
       }
     }
     if (!done) {
-      const Rel r = rel(in);
+      Rel r = rel(in);
+      if (!always_true(pred)) r = filter(r, *pred);
       for (size_t j = 0; j < es.a.size(); ++j) {
         const int m = monoid(acc.a[j].s);
-        int64_t c = 0;
-        if (is_const(es.a[j], &c)) {
-          out[j] = m == GBJ_AGG_SUM ? c * (int64_t)r.n : (r.n ? c : (m == GBJ_AGG_MAX ? INT64_MIN : INT64_MAX));
+        const Val x = value(r, es.a[j], false);
+        if (x.is_const) {
+          out[j] = const_agg(m, x.c, (int64_t)r.n);
           continue;
         }
-        const int32_t *col = column(r, es.a[j]);
         const gbj_agg a{m, GBJ_VAL_PROBE};
         int64_t *d = alloc<int64_t>(1);
-        ck(gbj_reduce(ctx_, col, nullptr, r.n, &a, 1, d, nullptr), "reduce");
+        ck(gbj_reduce(ctx_, x.d, nullptr, r.n, &a, 1, d, nullptr), "reduce");
         out[j] = to_host64(d, 1)[0];
       }
     }
     res->rows = 1;
     for (size_t j = 0; j < out.size(); ++j) {
-      res->names.push_back(acc.a[j].s + "_" + std::to_string(j));
+      res->names.push_back(out_name(es.a[j], acc.a[j].s + "_" + std::to_string(j)));
       res->cols.push_back({out[j]});
+    }
+  }
+
+  // Per-group aggregates over one key column: COUNT, SUM, MIN, MAX of each
+  // distinct value column (logical accumulators read MAX / MIN of the
+  // operand's truth column), sorted by key.
+  struct GroupSpec {
+    int m;        // accumulator
+    int vi;       // value column index, -1 for a constant
+    int64_t c;    // the constant
+  };
+  void group_values(const Rel &r, const JVal &es, const char *op, const std::vector<std::string> &accs,
+                    std::vector<const int32_t *> &vcols, std::vector<GroupSpec> &spec,
+                    bool nested_e) {
+    for (size_t j = 0; j < es.a.size(); ++j) {
+      const JVal &x = nested_e ? need(es.a[j], "e", op) : es.a[j];
+      const int m = monoid(accs[j]);
+      const Val val = value(r, x, m == GBJ_AGG_OR || m == GBJ_AGG_AND);
+      if (val.is_const) {
+        spec.push_back({m, -1, val.c});
+        continue;
+      }
+      auto it = std::find(vcols.begin(), vcols.end(), val.d);
+      spec.push_back({m, (int)(it - vcols.begin()), 0});
+      if (it == vcols.end()) vcols.push_back(val.d);
+    }
+  }
+  static int64_t group_value(const GroupSpec &g, const std::vector<int64_t> &row) {
+    const int64_t cnt = row[4 * std::max(g.vi, 0)];
+    if (g.vi < 0) return const_agg(g.m, g.c, cnt);
+    const int64_t *a = &row[4 * g.vi];
+    switch (g.m) {
+      case GBJ_AGG_SUM: return a[1];
+      case GBJ_AGG_MIN: case GBJ_AGG_AND: return a[2];
+      default: return a[3];  // MAX, OR
     }
   }
 
@@ -805,21 +1140,12 @@ class Exec {
     gbj_groupby_params prm{};
     if (const JVal *h = v.get("hash_bits")) prm.hash_bits = (int32_t)h->i;
     if (const JVal *m = v.get("maxInputSize")) prm.max_input_size = (uint64_t)std::max<int64_t>(m->i, 0);
-    // one gbj_groupby per distinct value column (COUNT/SUM/MIN/MAX of it);
-    // constants need only the counts
+    std::vector<std::string> accs;
+    for (const JVal &x : es.a) accs.push_back(need(x, "m", op).s);
+    // one gbj_groupby per distinct value column; constants need only the counts
     std::vector<const int32_t *> vcols;
-    std::vector<std::pair<int, int64_t>> spec;  // (value column index or -1, constant)
-    for (const JVal &x : es.a) {
-      int64_t c = 0;
-      if (is_const(need(x, "e", op), &c)) {
-        spec.push_back({-1, c});
-        continue;
-      }
-      const int32_t *col = column(r, need(x, "e", op));
-      auto it = std::find(vcols.begin(), vcols.end(), col);
-      spec.push_back({(int)(it - vcols.begin()), 0});
-      if (it == vcols.end()) vcols.push_back(col);
-    }
+    std::vector<GroupSpec> spec;
+    group_values(r, es, op, accs, vcols, spec, true);
     if (vcols.empty()) vcols.push_back(key);  // counts of the key column
     const uint64_t cap = std::max<uint64_t>(r.n, 1);
     std::map<int32_t, std::vector<int64_t>> groups;  // key -> per value column: cnt, sum, min, max
@@ -842,22 +1168,77 @@ class Exec {
     res->names.push_back(projection(ks.a[0]).second);
     res->cols.emplace_back();
     for (size_t j = 0; j < es.a.size(); ++j) {
-      res->names.push_back(need(es.a[j], "m", op).s + "_" + std::to_string(j));
+      res->names.push_back(out_name(need(es.a[j], "e", op), accs[j] + "_" + std::to_string(j)));
       res->cols.emplace_back();
     }
     for (const auto &kv : groups) {  // sorted by key
       res->cols[0].push_back(kv.first);
-      for (size_t j = 0; j < spec.size(); ++j) {
-        const int m = monoid(need(es.a[j], "m", op).s);
-        const int vi = spec[j].first;
-        const int64_t cnt = kv.second[4 * std::max(vi, 0)];
-        int64_t x;
-        if (vi < 0) x = m == GBJ_AGG_SUM ? spec[j].second * cnt : spec[j].second;
-        else x = kv.second[4 * vi + (m == GBJ_AGG_SUM ? 1 : m == GBJ_AGG_MIN ? 2 : 3)];
-        res->cols[1 + j].push_back(x);
-      }
+      for (size_t j = 0; j < spec.size(); ++j) res->cols[1 + j].push_back(group_value(spec[j], kv.second));
     }
   }
+
+  // RadixNest (radix-nest.cpp:326-700; plan fields plan-parser.cpp:1140-1268):
+  // group by f over the rows p keeps, one aggregate per e / accumulator,
+  // named by aggrLabels.  The key and each value column are widened to
+  // int64 and grouped by gbj_nest_i64, as the reference nests on 64-bit
+  // keys (radix-aggr.cpp, KEY_8B).  g (nulls to zeros) has no effect on
+  // non-null int32 columns; fields lists what the reference materialises.
+  void nest(const JVal &v, gbj_result *res) {
+    const char *op = "nest";
+    const JVal &es = need(v, "e", op), &acc = need(v, "accumulator", op), &labels = need(v, "aggrLabels", op);
+    Rel r = rel(need(v, "input", op));
+    if (!always_true(v.get("p"))) r = filter(r, need(v, "p", op));
+    const JVal &f = need(v, "f", op);
+    const int32_t *key = column(r, f);
+    std::vector<std::string> accs;
+    for (const JVal &a : acc.a) accs.push_back(a.s);
+    std::vector<const int32_t *> vcols;
+    std::vector<GroupSpec> spec;
+    group_values(r, es, op, accs, vcols, spec, false);
+    const uint64_t n = r.n, cap = std::max<uint64_t>(n, 1);
+    int64_t *k64 = alloc<int64_t>(cap);
+    if (n) {
+      k_widen<<<grid(n), 256, 0, ctx_->stream>>>(key, n, k64);
+      launched("k_widen");
+    }
+    std::map<int64_t, std::vector<int64_t>> groups;  // key -> per value column: cnt, sum, min, max
+    const size_t passes = std::max<size_t>(vcols.size(), 1);
+    for (size_t i = 0; i < passes; ++i) {
+      int64_t *v64 = nullptr;
+      if (i < vcols.size()) {
+        v64 = alloc<int64_t>(cap);
+        if (n) {
+          k_widen<<<grid(n), 256, 0, ctx_->stream>>>(vcols[i], n, v64);
+          launched("k_widen");
+        }
+      }
+      int64_t *ok = alloc<int64_t>(cap), *oc = alloc<int64_t>(cap), *os = alloc<int64_t>(cap);
+      int64_t *omn = alloc<int64_t>(cap), *omx = alloc<int64_t>(cap);
+      uint64_t *ng = alloc<uint64_t>(1);
+      ck(gbj_nest_i64(ctx_, k64, v64, n, 0, ok, oc, os, omn, omx, cap, ng, nullptr), "nest");
+      const uint64_t g = read1(ng);
+      const auto hk = to_host64(ok, g), hc = to_host64(oc, g), hs = to_host64(os, g);
+      const auto hmn = to_host64(omn, g), hmx = to_host64(omx, g);
+      for (uint64_t q = 0; q < g; ++q) {
+        auto &row = groups[hk[q]];
+        row.resize(4 * passes);
+        row[4 * i] = hc[q], row[4 * i + 1] = hs[q], row[4 * i + 2] = hmn[q], row[4 * i + 3] = hmx[q];
+      }
+    }
+    res->rows = groups.size();
+    res->names.push_back(projection(f).second);
+    res->cols.emplace_back();
+    for (size_t j = 0; j < es.a.size(); ++j) {
+      const JVal &l = labels.a[j];
+      res->names.push_back(l.t == JVal::Str ? l.s : accs[j] + "_" + std::to_string(j));
+      res->cols.emplace_back();
+    }
+    for (const auto &kv : groups) {  // sorted by key
+      res->cols[0].push_back(kv.first);
+      for (size_t j = 0; j < spec.size(); ++j) res->cols[1 + j].push_back(group_value(spec[j], kv.second));
+    }
+  }
+
 };
 
 }  // namespace

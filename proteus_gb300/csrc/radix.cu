@@ -325,7 +325,15 @@ __device__ __forceinline__ uint32_t item_partition(const uint64_t *__restrict__ 
   return lo;
 }
 
-enum : int { kAggGeneric = 0, kAggCountXor = 1, kAggCountProduct = 2 };
+// kAggRows: both sides carry row positions; a match first compares the
+// minor keys (when given), then reads the payloads by row.
+enum : int { kAggGeneric = 0, kAggCountXor = 1, kAggCountProduct = 2, kAggRows = 3 };
+
+// Columns a kAggRows match reads by row position (any may be null; the
+// minor-key columns are both set or both null).
+struct RowCols {
+  const int32_t *bmin, *pmin, *bpay, *ppay;
+};
 
 // Table slot of key k: Fibonacci hashing onto [0, cap) (multiply, then the
 // high word of hash * cap).  The keys of one partition share the low fmix32
@@ -336,14 +344,22 @@ __device__ __forceinline__ uint32_t table_slot(int32_t k, int bits, uint32_t cap
 }
 
 template <int kAgg>
-__device__ __forceinline__ void join_match(const gbj::AggSpec &spec, gbjd::Acc &acc, int64_t &a_cnt,
-                                           int64_t &a_sum, int32_t k, int32_t bv, int32_t pv) {
+__device__ __forceinline__ void join_match(const gbj::AggSpec &spec, const RowCols &rc, gbjd::Acc &acc,
+                                           int64_t &a_cnt, int64_t &a_sum, int32_t k, int32_t bv,
+                                           int32_t pv) {
   if (kAgg == kAggCountXor) {
     a_cnt += 1;
     a_sum += (int64_t)bv ^ (int64_t)pv;
   } else if (kAgg == kAggCountProduct) {
     a_cnt += 1;
     a_sum += (int64_t)bv * (int64_t)pv;
+  } else if (kAgg == kAggRows) {
+    // the minor-key check of the reference's partitioned join
+    // (gpu-partitioned-hash-join-chained.cpp:1284-1333)
+    if (rc.bmin && __ldg(rc.bmin + bv) != __ldg(rc.pmin + pv)) return;
+    const int64_t b = rc.bpay ? __ldg(rc.bpay + bv) : 0;
+    const int64_t p = rc.ppay ? __ldg(rc.ppay + pv) : 0;
+    acc.update(spec, k, b, p, bv, pv);
   } else {
     acc.update(spec, k, bv, pv, bv, pv);
   }
@@ -358,7 +374,7 @@ __global__ void __launch_bounds__(kThreads, kJoinCtas)
     k_radix_join(const int2 *__restrict__ R, const uint64_t *__restrict__ ro,
                  const int2 *__restrict__ S, const uint64_t *__restrict__ so,
                  const uint64_t *__restrict__ item_off, uint32_t P, int bits, uint64_t w,
-                 uint32_t sentinel_part, gbj::AggSpec spec, int64_t *out,
+                 uint32_t sentinel_part, gbj::AggSpec spec, RowCols rc, int64_t *out,
                  unsigned long long *item_ctr) {
   static_assert(2 * kRMax + 64 <= 65535, "16-bit index entries");
   constexpr uint32_t kCapMax = 2 * kRMax + 64;
@@ -468,7 +484,7 @@ __global__ void __launch_bounds__(kThreads, kJoinCtas)
         uint32_t hits = valid & before &
                         ((kk.x == k) | ((kk.y == k) << 1) | ((kk.z == k) << 2) | ((kk.w == k) << 3));
         while (hits) {
-          join_match<kAgg>(spec, acc, a_cnt, a_sum, k, tval[g0 + __ffs(hits) - 1], v);
+          join_match<kAgg>(spec, rc, acc, a_cnt, a_sum, k, tval[g0 + __ffs(hits) - 1], v);
           if (unique) return true;
           hits &= hits - 1;
         }
@@ -544,7 +560,7 @@ __global__ void __launch_bounds__(kThreads, kJoinCtas)
             if (idx == 0) break;
             const int2 bt = rp[idx - 1];
             if (bt.x == k) {
-              join_match<kAgg>(spec, acc, a_cnt, a_sum, k, bt.y, t[u].y);
+              join_match<kAgg>(spec, rc, acc, a_cnt, a_sum, k, bt.y, t[u].y);
               if (unique) break;
             }
             if (++hh == cap) hh = 0;
@@ -554,7 +570,7 @@ __global__ void __launch_bounds__(kThreads, kJoinCtas)
     }
     __syncthreads();
   }
-  if (kAgg != kAggGeneric) {
+  if (kAgg == kAggCountXor || kAgg == kAggCountProduct) {
     acc.v[0] = a_cnt;
     acc.v[1] = a_sum;
   }
@@ -571,8 +587,8 @@ constexpr size_t join_smem() {
 template <int kRMax, int kThreads, int kAgg>
 int launch_join(gbj_ctx *ctx, const int2 *R, const uint64_t *ro, const int2 *S,
                 const uint64_t *so, const uint64_t *item_off, uint32_t P, int bits,
-                uint64_t w, uint32_t sentinel_part, const AggSpec &spec, int64_t *out,
-                unsigned long long *ctr, cudaStream_t s) {
+                uint64_t w, uint32_t sentinel_part, const AggSpec &spec, const RowCols &rc,
+                int64_t *out, unsigned long long *ctr, cudaStream_t s) {
   const size_t smem = join_smem<kRMax, kThreads>();
   auto kern = k_radix_join<kRMax, kThreads, kAgg>;
   GBJ_CHECK_CUDA(ctx, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -581,7 +597,7 @@ int launch_join(gbj_ctx *ctx, const int2 *R, const uint64_t *ro, const int2 *S,
   GBJ_CHECK_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kThreads, smem));
   if (per_sm < 1) return set_error(ctx, GBJ_ERR_CUDA, "k_radix_join: no resident block fits");
   kern<<<ctx->sm_count * per_sm, kThreads, smem, s>>>(R, ro, S, so, item_off, P, bits, w,
-                                                     sentinel_part, spec, out, ctr);
+                                                     sentinel_part, spec, rc, out, ctr);
   return after_launch(ctx, "k_radix_join", s);
 }
 
@@ -606,7 +622,10 @@ int launch_tile_pass(gbj_ctx *ctx, const int32_t *keys, const int32_t *vals, con
 template <int kDigit>
 int partition_impl(gbj_ctx *ctx, const int32_t *keys, const int32_t *vals, uint64_t n, int shift,
                    int bits, int2 *out_pairs, int32_t *out_keys, int32_t *out_vals,
-                   uint64_t *offsets, cudaStream_t s) {
+                   uint64_t *offsets, cudaStream_t s, int passes) {
+  if ((passes == 1 && bits > 8) || (passes == 2 && bits < 2) || passes < 0 || passes > 2)
+    return set_error(ctx, GBJ_ERR_UNSUPPORTED,
+                     "partition: one pass takes at most 8 radix bits, two passes at least 2");
   const uint32_t P = 1u << bits, pmask = P - 1;
   Scratch scratch(ctx, s);
   uint32_t *hist, *cursor2;
@@ -627,7 +646,7 @@ int partition_impl(gbj_ctx *ctx, const int32_t *keys, const int32_t *vals, uint6
     GBJ_TRY(after_launch(ctx, "k_pid_hist", s));
   }
   GBJ_TRY(scan_u32_to_u64(ctx, hist, off, P, s));
-  if (bits <= 8) {
+  if (passes == 1 || (passes == 0 && bits <= 8)) {
     k_cursors<<<(P + 255) / 256, 256, 0, s>>>(off, P, 0, nullptr, cursor2, nullptr);
     GBJ_TRY(after_launch(ctx, "k_cursors", s));
     if (out_pairs)
@@ -672,12 +691,12 @@ namespace gbj {
 
 int partition_tuples(gbj_ctx *ctx, const int32_t *keys, const int32_t *vals, uint64_t n,
                      int digit, int shift, int bits, int2 *out_pairs, int32_t *out_keys,
-                     int32_t *out_vals, uint64_t *offsets, cudaStream_t s) {
+                     int32_t *out_vals, uint64_t *offsets, cudaStream_t s, int passes) {
   if (digit == GBJ_DIGIT_HASH)
     return partition_impl<GBJ_DIGIT_HASH>(ctx, keys, vals, n, shift, bits, out_pairs, out_keys,
-                                          out_vals, offsets, s);
+                                          out_vals, offsets, s, passes);
   return partition_impl<GBJ_DIGIT_KEY>(ctx, keys, vals, n, shift, bits, out_pairs, out_keys,
-                                       out_vals, offsets, s);
+                                       out_vals, offsets, s, passes);
 }
 
 }  // namespace gbj
@@ -706,17 +725,36 @@ int gbj_partition(gbj_ctx *ctx, const int32_t *d_keys, const int32_t *d_payload,
                           d_out_payload, d_offsets, s);
 }
 
-int gbj_radix_join_agg(gbj_ctx *ctx, const int32_t *d_build_keys,
-                       const int32_t *d_build_payload, uint64_t n_build,
-                       const int32_t *d_probe_keys, const int32_t *d_probe_payload,
-                       uint64_t n_probe, const gbj_radix_params *params, const gbj_agg *aggs,
-                       int32_t n_aggs, int64_t *d_out, void *stream) {
+}  // extern "C"
+
+// Shared body of gbj_radix_join_agg and gbj_radix_join_agg_minor.
+static int radix_join_impl(gbj_ctx *ctx, const int32_t *d_build_keys, const int32_t *d_build_minor,
+                           const int32_t *d_build_payload, uint64_t n_build,
+                           const int32_t *d_probe_keys, const int32_t *d_probe_minor,
+                           const int32_t *d_probe_payload, uint64_t n_probe,
+                           const gbj_radix_params *params, const gbj_agg *aggs, int32_t n_aggs,
+                           int64_t *d_out, void *stream) {
   if (!ctx || !d_out) return GBJ_ERR_INVALID;
   GBJ_TRY(validate_aggs(ctx, aggs, n_aggs));
   if (n_build >= (1ULL << 31) || n_probe >= (1ULL << 31))
     return set_error(ctx, GBJ_ERR_INVALID, "radix_join: inputs must have < 2^31 rows");
   if ((n_build && !d_build_keys) || (n_probe && !d_probe_keys))
     return set_error(ctx, GBJ_ERR_INVALID, "radix_join: null key column");
+  const bool minor = d_build_minor || d_probe_minor;
+  if (minor && ((n_build && !d_build_minor) || (n_probe && !d_probe_minor)))
+    return set_error(ctx, GBJ_ERR_INVALID,
+                     "radix_join: a minor key needs both sides (build_k_minor and probe_k_minor)");
+  // Every field of the parameters is honoured or refused.
+  if (params) {
+    if (params->bits < 0 || params->bits > kMaxPartBits || params->log_parts < 0 ||
+        params->log_parts > kMaxPartBits)
+      return set_error(ctx, GBJ_ERR_UNSUPPORTED, "radix_join: radix bits must be in [0, 15]");
+    if (params->passes < 0 || params->passes > 2)
+      return set_error(ctx, GBJ_ERR_UNSUPPORTED, "radix_join: passes must be 0 (auto), 1 or 2");
+    if (params->block != 0 && params->block != kJoinThreads)
+      return set_error(ctx, GBJ_ERR_UNSUPPORTED,
+                       "radix_join: the join kernel runs 1024 threads per block (block 0 or 1024)");
+  }
   AggSpec spec = make_spec(aggs, n_aggs);
   // Which value each side carries into the partitions.
   bool b_row = false, b_pay = false, p_row = false, p_pay = false;
@@ -731,11 +769,12 @@ int gbj_radix_join_agg(gbj_ctx *ctx, const int32_t *d_build_keys,
       default: break;
     }
   }
-  if ((b_row && b_pay) || (p_row && p_pay))
-    return set_error(ctx, GBJ_ERR_UNSUPPORTED,
-                     "radix_join: one side cannot carry both its payload and its row id");
   if ((b_pay && !d_build_payload && n_build) || (p_pay && !d_probe_payload && n_probe))
     return set_error(ctx, GBJ_ERR_INVALID, "radix_join: aggregate reads a missing payload");
+  // Row mode: both sides carry row positions and a match reads the minor
+  // keys and payloads by row (a composite key, or one side needing both its
+  // payload and its row id).
+  const bool by_rows = minor || (b_row && b_pay) || (p_row && p_pay);
   cudaStream_t s = pick_stream(ctx, stream);
   prof_mark(ctx, s);
   GBJ_TRY(init_agg_out(ctx, spec, d_out, s));
@@ -744,6 +783,7 @@ int gbj_radix_join_agg(gbj_ctx *ctx, const int32_t *d_build_keys,
   // ---- plan: fewest radix bits whose largest expected build partition
   //      (mean + 5 sd) fits the on-chip table; explicit params override ----
   constexpr int kRMax = kJoinRMax;
+  const int passes = params ? params->passes : 0;
   int bits = 1;
   while (bits < kMaxPartBits) {
     const double mean = (double)n_build / (double)(1u << bits);
@@ -754,11 +794,15 @@ int gbj_radix_join_agg(gbj_ctx *ctx, const int32_t *d_build_keys,
   if (!explicit_bits) {  // an autotuned choice for this size bucket, if any
     const int32_t tb = tuned_value(ctx, tune_key("radix", n_build, n_probe));
     if (tb > 0) bits = std::min<int>(tb, kMaxPartBits);
+    // a pinned pass count bounds the automatic choice
+    if (passes == 1) bits = std::min(bits, 8);
+    if (passes == 2) bits = std::max(bits, 2);
   }
-  if (params && params->log_parts > 0) bits = std::min(params->log_parts, kMaxPartBits);
-  if (params && params->bits > 0) bits = std::min(params->bits, kMaxPartBits);
-  if (params && params->passes > 2)
-    return set_error(ctx, GBJ_ERR_UNSUPPORTED, "radix_join: at most two partitioning passes");
+  if (params && params->log_parts > 0) bits = params->log_parts;
+  if (params && params->bits > 0) bits = params->bits;
+  if ((passes == 1 && bits > 8) || (passes == 2 && bits < 2))
+    return set_error(ctx, GBJ_ERR_UNSUPPORTED,
+                     "radix_join: one pass takes at most 8 radix bits, two passes at least 2");
   const uint32_t P = 1u << bits;
   const uint64_t w = 1u << 17;  // probe tuples per work item
   const uint32_t sentinel_part = gbjd::fmix32((uint32_t)INT32_MIN) & (P - 1);
@@ -773,23 +817,52 @@ int gbj_radix_join_agg(gbj_ctx *ctx, const int32_t *d_build_keys,
   GBJ_TRY(scratch.get(P + 1, &so));
   GBJ_TRY(scratch.get(P + 1, &items));
   GBJ_TRY(scratch.get(1, &ctr));
-  GBJ_TRY(partition_tuples(ctx, d_build_keys, b_pay ? d_build_payload : nullptr, n_build,
-                           GBJ_DIGIT_HASH, 0, bits, R, nullptr, nullptr, ro, s));
-  GBJ_TRY(partition_tuples(ctx, d_probe_keys, p_pay ? d_probe_payload : nullptr, n_probe,
-                           GBJ_DIGIT_HASH, 0, bits, S, nullptr, nullptr, so, s));
+  GBJ_TRY(partition_tuples(ctx, d_build_keys, b_pay && !by_rows ? d_build_payload : nullptr, n_build,
+                           GBJ_DIGIT_HASH, 0, bits, R, nullptr, nullptr, ro, s, passes));
+  GBJ_TRY(partition_tuples(ctx, d_probe_keys, p_pay && !by_rows ? d_probe_payload : nullptr, n_probe,
+                           GBJ_DIGIT_HASH, 0, bits, S, nullptr, nullptr, so, s, passes));
   k_join_items<<<(P + 255) / 256, 256, 0, s>>>(ro, so, P, kRMax, w, items);
   GBJ_TRY(after_launch(ctx, "k_join_items", s));
   GBJ_TRY(scan_u64(ctx, items, items, P, s));
   GBJ_CHECK_CUDA(ctx, cudaMemsetAsync(ctr, 0, sizeof(unsigned long long), s));
+  const RowCols rc{minor ? d_build_minor : nullptr, minor ? d_probe_minor : nullptr,
+                   b_pay ? d_build_payload : nullptr, p_pay ? d_probe_payload : nullptr};
+  if (by_rows)
+    return launch_join<kRMax, kJoinThreads, kAggRows>(ctx, R, ro, S, so, items, P, bits, w, sentinel_part,
+                                                      spec, rc, d_out, ctr, s);
   const bool two = spec.n == 2 && spec.op[0] == GBJ_AGG_COUNT && spec.op[1] == GBJ_AGG_SUM;
   if (two && spec.operand[1] == GBJ_VAL_ROWID_XOR)
     return launch_join<kRMax, kJoinThreads, kAggCountXor>(ctx, R, ro, S, so, items, P, bits, w, sentinel_part,
-                                                  spec, d_out, ctr, s);
+                                                          spec, rc, d_out, ctr, s);
   if (two && spec.operand[1] == GBJ_VAL_PRODUCT)
     return launch_join<kRMax, kJoinThreads, kAggCountProduct>(ctx, R, ro, S, so, items, P, bits, w,
-                                                      sentinel_part, spec, d_out, ctr, s);
+                                                              sentinel_part, spec, rc, d_out, ctr, s);
   return launch_join<kRMax, kJoinThreads, kAggGeneric>(ctx, R, ro, S, so, items, P, bits, w, sentinel_part,
-                                               spec, d_out, ctr, s);
+                                                       spec, rc, d_out, ctr, s);
+}
+
+extern "C" {
+
+int gbj_radix_join_agg(gbj_ctx *ctx, const int32_t *d_build_keys,
+                       const int32_t *d_build_payload, uint64_t n_build,
+                       const int32_t *d_probe_keys, const int32_t *d_probe_payload,
+                       uint64_t n_probe, const gbj_radix_params *params, const gbj_agg *aggs,
+                       int32_t n_aggs, int64_t *d_out, void *stream) {
+  return radix_join_impl(ctx, d_build_keys, nullptr, d_build_payload, n_build, d_probe_keys, nullptr,
+                         d_probe_payload, n_probe, params, aggs, n_aggs, d_out, stream);
+}
+
+int gbj_radix_join_agg_minor(gbj_ctx *ctx, const int32_t *d_build_keys,
+                             const int32_t *d_build_minor, const int32_t *d_build_payload,
+                             uint64_t n_build, const int32_t *d_probe_keys,
+                             const int32_t *d_probe_minor, const int32_t *d_probe_payload,
+                             uint64_t n_probe, const gbj_radix_params *params,
+                             const gbj_agg *aggs, int32_t n_aggs, int64_t *d_out,
+                             void *stream) {
+  if (ctx && ((n_build && !d_build_minor) || (n_probe && !d_probe_minor)))
+    return set_error(ctx, GBJ_ERR_INVALID, "radix_join_minor: both minor-key columns are required");
+  return radix_join_impl(ctx, d_build_keys, d_build_minor, d_build_payload, n_build, d_probe_keys,
+                         d_probe_minor, d_probe_payload, n_probe, params, aggs, n_aggs, d_out, stream);
 }
 
 }  // extern "C"

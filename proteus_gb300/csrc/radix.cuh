@@ -10,11 +10,12 @@ constexpr int kMaxPartBits = 15;
 // into a contiguous, partition-major output.  vals == nullptr carries the
 // row position.  Output either AoS (out_pairs != nullptr, int2 {key, val})
 // or SoA (out_keys / out_vals).  offsets gets 2^bits + 1 entries.
-// Count pass (per-CTA segment histograms) -> scan -> scatter pass; no
-// global atomics, tuples keep no particular order inside a partition.
+// One histogram pass, then one tile pass per digit group; tuples keep no
+// particular order inside a partition.  passes: 0 = one pass up to 8 bits,
+// two above; 1 = one pass (bits <= 8); 2 = two passes (bits >= 2).
 int partition_tuples(gbj_ctx *ctx, const int32_t *keys, const int32_t *vals,
                      uint64_t n, int digit, int shift, int bits,
                      int2 *out_pairs, int32_t *out_keys, int32_t *out_vals,
-                     uint64_t *offsets, cudaStream_t s);
+                     uint64_t *offsets, cudaStream_t s, int passes = 0);
 
 }  // namespace gbj

@@ -144,17 +144,32 @@ class Context:
         return b, p, cnt
 
     def radix_join_agg(self, bkeys, bpay, pkeys, ppay, aggs, out=None, bits=0, passes=0,
-                       log_parts=0, stream=None):
+                       log_parts=0, block=0, stream=None):
         import torch
 
         if out is None:
             out = torch.empty(len(aggs), dtype=torch.int64, device=bkeys.device)
-        prm = abi.RadixParams(bits, passes, 0, log_parts)
+        prm = abi.RadixParams(bits, passes, block, log_parts)
         arr = abi.aggs_array(aggs)
         self.check(self.lib.gbj_radix_join_agg(self.handle, _ptr(bkeys), _ptr(bpay), bkeys.numel(),
                                                _ptr(pkeys), _ptr(ppay), pkeys.numel(),
                                                C.byref(prm), arr, len(aggs), _ptr(out),
                                                self._s(stream)))
+        return out
+
+    def radix_join_agg_minor(self, bkeys, bminor, bpay, pkeys, pminor, ppay, aggs, out=None,
+                             bits=0, passes=0, stream=None):
+        """Partitioned join on (key, minor key): pairs need both equal."""
+        import torch
+
+        if out is None:
+            out = torch.empty(len(aggs), dtype=torch.int64, device=bkeys.device)
+        prm = abi.RadixParams(bits, passes, 0, 0)
+        arr = abi.aggs_array(aggs)
+        self.check(self.lib.gbj_radix_join_agg_minor(
+            self.handle, _ptr(bkeys), _ptr(bminor), _ptr(bpay), bkeys.numel(), _ptr(pkeys),
+            _ptr(pminor), _ptr(ppay), pkeys.numel(), C.byref(prm), arr, len(aggs), _ptr(out),
+            self._s(stream)))
         return out
 
     def partition(self, keys, payload, bits, shift=0, digit=abi.DIGIT_HASH, stream=None):
@@ -345,46 +360,7 @@ class Context:
 
 
 # ------------------------------------------------------ host generators
-def _np_ptr(a):
-    return a.ctypes.data_as(C.c_void_p) if a is not None else None
-
-
-def gen_build_side(seed: int, n: int, payload=True, threads=0):
-    lib = abi.load()
-    k = np.empty(n, dtype=np.int32)
-    p = np.empty(n, dtype=np.int32) if payload else None
-    rc = lib.gbj_gen_build_side(seed, n, _np_ptr(k), _np_ptr(p), threads)
-    if rc:
-        raise abi.GbjError(rc, "gen_build_side")
-    return k, p
-
-
-def gen_probe_uniform(seed: int, n: int, n_build: int, payload=True, threads=0):
-    lib = abi.load()
-    k = np.empty(n, dtype=np.int32)
-    p = np.empty(n, dtype=np.int32) if payload else None
-    rc = lib.gbj_gen_probe_uniform(seed, n, n_build, _np_ptr(k), _np_ptr(p), threads)
-    if rc:
-        raise abi.GbjError(rc, "gen_probe_uniform")
-    return k, p
-
-
-def gen_probe_zipf(seed: int, n: int, n_build: int, theta: float, hit_rate=0.5, payload=False,
-                   threads=0):
-    lib = abi.load()
-    k = np.empty(n, dtype=np.int32)
-    p = np.empty(n, dtype=np.int32) if payload else None
-    rc = lib.gbj_gen_probe_zipf(seed, n, n_build, theta, hit_rate, _np_ptr(k), _np_ptr(p), threads)
-    if rc:
-        raise abi.GbjError(rc, "gen_probe_zipf")
-    return k, p
-
-
-def gen_groupby(seed: int, n: int, cardinality: int, theta: float = 0.0, threads=0):
-    lib = abi.load()
-    k = np.empty(n, dtype=np.int32)
-    v = np.empty(n, dtype=np.int32)
-    rc = lib.gbj_gen_groupby(seed, n, cardinality, theta, _np_ptr(k), _np_ptr(v), threads)
-    if rc:
-        raise abi.GbjError(rc, "gen_groupby")
-    return k, v
+# The seeded synthetic inputs live in their own library (datagen), so that a
+# process can generate them without loading libgbjoin.so; re-exported here
+# for callers of this module.
+from datagen import gen_build_side, gen_groupby, gen_probe_uniform, gen_probe_zipf  # noqa: E402,F401

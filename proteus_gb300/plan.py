@@ -99,9 +99,16 @@ class RelBuilder:
         return RelBuilder(n)
 
     def partitioned_join(self, build: "RelBuilder", build_k: Expr, probe_k: Expr,
-                         max_build_input_size: int = 0, max_probe_input_size: int = 0):
+                         max_build_input_size: int = 0, max_probe_input_size: int = 0,
+                         build_k_minor: Expr | None = None, probe_k_minor: Expr | None = None):
+        """partitioned-hashjoin-chained; with minor keys a pair also needs
+        build_k_minor == probe_k_minor."""
         n = {"operator": "partitioned-hashjoin-chained", "build_input": build.node,
              "probe_input": self.node, "build_k": build_k.node, "probe_k": probe_k.node}
+        if build_k_minor is not None:
+            n["build_k_minor"] = build_k_minor.node
+        if probe_k_minor is not None:
+            n["probe_k_minor"] = probe_k_minor.node
         if max_build_input_size:
             n["maxBuildInputSize"] = max_build_input_size
         if max_probe_input_size:
@@ -121,6 +128,13 @@ class RelBuilder:
                            "e": [{"e": x.node, "m": m, "packet": 1, "offset": 32 * (i + 1)}
                                  for i, (x, m) in enumerate(e)],
                            "hash_bits": hash_bits, "maxInputSize": max_input_size})
+
+    def nest(self, f: Expr, e, accumulators, labels, p: Expr | None = None) -> "RelBuilder":
+        """The RadixNest operator ("nest"): group by f over the rows p keeps."""
+        return RelBuilder({"operator": "nest", "input": self.node, "f": f.node, "g": f.node,
+                           "p": (p if p is not None else lit(True)).node,
+                           "e": [x.node for x in e], "accumulator": list(accumulators),
+                           "aggrLabels": list(labels), "fields": [f.node]})
 
     def reduce(self, e, accumulators) -> "RelBuilder":
         return RelBuilder({"operator": "reduce", "input": self.node, "e": [x.node for x in e],

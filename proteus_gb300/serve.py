@@ -30,7 +30,9 @@ class QueryShape:
 
 def gen_shapes(seed: int, n: int, log_build=(10, 24), log_probe=(14, 27), log_card=(4, 16)) -> list:
     """Seeded query shapes (draws from gbj_gen_rand: identical everywhere)."""
-    lib = abi.load()
+    import datagen
+
+    lib = datagen.load()
     out = []
     for q in range(n):
         def u(i, q=q):
@@ -46,22 +48,17 @@ def gen_shapes(seed: int, n: int, log_build=(10, 24), log_probe=(14, 27), log_ca
 
 def gen_query(shape: QueryShape, threads=0):
     """Host columns (build keys, build groups, probe keys, probe values)."""
-    lib = abi.load()
-    bk = np.empty(shape.n_build, np.int32)
-    bg = np.empty(shape.n_build, np.int32)
-    pk = np.empty(shape.n_probe, np.int32)
-    pv = np.empty(shape.n_probe, np.int32)
-    rc = lib.gbj_gen_serve_query(shape.seed, shape.n_build, shape.n_probe, shape.match_rate,
-                                 shape.cardinality, *[a.ctypes.data_as(C.c_void_p) for a in (bk, bg, pk, pv)],
-                                 threads)
-    if rc:
-        raise abi.GbjError(rc, "gen_serve_query")
-    return bk, bg, pk, pv
+    import datagen
+
+    return datagen.gen_serve_query(shape.seed, shape.n_build, shape.n_probe, shape.match_rate,
+                                   shape.cardinality, threads)
 
 
 def poisson_arrivals(seed: int, n: int, rate: float) -> np.ndarray:
     """Arrival times (s) of a Poisson process of `rate` queries/s."""
-    lib = abi.load()
+    import datagen
+
+    lib = datagen.load()
     u = np.array([(int(lib.gbj_gen_rand(seed, 0x5F00, i)) >> 11) * (1.0 / (1 << 53)) for i in range(n)])
     return np.cumsum(-np.log1p(-u) / rate)
 

@@ -43,12 +43,9 @@ _S_DIM, _S_FACT, _S_QUERY = 0x5300, 0x5400, 0x5A00
 
 
 def _uniform(seed: int, stream: int, n: int, lo: int, hi: int, threads=0) -> np.ndarray:
-    lib = abi.load()
-    out = np.empty(n, dtype=np.int32)
-    rc = lib.gbj_gen_uniform_i32(seed, stream, n, lo, hi, out.ctypes.data_as(C.c_void_p), threads)
-    if rc:
-        raise abi.GbjError(rc, "gen_uniform_i32")
-    return out
+    import datagen
+
+    return datagen.gen_uniform_i32(seed, stream, n, lo, hi, threads)
 
 
 @dataclass
@@ -125,7 +122,9 @@ class Query:
 
 def gen_queries(seed: int, n_queries: int, dims: list) -> list:
     """Seeded query variants (draws from gbj_gen_rand, identical everywhere)."""
-    lib = abi.load()
+    import datagen
+
+    lib = datagen.load()
     nd = len(dims)
     out = []
     for q in range(n_queries):

@@ -12,7 +12,7 @@
    the generator reproduces them.
 
 Run from the repository root:  python tests/golden/make_golden.py
-(requires the reference tree at /root/reference or $PROTEUS_REF).
+(requires the reference source tree named by $PROTEUS_REF).
 """
 from __future__ import annotations
 
@@ -24,10 +24,15 @@ import sys
 
 import numpy as np
 
+
 ROOT = os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
 sys.path.insert(0, ROOT)
-REF = os.environ.get("PROTEUS_REF", "/root/reference")
+REF = os.environ.get("PROTEUS_REF", "")
+if not REF:
+    raise SystemExit("set PROTEUS_REF to the reference source tree")
 OUT = os.path.dirname(os.path.abspath(__file__))
+
+import datagen  # noqa: E402  (the repository root is on sys.path now)
 
 
 def read_csv(rel, delim, cols):
@@ -175,7 +180,7 @@ def partition_ht_agg_cases():
     cases = []
     for seed, n, span in ((21, 1 << 12, 1 << 40), (22, 1 << 16, 1 << 62), (23, 50001, 1 << 20),
                           (24, 1 << 17, 1 << 63)):
-        keys = np.array([int(lib.gbj_gen_rand(seed, 0x6A00, i)) % span for i in range(n)], dtype=np.uint64)
+        keys = np.array([int(datagen.load().gbj_gen_rand(seed, 0x6A00, i)) % span for i in range(n)], dtype=np.uint64)
         keys = keys.view(np.int64) - (np.int64(span // 2) if span < (1 << 63) else 0)
         counts, ok, orows = O.ref_partition_ht_agg(keys)
         cases.append({
@@ -195,7 +200,7 @@ def partition_ht_agg_cases():
 
 
 def _i64_keys(lib, seed, n, span, salt):
-    keys = np.array([int(lib.gbj_gen_rand(seed, salt, i)) % span for i in range(n)], dtype=np.uint64)
+    keys = np.array([int(datagen.load().gbj_gen_rand(seed, salt, i)) % span for i in range(n)], dtype=np.uint64)
     return keys.view(np.int64) - (np.int64(span // 2) if span < (1 << 63) else 0)
 
 
@@ -239,16 +244,60 @@ def nest_i64_cases():
     }
 
 
+# The reference's own plan files over its CSV test inputs
+# (tests/olap/tests-plan-parsing.cpp runs the first five and compares with
+# tests/olap/outputs/tests-plan-parsing/*-log.json; the GPU ones have no
+# golden output, their tests compare with the oracle).  Plans that read
+# float columns (reduce-twofields-scan, reduce-select-gpu) are left out:
+# the catalog here holds int32 columns.
+PLAN_FILES = [
+    ("reduce-scan", "tests/inputs/plans/reduce-scan.json",
+     "tests/olap/outputs/tests-plan-parsing/reduce-scan-log.json"),
+    ("reduce-join", "tests/inputs/plans/reduce-join.json",
+     "tests/olap/outputs/tests-plan-parsing/reduce-join-log.json"),
+    ("reduce-nest", "tests/inputs/plans/reduce-nest.json",
+     "tests/olap/outputs/tests-plan-parsing/reduce-nest-log.json"),
+    ("reduce-select", "tests/inputs/plans/reduce-select.json",
+     "tests/olap/outputs/tests-plan-parsing/reduce-select-log.json"),
+    ("reduce-multinest", "tests/inputs/plans/reduce-multinest.json",
+     "tests/olap/outputs/tests-plan-parsing/reduce-multinest-log.json"),
+    ("gpu-group-by", "tests/inputs/plans/gpu-group-by.json", None),
+    ("reduce-scan-gpu", "tests/inputs/plans/reduce-scan-gpu.json", None),
+]
+
+
+def reference_plans():
+    plans = []
+    for name, plan, golden in PLAN_FILES:
+        entry = {"name": name, "plan_file": plan, "plan": read_text(plan)}
+        if golden:
+            entry["golden_file"] = golden
+            entry["expected"] = json.loads(read_text(golden))
+        plans.append(entry)
+    return {
+        "about": "The reference's plan files over tests/inputs/{sailors,reserves}.csv, verbatim, with the "
+                 "expected outputs of tests/olap/tests-plan-parsing.cpp where the reference has them "
+                 "(compared unordered, as runAndVerify does).  Columns: reference_cases.json tables.",
+        "plans": plans,
+    }
+
+
+GENERATORS = {
+    "reference_cases": reference_cases,
+    "rjstepwise_cases": rjstepwise_cases,
+    "partition_ht_agg_cases": partition_ht_agg_cases,
+    "nest_i64_cases": nest_i64_cases,
+    "reference_plans": reference_plans,
+}
+
+
 def main():
-    with open(os.path.join(OUT, "reference_cases.json"), "w") as f:
-        json.dump(reference_cases(), f, indent=1)
-    with open(os.path.join(OUT, "rjstepwise_cases.json"), "w") as f:
-        json.dump(rjstepwise_cases(), f, indent=1)
-    with open(os.path.join(OUT, "partition_ht_agg_cases.json"), "w") as f:
-        json.dump(partition_ht_agg_cases(), f, indent=1)
-    with open(os.path.join(OUT, "nest_i64_cases.json"), "w") as f:
-        json.dump(nest_i64_cases(), f, indent=1)
-    print("wrote", OUT)
+    """python tests/golden/make_golden.py [name ...] (default: every fixture)."""
+    names = sys.argv[1:] or list(GENERATORS)
+    for name in names:
+        with open(os.path.join(OUT, name + ".json"), "w") as f:
+            json.dump(GENERATORS[name](), f, indent=1)
+    print("wrote", ", ".join(names), "to", OUT)
 
 
 if __name__ == "__main__":

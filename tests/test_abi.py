@@ -7,35 +7,58 @@ import re
 import numpy as np
 import pytest
 
+import datagen
 from proteus_gb300 import abi, engine
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 
-def declared_symbols():
+def declared_symbols(header=None):
+    """gbj_* entry points declared in include/*.h (or in one header)."""
     names = set()
     inc = os.path.join(ROOT, "include")
     for f in os.listdir(inc):
-        if f.endswith(".h"):
+        if f.endswith(".h") and (header is None or f == header):
             src = open(os.path.join(inc, f)).read()
             src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
             names |= set(re.findall(r"\b(gbj_[a-z0-9_]+)\s*\(", src))
     return names
 
 
-def test_exports_every_declared_symbol(lib):
-    names = declared_symbols()
-    assert len(names) >= 25
-    missing = [n for n in sorted(names) if getattr(lib, n, None) is None]
+# each header, the library exporting it and its ctypes binding
+LIBRARIES = {"gbjoin.h": (abi.load, abi.SIGNATURES), "gbj_datagen.h": (datagen.load, datagen.SIGNATURES)}
+
+
+def test_every_header_has_a_library():
+    headers = sorted(f for f in os.listdir(os.path.join(ROOT, "include")) if f.endswith(".h"))
+    assert headers == sorted(LIBRARIES)
+
+
+@pytest.mark.parametrize("header", sorted(LIBRARIES))
+def test_exports_every_declared_symbol(lib, header):
+    load, _ = LIBRARIES[header]
+    names = declared_symbols(header)
+    assert len(names) >= 10
+    so = load()
+    missing = [n for n in sorted(names) if getattr(so, n, None) is None]
     assert not missing, missing
 
 
-def test_binding_covers_header(lib):
-    names = declared_symbols()
-    unbound = sorted(n for n in names if n not in abi.SIGNATURES)
+@pytest.mark.parametrize("header", sorted(LIBRARIES))
+def test_binding_covers_header(lib, header):
+    _, sigs = LIBRARIES[header]
+    names = declared_symbols(header)
+    unbound = sorted(n for n in names if n not in sigs)
     assert not unbound, unbound
-    stale = sorted(n for n in abi.SIGNATURES if n not in names)
+    stale = sorted(n for n in sigs if n not in names)
     assert not stale, stale
+
+
+def test_generators_live_apart_from_the_gpu_library(lib):
+    """The generators are not in libgbjoin.so: a process that only generates
+    inputs (the benchmark's CPU arm) never maps the GPU library."""
+    assert getattr(lib, "gbj_gen_rand", None) is None
+    assert not any(n.startswith("gbj_gen_") for n in declared_symbols("gbjoin.h"))
 
 
 def test_ctx_create_without_gpu_fails_cleanly(lib):
@@ -89,7 +112,7 @@ def test_probe_zipf_shape(lib, theta):
 
 def test_zipf_sampler_distribution(lib):
     n, theta = 100, 1.0
-    xs = np.array([lib.gbj_gen_zipf(9, 1, n, theta, i) for i in range(40000)])
+    xs = np.array([datagen.load().gbj_gen_zipf(9, 1, n, theta, i) for i in range(40000)])
     assert xs.min() >= 1 and xs.max() <= n
     hn = sum(1.0 / i for i in range(1, n + 1))
     for r in (1, 2, 10):
@@ -98,9 +121,9 @@ def test_zipf_sampler_distribution(lib):
 
 def test_deterministic_math(lib):
     for x in (1e-300, 1e-5, 0.3, 1.0, 1.5, 2.0, 10.0, 12345.678, 1e300):
-        assert abs(lib.gbj_gen_det_log(x) - math.log(x)) <= 1e-14 * max(1.0, abs(math.log(x)))
+        assert abs(datagen.load().gbj_gen_det_log(x) - math.log(x)) <= 1e-14 * max(1.0, abs(math.log(x)))
     for x in (-700.0, -5.0, -1e-3, 0.0, 0.5, 1.0, 3.7, 100.0, 700.0):
-        assert abs(lib.gbj_gen_det_exp(x) - math.exp(x)) <= 1e-14 * math.exp(x)
+        assert abs(datagen.load().gbj_gen_det_exp(x) - math.exp(x)) <= 1e-14 * math.exp(x)
 
 
 def test_generators_thread_count_independent(lib):

@@ -5,8 +5,10 @@ import json
 import os
 
 import numpy as np
+
 import pytest
 
+import datagen
 from gpu_util import dev, host
 from proteus_gb300 import abi
 
@@ -15,7 +17,7 @@ pytestmark = pytest.mark.gpu
 
 def _keys(lib, c):
     span = int(c["span"])
-    keys = np.array([int(lib.gbj_gen_rand(c["seed"], 0x6A00, i)) % span for i in range(c["n"])], dtype=np.uint64)
+    keys = np.array([int(datagen.load().gbj_gen_rand(c["seed"], 0x6A00, i)) % span for i in range(c["n"])], dtype=np.uint64)
     return keys.view(np.int64) - (np.int64(span // 2) if span < (1 << 63) else 0)
 
 

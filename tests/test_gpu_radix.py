@@ -98,12 +98,73 @@ def test_radix_join_explicit_bits(ctx, oracle, bits):
     assert host(out).tolist() == oracle.join_agg(rk, None, sk, None, CONFIG2_AGGS)
 
 
-def test_radix_join_unsupported_mix(ctx):
-    rk, rp = engine.gen_build_side(1, 1000)
+def test_radix_join_payload_and_rowid_on_one_side(ctx, oracle):
+    """A side read both as payload and as row id runs in row mode."""
+    rng = np.random.default_rng(8)
+    rk = rng.integers(0, 3000, 20000).astype(np.int32)
+    rp = rng.integers(-10**6, 10**6, 20000).astype(np.int32)
+    sk = rng.integers(-10, 3100, 70001).astype(np.int32)
+    sp = rng.integers(-10**6, 10**6, 70001).astype(np.int32)
+    aggs = [(abi.AGG_SUM, abi.VAL_BUILD), (abi.AGG_SUM, abi.VAL_BUILD_ROWID),
+            (abi.AGG_MAX, abi.VAL_PRODUCT), (abi.AGG_SUM, abi.VAL_ROWID_XOR),
+            (abi.AGG_MIN, abi.VAL_PROBE), (abi.AGG_COUNT, abi.VAL_ONE)]
+    out = ctx.radix_join_agg(dev(rk), dev(rp), dev(sk), dev(sp), aggs)
+    ctx.sync()
+    assert host(out).tolist() == oracle.join_agg(rk, rp, sk, sp, aggs)
+
+
+@pytest.mark.parametrize("n_build,n_probe,bits", [(30000, 200003, 0), (1 << 18, 1 << 20, 12),
+                                                  (5000, 40000, 3)])
+def test_radix_join_minor_key(ctx, oracle, n_build, n_probe, bits):
+    """Composite keys: the major key repeats, the minor key tells rows apart
+    (build_k_minor / probe_k_minor)."""
+    rng = np.random.default_rng(n_build + bits)
+    bk = rng.integers(0, n_build // 8 + 1, n_build).astype(np.int32)
+    bm = rng.integers(0, 8, n_build).astype(np.int32)
+    bp = rng.integers(-1000, 1000, n_build).astype(np.int32)
+    pk = rng.integers(0, n_build // 8 + 40, n_probe).astype(np.int32)
+    pm = rng.integers(0, 9, n_probe).astype(np.int32)
+    pp = rng.integers(-1000, 1000, n_probe).astype(np.int32)
+    aggs = [(abi.AGG_COUNT, abi.VAL_ONE), (abi.AGG_SUM, abi.VAL_PRODUCT),
+            (abi.AGG_SUM, abi.VAL_ROWID_XOR), (abi.AGG_MAX, abi.VAL_BUILD),
+            (abi.AGG_MIN, abi.VAL_PROBE), (abi.AGG_OR, abi.VAL_BUILD_KEY),
+            (abi.AGG_AND, abi.VAL_PROBE)]
+    out = ctx.radix_join_agg_minor(dev(bk), dev(bm), dev(bp), dev(pk), dev(pm), dev(pp), aggs,
+                                   bits=bits)
+    ctx.sync()
+    exp = oracle.radix_join_agg_minor(bk, bm, bp, pk, pm, pp, aggs, threads=cpu_threads())
+    assert host(out).tolist() == exp
+    # the minor key removes matches the major key alone would count
+    major = oracle.radix_join_agg(bk, None, pk, None, aggs[:1], threads=cpu_threads())
+    assert exp[0] < major[0]
+
+
+def test_radix_join_minor_key_needs_both_sides(ctx):
+    e = dev(np.arange(10, dtype=np.int32))
+    with pytest.raises(abi.GbjError) as err:
+        ctx.radix_join_agg_minor(e, e, None, e, None, None, [(abi.AGG_COUNT, abi.VAL_ONE)])
+    assert err.value.code == abi.ERR_INVALID
+
+
+@pytest.mark.parametrize("kw", [dict(block=512), dict(passes=3), dict(passes=1, bits=9),
+                                dict(passes=2, bits=1), dict(bits=16)])
+def test_radix_params_refused(ctx, kw):
+    """Parameters the join cannot honour are refused, never ignored."""
+    rk, _ = engine.gen_build_side(1, 1000, payload=False)
     with pytest.raises(abi.GbjError) as e:
-        ctx.radix_join_agg(dev(rk), dev(rp), dev(rk), dev(rp),
-                           [(abi.AGG_SUM, abi.VAL_BUILD), (abi.AGG_SUM, abi.VAL_BUILD_ROWID)])
+        ctx.radix_join_agg(dev(rk), None, dev(rk), None, CONFIG2_AGGS, **kw)
     assert e.value.code == abi.ERR_UNSUPPORTED
+
+
+@pytest.mark.parametrize("passes,bits", [(1, 0), (1, 6), (2, 4), (2, 0), (0, 9)])
+def test_radix_params_passes_honoured(ctx, oracle, passes, bits):
+    rk, _ = engine.gen_build_side(4, 1 << 16, payload=False)
+    sk, _ = engine.gen_probe_zipf(4, 1 << 19, 1 << 16, 0.5, 0.5)
+    out = ctx.radix_join_agg(dev(rk), None, dev(sk), None, CONFIG2_AGGS, bits=bits, passes=passes,
+                             block=1024 if bits else 0)
+    ctx.sync()
+    assert host(out).tolist() == oracle.radix_join_agg(rk, None, sk, None, CONFIG2_AGGS,
+                                                       threads=cpu_threads())
 
 
 def test_radix_join_empty(ctx, oracle):

@@ -3,8 +3,10 @@ RJStepwise / partitionHT compiled from source (committed counts)."""
 import hashlib
 
 import numpy as np
+
 import pytest
 
+import datagen
 from proteus_gb300 import abi, engine
 
 COUNT1 = (abi.AGG_COUNT, abi.VAL_ONE)
@@ -138,7 +140,7 @@ def _agg_keys(lib, c):
     import numpy as np
 
     span = int(c["span"])
-    keys = np.array([int(lib.gbj_gen_rand(c["seed"], 0x6A00, i)) % span for i in range(c["n"])], dtype=np.uint64)
+    keys = np.array([int(datagen.load().gbj_gen_rand(c["seed"], 0x6A00, i)) % span for i in range(c["n"])], dtype=np.uint64)
     return keys.view(np.int64) - (np.int64(span // 2) if span < (1 << 63) else 0)
 
 
@@ -166,7 +168,7 @@ def test_partition_ht_agg_matches_reference_goldens(lib, oracle):
 def _i64_keys(lib, seed, n, span, salt):
     import numpy as np
 
-    keys = np.array([int(lib.gbj_gen_rand(seed, salt, i)) % span for i in range(n)], dtype=np.uint64)
+    keys = np.array([int(datagen.load().gbj_gen_rand(seed, salt, i)) % span for i in range(n)], dtype=np.uint64)
     return keys.view(np.int64) - (np.int64(span // 2) if span < (1 << 63) else 0)
 
 
@@ -243,3 +245,34 @@ def test_int64_twins_equal_reference_live(oracle, seed):
     k, cnt, _, _, _ = oracle.nest_i64(r)
     assert (cnt == oracle.ref_nest_counts(r, k)).all()
     assert int(cnt.sum()) == len(r)
+
+
+def test_logical_accumulators(oracle):
+    """or / and (LogOrMonoid / LogAndMonoid): truth of the operand, 0/1 result;
+    identities false / true."""
+    col = np.array([0, 3, 0, -1], dtype=np.int32)
+    ops = [(abi.AGG_OR, abi.VAL_PROBE), (abi.AGG_AND, abi.VAL_PROBE)]
+    assert oracle.reduce(col, ops) == [1, 0]
+    assert oracle.reduce(col, ops, rows=np.array([1, 3], dtype=np.int32)) == [1, 1]
+    assert oracle.reduce(col, ops, rows=np.array([0, 2], dtype=np.int32)) == [0, 0]
+    assert oracle.reduce(col, ops, rows=np.zeros(0, dtype=np.int32)) == [0, 1]
+
+
+def test_minor_key_join_brute_force(oracle):
+    """The minor-key restatement against a nested-loop join on (key, minor)."""
+    rng = np.random.default_rng(3)
+    bk, bm = rng.integers(0, 40, 700).astype(np.int32), rng.integers(0, 3, 700).astype(np.int32)
+    pk, pm = rng.integers(0, 45, 1500).astype(np.int32), rng.integers(0, 3, 1500).astype(np.int32)
+    bp, pp = rng.integers(-9, 9, 700).astype(np.int32), rng.integers(-9, 9, 1500).astype(np.int32)
+    aggs = [COUNT1, (abi.AGG_SUM, abi.VAL_PRODUCT), (abi.AGG_SUM, abi.VAL_ROWID_XOR),
+            (abi.AGG_MIN, abi.VAL_BUILD_ROWID), (abi.AGG_AND, abi.VAL_PROBE)]
+    exp = [0, 0, 0, np.iinfo(np.int64).max, 1]
+    for j in range(len(pk)):
+        for i in np.nonzero((bk == pk[j]) & (bm == pm[j]))[0]:
+            exp[0] += 1
+            exp[1] += int(bp[i]) * int(pp[j])
+            exp[2] += int(i) ^ j
+            exp[3] = min(exp[3], int(i))
+            exp[4] &= int(pp[j] != 0)
+    for threads in (1, 3):
+        assert oracle.radix_join_agg_minor(bk, bm, bp, pk, pm, pp, aggs, bits=3, threads=threads) == exp

@@ -52,7 +52,7 @@ def allocating(ctx, bk, bp, pk, pp, aggs):
     return r
 
 
-def test_noalloc_matches_allocating_path_twice(lib, ctx):
+def test_noalloc_matches_allocating_path_twice(lib, ctx, oracle):
     # call 1: full-size plain join (2^20 build rows, the array's maximum)
     rk, rp = engine.gen_build_side(71, abi.NOALLOC_MAX_BUILD)
     sk, sp = engine.gen_probe_uniform(71, 1 << 22, abi.NOALLOC_MAX_BUILD)
@@ -70,6 +70,9 @@ def test_noalloc_matches_allocating_path_twice(lib, ctx):
     d2 = [dev(x) for x in (rk2, rp2, sk2, sp2)]
     got2 = host(noalloc(lib, *d2, AGGS)).tolist()
     assert got2 == allocating(ctx, *d2, AGGS)
+    # and against the CPU oracle (the reference's chained-hash semantics), so a
+    # fault shared by both GPU paths cannot pass unseen
+    assert got2 == oracle.join_agg(rk2, rp2, sk2, sp2, AGGS)
     # and the first join again, after the second one
     assert host(noalloc(lib, *d, AGGS)).tolist() == got1
 
