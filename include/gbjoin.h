@@ -83,6 +83,13 @@ int gbj_pool_alloc(gbj_ctx *ctx, uint64_t bytes, void **d_ptr);
 int gbj_pool_free(gbj_ctx *ctx, void *d_ptr);
 int gbj_pool_stats(gbj_ctx *ctx, uint64_t *capacity, uint64_t *in_use,
                    uint64_t *peak);
+/* Caps the bytes the pool hands out at `bytes` (0 = the whole pool): an
+ * allocation past the cap fails with GBJ_ERR_OOM as if the pool were full.
+ * The reference's MemoryManager has a fixed pool per device
+ * (core/platform/lib/memory/memory-manager.cpp); this is the knob that
+ * shrinks ours without re-creating the context, e.g. to leave room for other
+ * users of the device or to exercise the out-of-memory paths. */
+int gbj_ctx_set_pool_limit(gbj_ctx *ctx, uint64_t bytes);
 
 /* ---------------------------------------------------- fused aggregations */
 /* Aggregates computed on join matches, standing in for the parent Reduce
@@ -515,7 +522,22 @@ int gbj_server_wait(gbj_server *srv, uint64_t ticket, double timeout_s,
  * submitted, launched and seen complete; -1 for a stage not reached. */
 int gbj_server_times(gbj_server *srv, uint64_t ticket, double *submitted,
                      double *launched, double *completed);
-/* Waits for every submitted query. */
+/* Cancels a query that is still queued (not yet launched): it completes at
+ * once with status GBJ_ERR_CANCELLED and *cancelled = 1.  A query already
+ * launched or complete is left alone (*cancelled = 0).  The reference runs
+ * one query at a time with nothing queued to cancel; this is the serving
+ * loop's own control. */
+int gbj_server_cancel(gbj_server *srv, uint64_t ticket, int32_t *cancelled);
+/* paused != 0: the loop launches no new batches (batches in flight finish,
+ * submissions queue up); 0 resumes.  gbj_server_destroy resumes first. */
+int gbj_server_pause(gbj_server *srv, int32_t paused);
+/* Number of automatic retries so far: a query (or a registered table) whose
+ * distinct build groups outnumbered its expected_groups runs once more with
+ * a group table sized for n_build groups, which cannot overflow; only a
+ * query that still fails reports GBJ_ERR_CAPACITY. */
+int gbj_server_retries(gbj_server *srv, uint64_t *retried);
+/* Waits for every submitted query (a paused server must be resumed for its
+ * queued queries to complete). */
 int gbj_server_drain(gbj_server *srv);
 /* Totals: queries completed, batches launched, peak budget bytes held. */
 int gbj_server_stats(gbj_server *srv, uint64_t *completed, uint64_t *batches,

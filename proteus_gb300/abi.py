@@ -99,6 +99,7 @@ SIGNATURES = {
     "gbj_pool_alloc": (C.c_int, [vp, u64, P(vp)]),
     "gbj_pool_free": (C.c_int, [vp, vp]),
     "gbj_pool_stats": (C.c_int, [vp, P(u64), P(u64), P(u64)]),
+    "gbj_ctx_set_pool_limit": (C.c_int, [vp, u64]),
     "gbj_join_build": (C.c_int, [vp, vp, vp, u64, i32, u64, vp, P(vp)]),
     "gbj_join_probe_agg": (C.c_int, [vp, vp, vp, vp, u64, P(Agg), i32, vp, vp]),
     "gbj_join_probe_pairs": (C.c_int, [vp, vp, vp, vp, u64, vp, vp, u64, vp, vp]),
@@ -124,6 +125,9 @@ SIGNATURES = {
     "gbj_server_wait": (C.c_int, [vp, u64, dbl, P(i32)]),
     "gbj_server_times": (C.c_int, [vp, u64, P(dbl), P(dbl), P(dbl)]),
     "gbj_server_drain": (C.c_int, [vp]),
+    "gbj_server_cancel": (C.c_int, [vp, u64, P(i32)]),
+    "gbj_server_pause": (C.c_int, [vp, i32]),
+    "gbj_server_retries": (C.c_int, [vp, P(u64)]),
     "gbj_server_stats": (C.c_int, [vp, P(u64), P(u64), P(u64)]),
     "gbj_server_destroy": (C.c_int, [vp]),
     "gbj_server_register_table": (C.c_int, [vp, vp, vp, u64, u64, P(u64)]),

@@ -138,6 +138,10 @@ int pool_alloc(gbj_ctx *ctx, uint64_t bytes, cudaStream_t s, void **out) {
   uint64_t size = (bytes + kAlign - 1) / kAlign * kAlign;
   if (size == 0) size = kAlign;
   uint64_t off;
+  if (p.limit && p.in_use + size > p.limit)
+    return set_error(ctx, GBJ_ERR_OOM,
+                     "device pool limit reached: requested " + std::to_string(bytes) + " B, in use " +
+                         std::to_string(p.in_use) + " of the " + std::to_string(p.limit) + " B limit");
   pool_reclaim(p, s, false);
   if (!pool_take(p, size, &off)) {
     pool_reclaim(p, s, true);
@@ -364,6 +368,13 @@ int gbj_pool_alloc(gbj_ctx *ctx, uint64_t bytes, void **d_ptr) {
 int gbj_pool_free(gbj_ctx *ctx, void *d_ptr) {
   if (!ctx) return GBJ_ERR_INVALID;
   return pool_release(ctx, d_ptr, ctx->stream);
+}
+
+int gbj_ctx_set_pool_limit(gbj_ctx *ctx, uint64_t bytes) {
+  if (!ctx) return GBJ_ERR_INVALID;
+  std::lock_guard<std::mutex> g(ctx->mu);
+  ctx->pool.limit = bytes;
+  return GBJ_OK;
 }
 
 int gbj_pool_stats(gbj_ctx *ctx, uint64_t *capacity, uint64_t *in_use,

@@ -20,6 +20,7 @@ enum : uint32_t {
   GBJ_DEV_CAPACITY = 1u << 0,  // a table / output buffer overflowed
   GBJ_DEV_TIMEOUT = 1u << 1,   // a bounded spin gave up
   GBJ_DEV_INVALID = 1u << 2,   // a device-side consistency check failed
+  GBJ_DEV_GROUPS = 1u << 3,    // a served query's group table was full
 };
 
 // Upper bound on the iterations of any device-side spin (bounded waits).
@@ -33,6 +34,7 @@ struct Pool {
   // event has completed (or waits on it when nothing else fits).
   char *base = nullptr;
   uint64_t capacity = 0, in_use = 0, peak = 0;
+  uint64_t limit = 0;  // gbj_ctx_set_pool_limit: most bytes handed out (0 = capacity)
   std::map<uint64_t, uint64_t> free_by_off;  // offset -> size
   std::unordered_map<uint64_t, uint64_t> used;  // offset -> size
   struct Deferred {
@@ -70,7 +72,11 @@ struct gbj_ctx {
 };
 
 struct gbj_table {
-  uint64_t *slots = nullptr;  // {key:32 | (row+1):32}, 0 = empty
+  // wide: 16-byte slots {key, row+1, payload, 0}; else 8-byte {key, row+1};
+  // row+1 == 0 marks an empty slot.  The table metadata word follows the
+  // slots.
+  void *slots = nullptr;
+  bool wide = false;
   uint64_t mask = 0;          // slots - 1
   const int32_t *keys = nullptr;
   const int32_t *payload = nullptr;

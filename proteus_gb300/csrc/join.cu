@@ -27,17 +27,36 @@ constexpr int kThreads = 512;
 __device__ __forceinline__ uint64_t make_slot(int32_t key, uint64_t row) {
   return ((row + 1) << 32) | (uint32_t)key;
 }
-__device__ __forceinline__ int32_t slot_key(uint64_t e) { return (int32_t)(uint32_t)e; }
-__device__ __forceinline__ uint32_t slot_row(uint64_t e) { return (uint32_t)(e >> 32) - 1; }
+
+// One table slot as a probe sees it: narrow tables hold {key, row+1} in 8
+// bytes; wide tables (build sides with a payload) hold {key, row+1,
+// payload, 0} in 16 bytes, so a match needs no second, dependent load of
+// the build payload.  row1 == 0 marks an empty slot in both layouts.
+struct SlotView {
+  int32_t key;
+  uint32_t row1;
+  int32_t pay;
+};
+
+template <bool kWide>
+__device__ __forceinline__ SlotView slot_at(const void *__restrict__ slots, uint64_t h) {
+  if (kWide) {
+    const int4 e = __ldg(reinterpret_cast<const int4 *>(slots) + h);
+    return {e.x, (uint32_t)e.y, e.z};
+  }
+  const uint64_t e = __ldg(reinterpret_cast<const uint64_t *>(slots) + h);
+  return {(int32_t)(uint32_t)e, (uint32_t)(e >> 32), 0};
+}
 
 // meta[0] = 1 once a duplicate build key was seen (probes may then not stop
 // at the first match).  A row that finds no free slot latches
 // GBJ_DEV_CAPACITY into *status (status may be null where the table has 2n
-// slots and cannot fill).
+// slots and cannot fill).  The claim is a CAS on the {key, row+1} word; a
+// wide slot's payload is written after it (the probe runs in a later kernel).
+template <bool kWide>
 __global__ void __launch_bounds__(kThreads)
-    k_join_build(const int32_t *__restrict__ keys, uint64_t n,
-                 uint64_t *__restrict__ slots, uint64_t mask,
-                 uint32_t *__restrict__ meta, uint32_t *status) {
+    k_join_build(const int32_t *__restrict__ keys, const int32_t *__restrict__ payload, uint64_t n,
+                 void *__restrict__ slots, uint64_t mask, uint32_t *__restrict__ meta, uint32_t *status) {
   const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
   for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += stride) {
     const int32_t k = keys[i];
@@ -45,15 +64,18 @@ __global__ void __launch_bounds__(kThreads)
     uint64_t h = gbjd::fmix32((uint32_t)k) & mask;
     bool dup = false, placed = false;
     for (uint64_t probe = 0; probe <= mask; ++probe) {
-      uint64_t cur = *(volatile uint64_t *)&slots[h];
+      unsigned long long *w = kWide ? reinterpret_cast<unsigned long long *>(reinterpret_cast<int4 *>(slots) + h)
+                                    : reinterpret_cast<unsigned long long *>(slots) + h;
+      uint64_t cur = *(volatile uint64_t *)w;
       if (cur == 0) {
-        cur = atomicCAS((unsigned long long *)&slots[h], 0ull, (unsigned long long)entry);
+        cur = atomicCAS(w, 0ull, (unsigned long long)entry);
         if (cur == 0) {
+          if (kWide) reinterpret_cast<int32_t *>(w)[2] = payload[i];
           placed = true;
           break;
         }
       }
-      dup |= (slot_key(cur) == k);
+      dup |= ((int32_t)(uint32_t)cur == k);
       h = (h + 1) & mask;
     }
     if (dup) meta[0] = 1;
@@ -63,15 +85,15 @@ __global__ void __launch_bounds__(kThreads)
 
 enum : int { kAggGeneric = 0, kAggCountXor = 1, kAggCountProduct = 2 };
 
-// Probe with fused aggregate.  Four probe keys per thread: their first slot
-// loads are issued together so each thread keeps several L2 requests in
+// Probe with fused aggregate.  Eight probe keys per thread: their first slot
+// loads are issued together so each thread keeps eight L2 requests in
 // flight; chains past the first slot are walked afterwards.  kAgg selects
 // a specialised accumulator for the two aggregate lists the workloads use.
-template <bool kVec, int kAgg>
+template <bool kVec, int kAgg, bool kWide>
 __global__ void __launch_bounds__(kThreads)
     k_join_probe_agg(const int32_t *__restrict__ keys,
                      const int32_t *__restrict__ pay, uint64_t n,
-                     const uint64_t *__restrict__ slots, uint64_t mask,
+                     const void *__restrict__ slots, uint64_t mask,
                      const int32_t *__restrict__ bpay,
                      const uint32_t *__restrict__ meta, gbj::AggSpec spec,
                      int64_t *out) {
@@ -80,62 +102,64 @@ __global__ void __launch_bounds__(kThreads)
   acc.init(spec);
   int64_t a_cnt = 0, a_sum = 0;
   const bool unique = meta[0] == 0;
-  const uint64_t nq = n / 4;
   const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
-  auto match = [&](int32_t k, int64_t pv, uint64_t prow, uint64_t e) {
-    const uint32_t r = slot_row(e);
+  auto match = [&](int32_t k, int64_t pv, uint64_t prow, const SlotView &e) {
+    const uint32_t r = e.row1 - 1;
     if (kAgg == kAggCountXor) {
       a_cnt += 1;
       a_sum += (int64_t)r ^ (int64_t)prow;
-    } else if (kAgg == kAggCountProduct) {
-      a_cnt += 1;
-      a_sum += (int64_t)__ldg(&bpay[r]) * pv;
     } else {
-      const int64_t bv = bpay ? __ldg(&bpay[r]) : 0;
-      acc.update(spec, k, bv, pv, r, prow);
+      const int64_t bv = kWide ? (int64_t)e.pay : (bpay ? (int64_t)__ldg(&bpay[r]) : 0);
+      if (kAgg == kAggCountProduct) {
+        a_cnt += 1;
+        a_sum += bv * pv;
+      } else {
+        acc.update(spec, k, bv, pv, r, prow);
+      }
     }
   };
-  auto probe_one = [&](int32_t k, int64_t pv, uint64_t prow, uint64_t h,
-                       uint64_t e) {
+  auto probe_one = [&](int32_t k, int64_t pv, uint64_t prow, uint64_t h, SlotView e) {
     for (uint64_t step = 0; step <= mask; ++step) {
-      if (e == 0) break;
-      if (slot_key(e) == k) {
+      if (e.row1 == 0) break;
+      if (e.key == k) {
         match(k, pv, prow, e);
         if (unique) break;
       }
       h = (h + 1) & mask;
-      e = __ldg(&slots[h]);
+      e = slot_at<kWide>(slots, h);
     }
   };
+  uint64_t done = 0;
   if (kVec) {
-    for (uint64_t q = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; q < nq; q += stride) {
-      const int4 k4 = __ldcs(reinterpret_cast<const int4 *>(keys) + q);
-      int4 p4 = make_int4(0, 0, 0, 0);
-      if (pay) p4 = __ldcs(reinterpret_cast<const int4 *>(pay) + q);
-      const int32_t kk[4] = {k4.x, k4.y, k4.z, k4.w};
-      const int32_t pp[4] = {p4.x, p4.y, p4.z, p4.w};
-      uint64_t h[4], e[4];
+    const uint64_t n8 = n / 8;
+    const int4 *k4 = reinterpret_cast<const int4 *>(keys);
+    const int4 *p4 = reinterpret_cast<const int4 *>(pay);
+    for (uint64_t q = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; q < n8; q += stride) {
+      const int4 ka = __ldcs(k4 + 2 * q), kb = __ldcs(k4 + 2 * q + 1);
+      int4 pa = make_int4(0, 0, 0, 0), pb = pa;
+      if (pay) {
+        pa = __ldcs(p4 + 2 * q);
+        pb = __ldcs(p4 + 2 * q + 1);
+      }
+      const int32_t kk[8] = {ka.x, ka.y, ka.z, ka.w, kb.x, kb.y, kb.z, kb.w};
+      const int32_t pp[8] = {pa.x, pa.y, pa.z, pa.w, pb.x, pb.y, pb.z, pb.w};
+      uint64_t h[8];
+      SlotView e[8];
 #pragma unroll
-      for (int j = 0; j < 4; ++j) {
+      for (int j = 0; j < 8; ++j) {
         h[j] = gbjd::fmix32((uint32_t)kk[j]) & mask;
-        e[j] = __ldg(&slots[h[j]]);
+        e[j] = slot_at<kWide>(slots, h[j]);
       }
 #pragma unroll
-      for (int j = 0; j < 4; ++j) probe_one(kk[j], pp[j], q * 4 + j, h[j], e[j]);
+      for (int j = 0; j < 8; ++j) probe_one(kk[j], pp[j], q * 8 + j, h[j], e[j]);
     }
-    // tail (n % 4 rows) by the first threads of block 0
-    if (blockIdx.x == 0 && threadIdx.x < (n & 3)) {
-      const uint64_t i = nq * 4 + threadIdx.x;
-      const int32_t k = keys[i];
-      const uint64_t h = gbjd::fmix32((uint32_t)k) & mask;
-      probe_one(k, pay ? pay[i] : 0, i, h, __ldg(&slots[h]));
-    }
-  } else {
-    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += stride) {
-      const int32_t k = keys[i];
-      const uint64_t h = gbjd::fmix32((uint32_t)k) & mask;
-      probe_one(k, pay ? pay[i] : 0, i, h, __ldg(&slots[h]));
-    }
+    done = n8 * 8;
+  }
+  // rows the vector loop did not cover (all of them without kVec)
+  for (uint64_t i = done + blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += stride) {
+    const int32_t k = keys[i];
+    const uint64_t h = gbjd::fmix32((uint32_t)k) & mask;
+    probe_one(k, pay ? pay[i] : 0, i, h, slot_at<kWide>(slots, h));
   }
   if (kAgg != kAggGeneric) {
     acc.v[0] = a_cnt;
@@ -146,10 +170,11 @@ __global__ void __launch_bounds__(kThreads)
 
 // Probe emitting (build row, probe row) pairs through warp-aggregated
 // reservations of the output cursor.
+template <bool kWide>
 __global__ void __launch_bounds__(kThreads)
     k_join_probe_pairs(const int32_t *__restrict__ keys,
                        const int32_t *__restrict__ prows, uint64_t n,
-                       const uint64_t *__restrict__ slots, uint64_t mask,
+                       const void *__restrict__ slots, uint64_t mask,
                        const uint32_t *__restrict__ meta,
                        int32_t *__restrict__ out_b, int32_t *__restrict__ out_p,
                        uint64_t cap, unsigned long long *count,
@@ -161,15 +186,15 @@ __global__ void __launch_bounds__(kThreads)
     const int32_t pr = prows ? prows[i] : (int32_t)i;
     uint64_t h = gbjd::fmix32((uint32_t)k) & mask;
     for (uint64_t step = 0; step <= mask; ++step) {
-      const uint64_t e = __ldg(&slots[h]);
-      if (e == 0) break;
-      if (slot_key(e) == k) {
+      const SlotView e = slot_at<kWide>(slots, h);
+      if (e.row1 == 0) break;
+      if (e.key == k) {
         cg::coalesced_group g = cg::coalesced_threads();
         unsigned long long base = 0;
         if (g.thread_rank() == 0) base = atomicAdd(count, (unsigned long long)g.size());
         base = g.shfl(base, 0) + g.thread_rank();
         if (base < cap) {
-          out_b[base] = (int32_t)slot_row(e);
+          out_b[base] = (int32_t)(e.row1 - 1);
           out_p[base] = pr;
         } else {
           gbjd::latch(status, GBJ_DEV_CAPACITY);
@@ -227,21 +252,23 @@ int grid_for(gbj_ctx *ctx, uint64_t work, int threads, int per_sm = 4) {
   return grid_for_sms(ctx->sm_count, work, threads, per_sm);
 }
 
-// Picks the probe kernel: int4 loads when both probe columns are 16-byte
-// aligned, and a specialised accumulator for COUNT + SUM(product / xor).
-void launch_probe(int sm_count, const int32_t *keys, const int32_t *pay, uint64_t n,
-                  const uint64_t *slots, uint64_t mask, const int32_t *bpay,
-                  const uint32_t *meta, const gbj::AggSpec &spec, int64_t *out,
-                  cudaStream_t s) {
+// Picks the probe kernel: 16-byte loads when both probe columns are
+// 16-byte aligned, a specialised accumulator for COUNT + SUM(product / xor),
+// and the slot layout of the table.
+template <bool kWide>
+void launch_probe_t(int sm_count, const int32_t *keys, const int32_t *pay, uint64_t n, const void *slots,
+                    uint64_t mask, const int32_t *bpay, const uint32_t *meta, const gbj::AggSpec &spec,
+                    int64_t *out, cudaStream_t s) {
   const bool vec = ((uintptr_t)keys % 16 == 0) && (!pay || (uintptr_t)pay % 16 == 0);
   const bool two = spec.n == 2 && spec.op[0] == GBJ_AGG_COUNT && spec.op[1] == GBJ_AGG_SUM;
   const int agg = two && spec.operand[1] == GBJ_VAL_ROWID_XOR ? kAggCountXor
                   : two && spec.operand[1] == GBJ_VAL_PRODUCT ? kAggCountProduct
                                                               : kAggGeneric;
-  const int gv = grid_for_sms(sm_count, (n + 3) / 4, kThreads);
+  const int gv = grid_for_sms(sm_count, (n + 7) / 8, kThreads);
   const int gs = grid_for_sms(sm_count, n, kThreads);
-#define GBJ_PROBE(V, A) \
-  k_join_probe_agg<V, A><<<V ? gv : gs, kThreads, 0, s>>>(keys, pay, n, slots, mask, bpay, meta, spec, out)
+#define GBJ_PROBE(V, A)                                                                                  \
+  k_join_probe_agg<V, A, kWide><<<V ? gv : gs, kThreads, 0, s>>>(keys, pay, n, slots, mask, bpay, meta, \
+                                                                 spec, out)
   if (vec) {
     if (agg == kAggCountXor) GBJ_PROBE(true, kAggCountXor);
     else if (agg == kAggCountProduct) GBJ_PROBE(true, kAggCountProduct);
@@ -252,6 +279,13 @@ void launch_probe(int sm_count, const int32_t *keys, const int32_t *pay, uint64_
     else GBJ_PROBE(false, kAggGeneric);
   }
 #undef GBJ_PROBE
+}
+
+void launch_probe(int sm_count, bool wide, const int32_t *keys, const int32_t *pay, uint64_t n, const void *slots,
+                  uint64_t mask, const int32_t *bpay, const uint32_t *meta, const gbj::AggSpec &spec,
+                  int64_t *out, cudaStream_t s) {
+  if (wide) launch_probe_t<true>(sm_count, keys, pay, n, slots, mask, bpay, meta, spec, out, s);
+  else launch_probe_t<false>(sm_count, keys, pay, n, slots, mask, bpay, meta, spec, out, s);
 }
 
 // ------------------------------------------------ allocation-free variant
@@ -313,6 +347,12 @@ int noalloc_fail(int code, const char *msg) {
   return code;
 }
 
+// The metadata word after a table's slots.
+const uint32_t *table_meta(const gbj_table *t) {
+  return reinterpret_cast<const uint32_t *>(static_cast<const char *>(t->slots) +
+                                            (t->mask + 1) * (t->wide ? 16 : 8));
+}
+
 }  // namespace
 
 namespace gbj {
@@ -344,26 +384,34 @@ int gbj_join_build(gbj_ctx *ctx, const int32_t *d_keys,
   if (slots < 64) slots = 64;
   gbj_table *t = new gbj_table();
   void *mem = nullptr;
-  int rc = pool_alloc(ctx, slots * sizeof(uint64_t) + 256, s, &mem);
+  // a build side with a payload gets 16-byte slots that carry it
+  const bool wide = d_payload != nullptr;
+  const uint64_t slot_bytes = wide ? 16 : 8;
+  int rc = pool_alloc(ctx, slots * slot_bytes + 256, s, &mem);
   if (rc) {
     delete t;
     return rc;
   }
-  t->slots = (uint64_t *)mem;
+  t->slots = mem;
+  t->wide = wide;
   t->mask = slots - 1;
   t->keys = d_keys;
   t->payload = d_payload;
   t->n = n;
-  uint32_t *meta = (uint32_t *)(t->slots + slots);
-  cudaError_t e = cudaMemsetAsync(mem, 0, slots * sizeof(uint64_t) + 256, s);
+  uint32_t *meta = (uint32_t *)((char *)mem + slots * slot_bytes);
+  cudaError_t e = cudaMemsetAsync(mem, 0, slots * slot_bytes + 256, s);
   if (e != cudaSuccess) {
     pool_release(ctx, mem, s);
     delete t;
     return cuda_error(ctx, e, "cudaMemsetAsync(table)");
   }
   if (n) {
-    k_join_build<<<grid_for(ctx, n, kThreads), kThreads, 0, s>>>(d_keys, n, t->slots, t->mask,
-                                                                 meta, ctx->d_status);
+    if (wide)
+      k_join_build<true><<<grid_for(ctx, n, kThreads), kThreads, 0, s>>>(d_keys, d_payload, n, t->slots,
+                                                                       t->mask, meta, ctx->d_status);
+    else
+      k_join_build<false><<<grid_for(ctx, n, kThreads), kThreads, 0, s>>>(d_keys, nullptr, n, t->slots,
+                                                                        t->mask, meta, ctx->d_status);
     rc = after_launch(ctx, "k_join_build", s);
     if (rc) {
       pool_release(ctx, mem, s);
@@ -402,8 +450,8 @@ int gbj_join_probe_agg(gbj_ctx *ctx, const gbj_table *t, const int32_t *d_keys,
   prof_mark(ctx, s);
   GBJ_TRY(init_agg_out(ctx, spec, d_out, s));
   if (n == 0) return GBJ_OK;
-  const uint32_t *meta = (const uint32_t *)(t->slots + t->mask + 1);
-  launch_probe(ctx->sm_count, d_keys, d_payload, n, t->slots, t->mask, t->payload, meta, spec,
+  const uint32_t *meta = table_meta(t);
+  launch_probe(ctx->sm_count, t->wide, d_keys, d_payload, n, t->slots, t->mask, t->payload, meta, spec,
                d_out, s);
   return after_launch(ctx, "k_join_probe_agg", s);
 }
@@ -419,10 +467,15 @@ int gbj_join_probe_pairs(gbj_ctx *ctx, const gbj_table *t, const int32_t *d_keys
   prof_mark(ctx, s);
   GBJ_CHECK_CUDA(ctx, cudaMemsetAsync(d_count, 0, sizeof(uint64_t), s));
   if (n == 0) return GBJ_OK;
-  const uint32_t *meta = (const uint32_t *)(t->slots + t->mask + 1);
-  k_join_probe_pairs<<<grid_for(ctx, n, kThreads), kThreads, 0, s>>>(
-      d_keys, d_probe_rows, n, t->slots, t->mask, meta, d_build_rows, d_out_probe_rows,
-      capacity, (unsigned long long *)d_count, ctx->d_status);
+  const uint32_t *meta = table_meta(t);
+  if (t->wide)
+    k_join_probe_pairs<true><<<grid_for(ctx, n, kThreads), kThreads, 0, s>>>(
+        d_keys, d_probe_rows, n, t->slots, t->mask, meta, d_build_rows, d_out_probe_rows, capacity,
+        (unsigned long long *)d_count, ctx->d_status);
+  else
+    k_join_probe_pairs<false><<<grid_for(ctx, n, kThreads), kThreads, 0, s>>>(
+        d_keys, d_probe_rows, n, t->slots, t->mask, meta, d_build_rows, d_out_probe_rows, capacity,
+        (unsigned long long *)d_count, ctx->d_status);
   return after_launch(ctx, "k_join_probe_pairs", s);
 }
 
@@ -534,10 +587,10 @@ int gbj_join_agg_noalloc(const int32_t *d_build_keys, const int32_t *d_build_pay
   }
   k_noalloc_init_out<<<1, 32, 0, s>>>(spec, d_out);
   if (n_build)
-    k_join_build<<<grid_for_sms(d.sm_count, n_build, kThreads), kThreads, 0, s>>>(
-        d_build_keys, n_build, table, slots - 1, meta, nullptr);
+    k_join_build<false><<<grid_for_sms(d.sm_count, n_build, kThreads), kThreads, 0, s>>>(
+        d_build_keys, nullptr, n_build, table, slots - 1, meta, nullptr);
   if (n_probe)
-    launch_probe(d.sm_count, d_probe_keys, d_probe_payload, n_probe, table, slots - 1,
+    launch_probe(d.sm_count, false, d_probe_keys, d_probe_payload, n_probe, table, slots - 1,
                  d_build_payload, meta, spec, d_out, s);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return noalloc_fail(GBJ_ERR_CUDA, cudaGetErrorString(e));

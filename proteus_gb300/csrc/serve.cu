@@ -209,8 +209,8 @@ __global__ void __launch_bounds__(kThreads) k_serve_build(const SBatch *__restri
     for (uint64_t i = lo + threadIdx.x; i < hi; i += blockDim.x) {
       const int32_t k = __ldcs(q.bk + i);
       const int64_t gs = claim(__ldcs(q.bg + i));
-      if (gs < 0) {
-        gbjd::latch(&slot->status[qi], GBJ_DEV_CAPACITY);
+      if (gs < 0) {  // more distinct groups than expected_groups allowed for
+        gbjd::latch(&slot->status[qi], GBJ_DEV_GROUPS);
         continue;
       }
       if (k == INT32_MIN) {
@@ -367,6 +367,8 @@ struct QueryRec {
   double t_sub = -1, t_launch = -1, t_done = -1;
   int32_t status = GBJ_OK;
   bool done = false;
+  bool launched = false;
+  int retries = 0;
   void *mem = nullptr;
 };
 
@@ -412,8 +414,9 @@ struct gbj_server {
   std::vector<QueryRec> recs;  // index = ticket - 1
   Slot slots[kMaxSlots];
   int nslots = 0;
-  uint64_t held = 0, peak = 0, completed = 0, batches = 0;
+  uint64_t held = 0, peak = 0, completed = 0, batches = 0, retried = 0;
   bool stop = false;
+  bool paused = false;  // gbj_server_pause: no new batches are launched
   std::thread th;
   std::chrono::steady_clock::time_point t0;
   int grid[kPhases] = {0, 0, 0, 0};
@@ -502,17 +505,32 @@ void finish_query(gbj_server *sv, QueryRec &r, int32_t status, double t) {
   sv->cv_done.notify_all();
 }
 
+uint64_t enqueue_rec(gbj_server *sv, uint64_t ticket);
+
 // Completes the slot's batch (its event has fired).  Caller holds sv->mu.
+// A query whose group table ran out of slots (expected_groups below its
+// distinct build groups) is queued once more, sized for every build row
+// being its own group, which cannot overflow; other failures complete it.
 void complete_slot(gbj_server *sv, Slot &sl) {
   const double t = sv->now();
   for (size_t i = 0; i < sl.tickets.size(); ++i) {
     QueryRec &r = sv->recs[sl.tickets[i] - 1];
     const uint32_t bits = sl.h_status[i];
-    const int32_t st = bits & GBJ_DEV_CAPACITY ? GBJ_ERR_CAPACITY
-                       : bits & GBJ_DEV_TIMEOUT ? GBJ_ERR_TIMEOUT
-                       : bits ? GBJ_ERR_INVALID : GBJ_OK;
     if (r.mem) pool_release(sv->ctx, r.mem, sl.stream);
     r.mem = nullptr;
+    if (bits == GBJ_DEV_GROUPS && r.retries == 0 && !r.q.table_id &&
+        r.q.expected_groups < std::max<uint64_t>(r.q.n_build, 1) && !sv->stop) {
+      r.retries = 1;
+      r.launched = false;
+      r.q.expected_groups = std::max<uint64_t>(r.q.n_build, 1);
+      r.bytes = query_bytes(sv, r.q);
+      sv->retried++;
+      enqueue_rec(sv, sl.tickets[i]);
+      continue;
+    }
+    const int32_t st = bits & (GBJ_DEV_CAPACITY | GBJ_DEV_GROUPS) ? GBJ_ERR_CAPACITY
+                       : bits & GBJ_DEV_TIMEOUT ? GBJ_ERR_TIMEOUT
+                       : bits ? GBJ_ERR_INVALID : GBJ_OK;
     finish_query(sv, r, st, t);
   }
   sv->held -= sl.bytes;
@@ -540,6 +558,7 @@ bool launch_batch(gbj_server *sv, Slot &sl) {
     void *mem = nullptr;
     if (pool_alloc(ctx, r.bytes, sl.stream, &mem) != GBJ_OK) break;  // pool busy: retry later
     r.mem = mem;
+    r.launched = true;
     take.push_back(t);
     bytes += r.bytes;
     queue.pop_front();
@@ -670,13 +689,13 @@ void dispatcher(gbj_server *sv) {
       }
     }
     if (progressed) sv->cv_done.notify_all();
-    for (int i = 0; i < sv->nslots; ++i) {
+    for (int i = 0; i < sv->nslots && !sv->paused; ++i) {
       Slot &sl = sv->slots[i];
       if (!sl.busy && !sv->queue[sl.large ? 1 : 0].empty() && launch_batch(sv, sl)) progressed = true;
     }
     for (int i = 0; i < sv->nslots; ++i) busy = busy || sv->slots[i].busy;
     const bool queued = !sv->queue[0].empty() || !sv->queue[1].empty();
-    if (!busy && queued && !progressed) {
+    if (!busy && queued && !progressed && !sv->paused) {
       // nothing in flight and a head query still does not fit the pool
       std::deque<uint64_t> &qq = sv->queue[sv->queue[0].empty() ? 1 : 0];
       QueryRec &r = sv->recs[qq.front() - 1];
@@ -692,7 +711,9 @@ void dispatcher(gbj_server *sv) {
       lk.lock();
       continue;
     }
-    sv->cv_work.wait(lk, [&] { return sv->stop || !sv->queue[0].empty() || !sv->queue[1].empty(); });
+    sv->cv_work.wait(lk, [&] {
+      return sv->stop || (!sv->paused && (!sv->queue[0].empty() || !sv->queue[1].empty()));
+    });
   }
 }
 
@@ -782,6 +803,15 @@ int check_query(gbj_ctx *ctx, const gbj_serve_query *q) {
   return GBJ_OK;
 }
 
+// Puts a recorded query on its size class's queue.  Caller holds sv->mu.
+uint64_t enqueue_rec(gbj_server *sv, uint64_t ticket) {
+  const gbj_serve_query &q = sv->recs[ticket - 1].q;
+  const uint64_t build_rows = q.table_id ? 0 : q.n_build;
+  const bool large = sv->prm.large_slots > 0 && build_rows + q.n_probe > sv->prm.small_rows;
+  sv->queue[large ? 1 : 0].push_back(ticket);
+  return ticket;
+}
+
 // Queues one checked query.  Caller holds sv->mu.
 uint64_t enqueue_query(gbj_server *sv, const gbj_serve_query *q, double t) {
   QueryRec r;
@@ -789,11 +819,7 @@ uint64_t enqueue_query(gbj_server *sv, const gbj_serve_query *q, double t) {
   r.bytes = query_bytes(sv, *q);
   r.t_sub = t;
   sv->recs.push_back(r);
-  const uint64_t ticket = sv->recs.size();
-  const uint64_t build_rows = q->table_id ? 0 : q->n_build;
-  const bool large = sv->prm.large_slots > 0 && build_rows + q->n_probe > sv->prm.small_rows;
-  sv->queue[large ? 1 : 0].push_back(ticket);
-  return ticket;
+  return enqueue_rec(sv, sv->recs.size());
 }
 }  // namespace
 
@@ -830,6 +856,42 @@ extern "C" int gbj_server_wait(gbj_server *sv, uint64_t ticket, double timeout_s
   return GBJ_OK;
 }
 
+extern "C" int gbj_server_cancel(gbj_server *sv, uint64_t ticket, int32_t *cancelled) {
+  if (!sv) return GBJ_ERR_INVALID;
+  std::lock_guard<std::mutex> lk(sv->mu);
+  if (ticket == 0 || ticket > sv->recs.size()) return set_error(sv->ctx, GBJ_ERR_INVALID, "server: unknown ticket");
+  QueryRec &r = sv->recs[ticket - 1];
+  bool hit = false;
+  if (!r.done && !r.launched) {
+    for (auto &qq : sv->queue) {
+      auto it = std::find(qq.begin(), qq.end(), ticket);
+      if (it != qq.end()) {
+        qq.erase(it);
+        hit = true;
+        break;
+      }
+    }
+    if (hit) finish_query(sv, r, GBJ_ERR_CANCELLED, sv->now());
+  }
+  if (cancelled) *cancelled = hit ? 1 : 0;
+  return GBJ_OK;
+}
+
+extern "C" int gbj_server_pause(gbj_server *sv, int32_t paused) {
+  if (!sv) return GBJ_ERR_INVALID;
+  std::lock_guard<std::mutex> lk(sv->mu);
+  sv->paused = paused != 0;
+  sv->cv_work.notify_one();
+  return GBJ_OK;
+}
+
+extern "C" int gbj_server_retries(gbj_server *sv, uint64_t *retried) {
+  if (!sv || !retried) return GBJ_ERR_INVALID;
+  std::lock_guard<std::mutex> lk(sv->mu);
+  *retried = sv->retried;
+  return GBJ_OK;
+}
+
 extern "C" int gbj_server_times(gbj_server *sv, uint64_t ticket, double *submitted, double *launched,
                                 double *completed) {
   if (!sv) return GBJ_ERR_INVALID;
@@ -860,6 +922,7 @@ extern "C" int gbj_server_stats(gbj_server *sv, uint64_t *completed, uint64_t *b
 
 extern "C" int gbj_server_destroy(gbj_server *sv) {
   if (!sv) return GBJ_ERR_INVALID;
+  gbj_server_pause(sv, 0);  // queued queries run before the loop stops
   gbj_server_drain(sv);
   {
     std::lock_guard<std::mutex> lk(sv->mu);
@@ -876,9 +939,10 @@ extern "C" int gbj_server_destroy(gbj_server *sv) {
   return GBJ_OK;
 }
 
-extern "C" int gbj_server_register_table(gbj_server *sv, const int32_t *d_build_keys,
-                                         const int32_t *d_build_group, uint64_t n_build,
-                                         uint64_t expected_groups, uint64_t *table_id) {
+// One registration attempt; *dev_status gets the build's device status bits.
+static int register_table_once(gbj_server *sv, const int32_t *d_build_keys, const int32_t *d_build_group,
+                               uint64_t n_build, uint64_t expected_groups, uint64_t *table_id,
+                               uint32_t *dev_status) {
   if (!sv || !table_id) return GBJ_ERR_INVALID;
   gbj_ctx *ctx = sv->ctx;
   if (n_build && (!d_build_keys || !d_build_group))
@@ -949,6 +1013,7 @@ extern "C" int gbj_server_register_table(gbj_server *sv, const int32_t *d_build_
   delete h;
   if (d_desc) pool_release(ctx, d_desc, s);
   if (d_slot) pool_release(ctx, d_slot, s);
+  *dev_status = status;
   if (rc == GBJ_OK && status) rc = set_error(ctx, GBJ_ERR_CAPACITY, "server: table build overflowed");
   if (rc != GBJ_OK) {
     pool_release(ctx, t.mem, s);
@@ -959,6 +1024,23 @@ extern "C" int gbj_server_register_table(gbj_server *sv, const int32_t *d_build_
   sv->held += bytes;
   sv->peak = std::max(sv->peak, sv->held);
   return GBJ_OK;
+}
+
+// A build whose groups outnumber expected_groups is built once more with a
+// group table for every build row being its own group.
+extern "C" int gbj_server_register_table(gbj_server *sv, const int32_t *d_build_keys,
+                                         const int32_t *d_build_group, uint64_t n_build,
+                                         uint64_t expected_groups, uint64_t *table_id) {
+  uint32_t bits = 0;
+  const int rc = register_table_once(sv, d_build_keys, d_build_group, n_build, expected_groups, table_id, &bits);
+  if (rc == GBJ_ERR_CAPACITY && bits == GBJ_DEV_GROUPS && expected_groups < n_build) {
+    {
+      std::lock_guard<std::mutex> lk(sv->mu);
+      sv->retried++;
+    }
+    return register_table_once(sv, d_build_keys, d_build_group, n_build, n_build, table_id, &bits);
+  }
+  return rc;
 }
 
 extern "C" int gbj_server_unregister_table(gbj_server *sv, uint64_t table_id) {

@@ -75,6 +75,10 @@ class Context:
     def sync(self, stream=None):
         self.check(self.lib.gbj_sync(self.handle, stream if stream is not None else _cur_stream()))
 
+    def set_pool_limit(self, nbytes: int):
+        """Caps the bytes the resident pool hands out (0 = no cap)."""
+        self.check(self.lib.gbj_ctx_set_pool_limit(self.handle, nbytes))
+
     def launches(self) -> int:
         return int(self.lib.gbj_kernel_launches(self.handle))
 

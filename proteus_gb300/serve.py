@@ -152,6 +152,20 @@ class Server:
         self._keep.pop(ticket, None)
         return st.value
 
+    def cancel(self, ticket: int) -> bool:
+        """Cancels a still-queued query; True if it was cancelled."""
+        c = C.c_int32()
+        self.ctx.check(self.ctx.lib.gbj_server_cancel(self.handle, ticket, C.byref(c)))
+        return bool(c.value)
+
+    def pause(self, paused: bool = True):
+        self.ctx.check(self.ctx.lib.gbj_server_pause(self.handle, int(paused)))
+
+    def retries(self) -> int:
+        r = C.c_uint64()
+        self.ctx.check(self.ctx.lib.gbj_server_retries(self.handle, C.byref(r)))
+        return r.value
+
     def times(self, ticket: int):
         a, b, c = C.c_double(), C.c_double(), C.c_double()
         self.ctx.check(self.ctx.lib.gbj_server_times(self.handle, ticket, C.byref(a), C.byref(b), C.byref(c)))
