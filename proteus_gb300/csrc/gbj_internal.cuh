@@ -170,6 +170,20 @@ __host__ __device__ __forceinline__ uint32_t fmix32(uint32_t h) {
   return h;
 }
 
+// Inverse of fmix32 (each step of the finaliser is invertible modulo 2^32:
+// x ^= x >> 16 is its own inverse, x ^= x >> 13 is undone by
+// x ^= (x >> 13) ^ (x >> 26), and the odd multipliers have the modular
+// inverses 0xa5cb9243 = 0x85ebca6b^-1 and 0x7ed1b41d = 0xc2b2ae35^-1).
+// Partitioned join tuples carry fmix32(key); this recovers the key.
+__host__ __device__ __forceinline__ uint32_t fmix32_inv(uint32_t h) {
+  h ^= h >> 16;
+  h *= 0x7ed1b41du;
+  h ^= (h >> 13) ^ (h >> 26);
+  h *= 0xa5cb9243u;
+  h ^= h >> 16;
+  return h;
+}
+
 __device__ __forceinline__ void latch(uint32_t *status, uint32_t bit) {
   atomicOr(status, bit);
 }

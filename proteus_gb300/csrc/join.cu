@@ -85,10 +85,12 @@ __global__ void __launch_bounds__(kThreads)
 
 enum : int { kAggGeneric = 0, kAggCountXor = 1, kAggCountProduct = 2 };
 
-// Probe with fused aggregate.  Eight probe keys per thread: their first slot
-// loads are issued together so each thread keeps eight L2 requests in
-// flight; chains past the first slot are walked afterwards.  kAgg selects
-// a specialised accumulator for the two aggregate lists the workloads use.
+// Probe with fused aggregate.  Eight probe keys per thread walk their slot
+// chains in lockstep: every round checks the slot each still-open probe
+// holds and issues the next slot loads of all of them together, so a warp
+// waits for the longest chain once per round instead of once per probe and
+// keeps up to eight L2 requests per thread in flight.  kAgg selects a
+// specialised accumulator for the two aggregate lists the workloads use.
 template <bool kVec, int kAgg, bool kWide>
 __global__ void __launch_bounds__(kThreads)
     k_join_probe_agg(const int32_t *__restrict__ keys,
@@ -143,15 +145,36 @@ __global__ void __launch_bounds__(kThreads)
       }
       const int32_t kk[8] = {ka.x, ka.y, ka.z, ka.w, kb.x, kb.y, kb.z, kb.w};
       const int32_t pp[8] = {pa.x, pa.y, pa.z, pa.w, pb.x, pb.y, pb.z, pb.w};
-      uint64_t h[8];
+      // slot indices fit 32 bits: tables hold at most 2^32 slots
+      const uint32_t m32 = (uint32_t)mask;
+      uint32_t h[8];
       SlotView e[8];
 #pragma unroll
       for (int j = 0; j < 8; ++j) {
-        h[j] = gbjd::fmix32((uint32_t)kk[j]) & mask;
+        h[j] = gbjd::fmix32((uint32_t)kk[j]) & m32;
         e[j] = slot_at<kWide>(slots, h[j]);
       }
+      uint32_t open = 0xffu;  // probes whose chain is not finished
+      for (uint64_t step = 0; open && step <= mask; ++step) {
 #pragma unroll
-      for (int j = 0; j < 8; ++j) probe_one(kk[j], pp[j], q * 8 + j, h[j], e[j]);
+        for (int j = 0; j < 8; ++j) {
+          if (open >> j & 1u) {
+            if (e[j].row1 == 0) {
+              open &= ~(1u << j);
+            } else if (e[j].key == kk[j]) {
+              match(kk[j], pp[j], q * 8 + j, e[j]);
+              if (unique) open &= ~(1u << j);
+            }
+          }
+        }
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+          if (open >> j & 1u) {
+            h[j] = (h[j] + 1) & m32;
+            e[j] = slot_at<kWide>(slots, h[j]);
+          }
+        }
+      }
     }
     done = n8 * 8;
   }

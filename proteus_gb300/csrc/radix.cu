@@ -55,6 +55,11 @@ constexpr int kTileWarps = kTileThreads / 32;
 constexpr int kMaxDigits = 256;      // <= 8 digit bits per pass
 constexpr int32_t kEmpty = INT32_MIN;
 
+// Digit functions: of the key itself (GBJ_DIGIT_KEY), of fmix32(key)
+// (GBJ_DIGIT_HASH), or of a tuple word that already holds fmix32(key)
+// (kDigitPre: the partitioned join's tuples).
+constexpr int kDigitPre = 2;
+
 template <int kDigit>
 __device__ __forceinline__ uint32_t digit_of(int32_t key, int shift, uint32_t mask) {
   const uint32_t v = kDigit == GBJ_DIGIT_HASH ? gbjd::fmix32((uint32_t)key) : (uint32_t)key;
@@ -118,11 +123,14 @@ struct TileSmem {
 // (kPairsIn = false), or, for a second pass, kTile-tuple pieces of each
 // parent bucket of the AoS input (tile_off = prefix of tiles per bucket).
 // digit = (f(key) >> dshift) & dmask; the output cursor of (bucket b,
-// digit d) is cursor[b * (dmask + 1) + d].
-template <int kDigit, bool kPairsIn, bool kAoSOut>
+// digit d) is cursor[b * (dmask + 1) + d].  kHashLoad: the SoA keys are
+// replaced by fmix32(key) as they are loaded (the tuples then carry the
+// hash and kDigit is kDigitPre).  Row positions are below 2^31, so tile
+// arithmetic is 32-bit.
+template <int kDigit, bool kPairsIn, bool kAoSOut, bool kHashLoad>
 __global__ void __launch_bounds__(kTileThreads, kTileCtas)
     k_tile_pass(const int32_t *__restrict__ keys, const int32_t *__restrict__ vals,
-                const int2 *__restrict__ pin, uint64_t n, int dshift, uint32_t dmask,
+                const int2 *__restrict__ pin, uint32_t n, int dshift, uint32_t dmask,
                 const uint64_t *__restrict__ bucket_off, const uint64_t *__restrict__ tile_off,
                 uint32_t nb, uint32_t *__restrict__ cursor, int2 *__restrict__ out_pairs,
                 int32_t *__restrict__ out_k, int32_t *__restrict__ out_v) {
@@ -130,9 +138,9 @@ __global__ void __launch_bounds__(kTileThreads, kTileCtas)
   TileSmem &S = *reinterpret_cast<TileSmem *>(smem_raw);
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const uint32_t ndig = dmask + 1;
-  const uint64_t ntiles = kPairsIn ? tile_off[nb] : (n + kTile - 1) / kTile;
+  const uint32_t ntiles = kPairsIn ? (uint32_t)tile_off[nb] : (n + kTile - 1) / kTile;
   // tile t -> its rows [lo, hi) and bucket b
-  auto tile_range = [&](uint64_t t, uint64_t &lo, uint64_t &hi, uint32_t &b) {
+  auto tile_range = [&](uint32_t t, uint32_t &lo, uint32_t &hi, uint32_t &b) {
     b = 0;
     if (kPairsIn) {
       uint32_t a = 0, z = nb;  // tile_off[a] <= t < tile_off[z]
@@ -141,29 +149,31 @@ __global__ void __launch_bounds__(kTileThreads, kTileCtas)
         if (tile_off[mid] <= t) a = mid; else z = mid;
       }
       b = a;
-      lo = bucket_off[b] + (t - tile_off[b]) * kTile;
-      hi = lo + kTile < bucket_off[b + 1] ? lo + kTile : bucket_off[b + 1];
+      const uint32_t bend = (uint32_t)bucket_off[b + 1];
+      lo = (uint32_t)bucket_off[b] + (t - (uint32_t)tile_off[b]) * kTile;
+      hi = lo + kTile < bend ? lo + kTile : bend;
     } else {
       lo = t * kTile;
       hi = lo + kTile < n ? lo + kTile : n;
     }
   };
   int2 tup[kTilePer];
-  auto load_tile = [&](uint64_t lo, uint64_t hi) {
+  auto load_tile = [&](uint32_t lo, uint32_t hi) {
 #pragma unroll
     for (int j = 0; j < kTilePer; ++j) {
-      const uint64_t i = lo + tid + j * kTileThreads;
+      const uint32_t i = lo + tid + j * kTileThreads;
       if (i < hi) {
         if (kPairsIn) {
           tup[j] = __ldcs(pin + i);
         } else {
-          tup[j].x = __ldcs(keys + i);
+          const int32_t k = __ldcs(keys + i);
+          tup[j].x = kHashLoad ? (int32_t)gbjd::fmix32((uint32_t)k) : k;
           tup[j].y = vals ? __ldcs(vals + i) : (int32_t)i;
         }
       }
     }
   };
-  uint64_t t = blockIdx.x, lo = 0, hi = 0;
+  uint32_t t = blockIdx.x, lo = 0, hi = 0;
   uint32_t b = 0;
   if (t < ntiles) {
     tile_range(t, lo, hi, b);
@@ -175,10 +185,11 @@ __global__ void __launch_bounds__(kTileThreads, kTileCtas)
   for (; t < ntiles; t += gridDim.x) {
     for (uint32_t d = lane; d < ndig; d += 32) S.whist[warp][d] = 0;
     __syncwarp();
+    const uint32_t cnt = hi - lo;
     uint32_t dg[kTilePer], rk[kTilePer];
 #pragma unroll
     for (int j = 0; j < kTilePer; ++j) {
-      if (lo + tid + j * kTileThreads < hi) {
+      if (tid + j * kTileThreads < cnt) {
         dg[j] = digit_of<kDigit>(tup[j].x, dshift, dmask);
         rk[j] = atomicAdd(&S.whist[warp][dg[j]], 1u);
       }
@@ -222,7 +233,7 @@ __global__ void __launch_bounds__(kTileThreads, kTileCtas)
     __syncthreads();
 #pragma unroll
     for (int j = 0; j < kTilePer; ++j) {
-      if (lo + tid + j * kTileThreads < hi) {
+      if (tid + j * kTileThreads < cnt) {
         const uint32_t pos = S.whist[warp][dg[j]] + rk[j];
         S.sorted[pos] = tup[j];
       }
@@ -230,8 +241,7 @@ __global__ void __launch_bounds__(kTileThreads, kTileCtas)
     // written after the scatter, so the cursor atomic's round trip overlaps it
     // (modulo 2^32: gdelta + i is the output position)
     if ((uint32_t)tid < ndig) S.gdelta[tid] = gpos - my_start;
-    const uint32_t cnt = (uint32_t)(hi - lo);
-    const uint64_t tn = t + gridDim.x;
+    const uint32_t tn = t + gridDim.x;
     if (tn < ntiles) {
       tile_range(tn, lo, hi, b);
       load_tile(lo, hi);
@@ -335,21 +345,27 @@ struct RowCols {
   const int32_t *bmin, *pmin, *bpay, *ppay;
 };
 
-// Table slot of key k: Fibonacci hashing onto [0, cap) (multiply, then the
-// high word of hash * cap).  The keys of one partition share the low fmix32
-// bits that chose it; the multiplicative hash is independent of those.
-__device__ __forceinline__ uint32_t table_slot(int32_t k, int bits, uint32_t cap) {
-  (void)bits;
-  return __umulhi((uint32_t)k * 0x9E3779B1u, cap);
-}
+// The join works on hashed tuples: the first word of every partitioned
+// tuple is h = fmix32(key), which is a bijection of the 32-bit keys, so
+// h equality is key equality and the key itself is fmix32_inv(h) when an
+// aggregate reads it.  The partition id is the low `bits` bits of h; the
+// on-chip table places h by its high bits (independent of the partition).
+//
+// Table: 4-slot buckets; bucket b = slots [4b, 4b + 4).  An insert tries
+// the four slots of its home bucket, then the next bucket; a probe reads a
+// whole bucket with one 16-byte shared load and stops at a bucket with an
+// empty slot (slots only fill during the build, so a key was never placed
+// past a bucket that still has room).
+__device__ __forceinline__ uint32_t home_bucket(uint32_t h, uint32_t nb) { return __umulhi(h, nb); }
 
 template <int kAgg>
 __device__ __forceinline__ void join_match(const gbj::AggSpec &spec, const RowCols &rc, gbjd::Acc &acc,
-                                           int64_t &a_cnt, int64_t &a_sum, int32_t k, int32_t bv,
+                                           int64_t &a_cnt, int64_t &a_sum, uint32_t h, int32_t bv,
                                            int32_t pv) {
   if (kAgg == kAggCountXor) {
+    // row ids are non-negative: their xor is a zero-extended 32-bit value
     a_cnt += 1;
-    a_sum += (int64_t)bv ^ (int64_t)pv;
+    a_sum += (uint32_t)(bv ^ pv);
   } else if (kAgg == kAggCountProduct) {
     a_cnt += 1;
     a_sum += (int64_t)bv * (int64_t)pv;
@@ -359,21 +375,31 @@ __device__ __forceinline__ void join_match(const gbj::AggSpec &spec, const RowCo
     if (rc.bmin && __ldg(rc.bmin + bv) != __ldg(rc.pmin + pv)) return;
     const int64_t b = rc.bpay ? __ldg(rc.bpay + bv) : 0;
     const int64_t p = rc.ppay ? __ldg(rc.ppay + pv) : 0;
-    acc.update(spec, k, b, p, bv, pv);
+    acc.update(spec, (int32_t)gbjd::fmix32_inv(h), b, p, bv, pv);
   } else {
-    acc.update(spec, k, bv, pv, bv, pv);
+    acc.update(spec, (int32_t)gbjd::fmix32_inv(h), bv, pv, bv, pv);
   }
 }
 
+// One work item's extent, computed by thread 0 and shared with the block.
+struct JoinItem {
+  unsigned long long rb, sb;  // first build / probe tuple (global index)
+  uint32_t m, ns;             // build chunk size, probe chunk size
+  uint32_t part;
+  int valid;
+};
+
 // Persistent partition join.  Dynamic shared memory holds, for the current
-// build chunk of m tuples and cap = 2m rounded up to 64 slots, either
-//   keys[cap] + values[cap]            (every partition but one), or
-//   pairs[kRMax] + index[cap] (16-bit) (the partition INT32_MIN maps to).
+// build chunk of m tuples (nb = ceil(2m / 4) buckets rounded up to 16):
+//   keys[4 nb] + values[4 nb]            (every partition but one), or
+//   pairs[kRMax] + index[4 nb] (16-bit) (the partition whose tuples may hash
+//                                         to the empty marker).
+// followed by the per-warp probe queues.
 template <int kRMax, int kThreads, int kAgg>
-__global__ void __launch_bounds__(kThreads, kJoinCtas)
+__global__ void __launch_bounds__(kThreads, 1)
     k_radix_join(const int2 *__restrict__ R, const uint64_t *__restrict__ ro,
                  const int2 *__restrict__ S, const uint64_t *__restrict__ so,
-                 const uint64_t *__restrict__ item_off, uint32_t P, int bits, uint64_t w,
+                 const uint64_t *__restrict__ item_off, uint32_t P, uint32_t w,
                  uint32_t sentinel_part, gbj::AggSpec spec, RowCols rc, int64_t *out,
                  unsigned long long *item_ctr) {
   static_assert(2 * kRMax + 64 <= 65535, "16-bit index entries");
@@ -383,83 +409,100 @@ __global__ void __launch_bounds__(kThreads, kJoinCtas)
   int32_t *tval = tkey + kCapMax;
   int2 *rp = reinterpret_cast<int2 *>(smem);
   unsigned short *tab = reinterpret_cast<unsigned short *>(rp + kRMax);
-  // unresolved probes of one round, 128 per warp: {key, probe value, next group, -}
+  // unresolved probes of one round, 128 per warp: {h, probe value, next bucket, -}
   int4 *queue = reinterpret_cast<int4 *>(tval + kCapMax);
   __shared__ int64_t red[32 * GBJ_MAX_AGGS];
-  __shared__ unsigned long long s_item;
-  __shared__ uint32_t s_part;
+  __shared__ JoinItem s_it;
   __shared__ int s_dup;
   gbjd::Acc acc;
   acc.init(spec);
   int64_t a_cnt = 0, a_sum = 0;
-  const uint64_t total = item_off[P];
-  if (threadIdx.x == 0) {
-    s_item = atomicAdd(item_ctr, 1ull);
-    s_part = s_item < total ? item_partition(item_off, P, total, s_item) : 0;
-  }
+  const unsigned long long total = item_off[P];
+  // thread 0: claims the next item and resolves its extent
+  auto fetch = [&]() {
+    const unsigned long long item = atomicAdd(item_ctr, 1ull);
+    JoinItem it{};
+    it.valid = item < total;
+    if (it.valid) {
+      const uint32_t p = item_partition(item_off, P, total, item);
+      const uint64_t r0 = ro[p], r1 = ro[p + 1], s0 = so[p], s1 = so[p + 1];
+      const uint64_t nrc = (r1 - r0 + kRMax - 1) / kRMax;
+      const uint64_t local = item - item_off[p];
+      it.rb = r0 + (local % nrc) * kRMax;
+      it.m = (uint32_t)((it.rb + kRMax < r1 ? it.rb + kRMax : r1) - it.rb);
+      it.sb = s0 + (local / nrc) * w;
+      it.ns = (uint32_t)((it.sb + w < s1 ? it.sb + w : s1) - it.sb);
+      it.part = p;
+    }
+    s_it = it;
+  };
+  if (threadIdx.x == 0) fetch();
   __syncthreads();
+  const int lane = threadIdx.x & 31;
+  const unsigned lt = (1u << lane) - 1u;
+  int4 *wq = queue + (threadIdx.x >> 5) * (4 * 32);
   for (;;) {
-    const uint64_t item = s_item;
-    const uint32_t p = s_part;
-    if (item >= total) break;
-    const uint64_t r0 = ro[p], r1 = ro[p + 1], s0 = so[p], s1 = so[p + 1];
-    const uint64_t nrc = (r1 - r0 + kRMax - 1) / kRMax;
-    const uint64_t local = item - item_off[p];
-    const uint64_t rb = r0 + (local % nrc) * kRMax;
-    const uint64_t re = rb + kRMax < r1 ? rb + kRMax : r1;
-    const uint64_t sb = s0 + (local / nrc) * w;
-    const uint64_t se = sb + w < s1 ? sb + w : s1;
-    const int m = (int)(re - rb);
-    const uint32_t cap = (uint32_t)((2 * m + 63) & ~63);
-    const bool fast = p != sentinel_part;
+    const JoinItem it = s_it;
+    if (!it.valid) break;
+    const int2 *Rp = R + it.rb;
+    const int2 *Sp = S + it.sb;
+    const uint32_t m = it.m, ns = it.ns;
+    const uint32_t nb = ((2 * m + 3) / 4 + 15) & ~15u;  // buckets
+    const uint32_t cap = 4 * nb;
+    const bool fast = it.part != sentinel_part;
     if (threadIdx.x == 0) s_dup = 0;
     if (fast) {
-      // ---- keys + values table ----
+      // ---- keys + values table of 4-slot buckets ----
       int4 *tk4 = reinterpret_cast<int4 *>(tkey);
-      for (uint32_t i = threadIdx.x; i < cap / 4; i += kThreads)
-        tk4[i] = make_int4(kEmpty, kEmpty, kEmpty, kEmpty);
+      for (uint32_t i = threadIdx.x; i < nb; i += kThreads) tk4[i] = make_int4(kEmpty, kEmpty, kEmpty, kEmpty);
       __syncthreads();
       bool dup = false;
       auto insert = [&](int2 t) {
-        uint32_t h = table_slot(t.x, bits, cap);
-        for (uint32_t step = 0; step < cap; ++step) {
-          const int32_t old = atomicCAS(&tkey[h], kEmpty, t.x);
-          if (old == kEmpty) {
-            tval[h] = t.y;
-            return;
+        const uint32_t h = (uint32_t)t.x;
+        uint32_t b = home_bucket(h, nb);
+        const uint32_t o = h >> 16;  // start slot in the bucket (spreads the CASes)
+        for (uint32_t step = 0; step < nb; ++step) {
+#pragma unroll
+          for (uint32_t j = 0; j < 4; ++j) {
+            const uint32_t sl = 4 * b + ((o + j) & 3);
+            const int32_t old = atomicCAS(&tkey[sl], kEmpty, t.x);
+            if (old == kEmpty) {
+              tval[sl] = t.y;
+              return;
+            }
+            dup |= (old == t.x);
           }
-          dup |= (old == t.x);
-          if (++h == cap) h = 0;
+          b = b + 1 == nb ? 0 : b + 1;
         }
       };
       // the whole chunk's loads in flight at once (8 per thread per round)
-      for (uint64_t i0 = rb + threadIdx.x; i0 < re; i0 += 8 * kThreads) {
+      for (uint32_t i0 = threadIdx.x; i0 < m; i0 += 8 * kThreads) {
         int2 t[8];
 #pragma unroll
         for (int u = 0; u < 8; ++u) {
-          const uint64_t i = i0 + (uint64_t)u * kThreads;
-          if (i < re) t[u] = __ldcs(R + i);
+          const uint32_t i = i0 + u * kThreads;
+          if (i < m) t[u] = __ldcs(Rp + i);
         }
 #pragma unroll
         for (int u = 0; u < 8; ++u)
-          if (i0 + (uint64_t)u * kThreads < re) insert(t[u]);
+          if (i0 + u * kThreads < m) insert(t[u]);
       }
       if (dup) s_dup = 1;
     } else {
-      // ---- pairs + 16-bit index table (INT32_MIN keys allowed) ----
+      // ---- pairs + 16-bit index table (any hash value allowed) ----
       uint32_t *tab32 = reinterpret_cast<uint32_t *>(tab);
       for (uint32_t i = threadIdx.x; i < cap / 2; i += kThreads) tab32[i] = 0;
-      for (int i = threadIdx.x; i < m; i += kThreads) rp[i] = R[rb + i];
+      for (uint32_t i = threadIdx.x; i < m; i += kThreads) rp[i] = Rp[i];
       __syncthreads();
       bool dup = false;
-      for (int i = threadIdx.x; i < m; i += kThreads) {
+      for (uint32_t i = threadIdx.x; i < m; i += kThreads) {
         const int32_t k = rp[i].x;
-        uint32_t h = table_slot(k, bits, cap);
+        uint32_t hh = __umulhi((uint32_t)k, cap);
         for (uint32_t step = 0; step < cap; ++step) {
-          const unsigned short old = atomicCAS(&tab[h], (unsigned short)0, (unsigned short)(i + 1));
+          const unsigned short old = atomicCAS(&tab[hh], (unsigned short)0, (unsigned short)(i + 1));
           if (old == 0) break;
           dup |= (rp[old - 1].x == k);
-          if (++h == cap) h = 0;
+          if (++hh == cap) hh = 0;
         }
       }
       if (dup) s_dup = 1;
@@ -467,100 +510,85 @@ __global__ void __launch_bounds__(kThreads, kJoinCtas)
     __syncthreads();
     const bool unique = s_dup == 0;
     // next item: fetched now, consumed after the closing barrier
-    if (threadIdx.x == 0) {
-      const unsigned long long nx = atomicAdd(item_ctr, 1ull);
-      s_item = nx;
-      s_part = nx < total ? item_partition(item_off, P, total, nx) : 0;
-    }
+    if (threadIdx.x == 0) fetch();
     if (fast) {
-      // One 4-slot group from the probe start: the candidates are the slots
-      // before the first empty one.  Returns true when the probe is done.
-      auto group = [&](int32_t k, int32_t v, uint32_t g0, uint32_t o) -> bool {
-        const int4 kk = *reinterpret_cast<const int4 *>(tkey + g0);
-        const uint32_t valid = (0xfu << o) & 0xfu;
-        const uint32_t em = valid & ((kk.x == kEmpty) | ((kk.y == kEmpty) << 1) |
-                                     ((kk.z == kEmpty) << 2) | ((kk.w == kEmpty) << 3));
-        const uint32_t before = em ? (em & (0u - em)) - 1u : 0xfu;
-        uint32_t hits = valid & before &
-                        ((kk.x == k) | ((kk.y == k) << 1) | ((kk.z == k) << 2) | ((kk.w == k) << 3));
+      const int4 *tk4 = reinterpret_cast<const int4 *>(tkey);
+      // One bucket: matches among its four slots; true when the probe is done
+      // (a match of a unique key, or a bucket with an empty slot).
+      auto bucket = [&](uint32_t h, int32_t v, uint32_t b) -> bool {
+        const int4 kk = tk4[b];
+        const int32_t k = (int32_t)h;
+        uint32_t hits = (kk.x == k) | ((kk.y == k) << 1) | ((kk.z == k) << 2) | ((kk.w == k) << 3);
+        const bool room = (kk.x == kEmpty) | (kk.y == kEmpty) | (kk.z == kEmpty) | (kk.w == kEmpty);
         while (hits) {
-          join_match<kAgg>(spec, rc, acc, a_cnt, a_sum, k, tval[g0 + __ffs(hits) - 1], v);
+          join_match<kAgg>(spec, rc, acc, a_cnt, a_sum, h, tval[4 * b + __ffs(hits) - 1], v);
           if (unique) return true;
           hits &= hits - 1;
         }
-        return em != 0;
+        return room;
       };
-      // Probe rounds of 4 tuples per thread: every probe checks its first
-      // group; the few that must continue go to the warp's own queue, which
-      // the warp's lanes then drain together, so no lane idles behind one
-      // long walk and no CTA-wide barrier is needed.  The next round's
-      // tuples are loaded while this round is probed.
-      const int lane = threadIdx.x & 31;
-      const unsigned lt = (1u << lane) - 1u;
-      int4 *wq = queue + (threadIdx.x >> 5) * (4 * 32);
+      // Probe rounds of 4 tuples per thread: every probe checks its home
+      // bucket; the few that must continue go to the warp's own queue, which
+      // the warp's lanes then drain together.  The next round's tuples are
+      // loaded while this round is probed.
       int2 nxt[4];
 #pragma unroll
       for (int u = 0; u < 4; ++u) {
-        const uint64_t j = sb + threadIdx.x + (uint64_t)u * kThreads;
-        nxt[u] = j < se ? __ldcs(S + j) : make_int2(0, 0);
+        const uint32_t j = threadIdx.x + u * kThreads;
+        nxt[u] = j < ns ? __ldcs(Sp + j) : make_int2(0, 0);
       }
-      for (uint64_t j0 = sb; j0 < se; j0 += 4 * kThreads) {
+      for (uint32_t j0 = 0; j0 < ns; j0 += 4 * kThreads) {
         int2 t[4];
 #pragma unroll
         for (int u = 0; u < 4; ++u) {
           t[u] = nxt[u];
-          const uint64_t j = j0 + 4 * kThreads + threadIdx.x + (uint64_t)u * kThreads;
-          nxt[u] = j < se ? __ldcs(S + j) : make_int2(0, 0);
+          const uint32_t j = j0 + 4 * kThreads + threadIdx.x + u * kThreads;
+          nxt[u] = j < ns ? __ldcs(Sp + j) : make_int2(0, 0);
         }
         uint32_t qn = 0;  // warp-uniform queue length
 #pragma unroll
         for (int u = 0; u < 4; ++u) {
           bool more = false;
-          uint32_t h = 0;
-          if (j0 + threadIdx.x + (uint64_t)u * kThreads < se) {
-            h = table_slot(t[u].x, bits, cap);
-            more = !group(t[u].x, t[u].y, h & ~3u, h & 3u);
+          uint32_t b = 0;
+          if (j0 + threadIdx.x + u * kThreads < ns) {
+            b = home_bucket((uint32_t)t[u].x, nb);
+            more = !bucket((uint32_t)t[u].x, t[u].y, b);
           }
           const unsigned bal = __ballot_sync(0xffffffffu, more);
-          if (more) {
-            uint32_t g1 = (h & ~3u) + 4;
-            if (g1 >= cap) g1 = 0;
-            wq[qn + __popc(bal & lt)] = make_int4(t[u].x, t[u].y, (int)g1, 0);
-          }
+          if (more) wq[qn + __popc(bal & lt)] = make_int4(t[u].x, t[u].y, (int)(b + 1 == nb ? 0 : b + 1), 0);
           qn += __popc(bal);
         }
         __syncwarp();
         for (uint32_t i = lane; i < qn; i += 32) {
           const int4 e = wq[i];
-          uint32_t g0 = (uint32_t)e.z;
-          for (uint32_t step = 4; step < cap; step += 4) {
-            if (group(e.x, e.y, g0, 0)) break;
-            g0 += 4;
-            if (g0 >= cap) g0 = 0;
+          uint32_t b = (uint32_t)e.z;
+          for (uint32_t step = 1; step < nb; ++step) {
+            if (bucket((uint32_t)e.x, e.y, b)) break;
+            b = b + 1 == nb ? 0 : b + 1;
           }
         }
         __syncwarp();
       }
     } else {
       // index table: plain linear probing, one slot per step
-      for (uint64_t j0 = sb + threadIdx.x; j0 < se; j0 += 4 * kThreads) {
+      for (uint32_t j0 = threadIdx.x; j0 < ns; j0 += 4 * kThreads) {
         int2 t[4];
 #pragma unroll
         for (int u = 0; u < 4; ++u) {
-          const uint64_t j = j0 + (uint64_t)u * kThreads;
-          t[u] = j < se ? __ldcs(S + j) : make_int2(0, 0);
+          const uint32_t j = j0 + u * kThreads;
+          t[u] = j < ns ? __ldcs(Sp + j) : make_int2(0, 0);
         }
 #pragma unroll
         for (int u = 0; u < 4; ++u) {
-          if (j0 + (uint64_t)u * kThreads >= se) continue;
+          if (j0 + u * kThreads >= ns) continue;
           const int32_t k = t[u].x;
-          uint32_t hh = table_slot(k, bits, cap);
+          uint32_t hh = __umulhi((uint32_t)k, cap);
           for (uint32_t step = 0; step < cap; ++step) {
             const unsigned short idx = tab[hh];
             if (idx == 0) break;
             const int2 bt = rp[idx - 1];
             if (bt.x == k) {
-              join_match<kAgg>(spec, rc, acc, a_cnt, a_sum, k, bt.y, t[u].y);
+              join_match<kAgg>(spec, rc, acc, a_cnt, a_sum, (uint32_t)k, bt.y, t[u].y);
               if (unique) break;
             }
             if (++hh == cap) hh = 0;
@@ -586,8 +614,8 @@ constexpr size_t join_smem() {
 
 template <int kRMax, int kThreads, int kAgg>
 int launch_join(gbj_ctx *ctx, const int2 *R, const uint64_t *ro, const int2 *S,
-                const uint64_t *so, const uint64_t *item_off, uint32_t P, int bits,
-                uint64_t w, uint32_t sentinel_part, const AggSpec &spec, const RowCols &rc,
+                const uint64_t *so, const uint64_t *item_off, uint32_t P,
+                uint32_t w, uint32_t sentinel_part, const AggSpec &spec, const RowCols &rc,
                 int64_t *out, unsigned long long *ctr, cudaStream_t s) {
   const size_t smem = join_smem<kRMax, kThreads>();
   auto kern = k_radix_join<kRMax, kThreads, kAgg>;
@@ -596,17 +624,17 @@ int launch_join(gbj_ctx *ctx, const int2 *R, const uint64_t *ro, const int2 *S,
   int per_sm = 0;
   GBJ_CHECK_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kThreads, smem));
   if (per_sm < 1) return set_error(ctx, GBJ_ERR_CUDA, "k_radix_join: no resident block fits");
-  kern<<<ctx->sm_count * per_sm, kThreads, smem, s>>>(R, ro, S, so, item_off, P, bits, w,
+  kern<<<ctx->sm_count * per_sm, kThreads, smem, s>>>(R, ro, S, so, item_off, P, w,
                                                      sentinel_part, spec, rc, out, ctr);
   return after_launch(ctx, "k_radix_join", s);
 }
 
-template <int kDigit, bool kPairsIn, bool kAoSOut>
+template <int kDigit, bool kPairsIn, bool kAoSOut, bool kHashLoad>
 int launch_tile_pass(gbj_ctx *ctx, const int32_t *keys, const int32_t *vals, const int2 *pin,
                      uint64_t n, int dshift, uint32_t dmask, const uint64_t *bucket_off,
                      const uint64_t *tile_off, uint32_t nb, uint32_t *cursor, int2 *op, int32_t *ok,
                      int32_t *ov, cudaStream_t s) {
-  auto kern = k_tile_pass<kDigit, kPairsIn, kAoSOut>;
+  auto kern = k_tile_pass<kDigit, kPairsIn, kAoSOut, kHashLoad>;
   const size_t smem = sizeof(TileSmem);
   GBJ_CHECK_CUDA(ctx, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   int per_sm = 0;
@@ -614,18 +642,25 @@ int launch_tile_pass(gbj_ctx *ctx, const int32_t *keys, const int32_t *vals, con
   if (per_sm < 1) per_sm = 1;
   const uint64_t tiles_hint = (n + kTile - 1) / kTile + nb;
   const uint64_t grid = std::max<uint64_t>(1, std::min<uint64_t>((uint64_t)ctx->sm_count * per_sm, tiles_hint));
-  kern<<<(unsigned)grid, kTileThreads, smem, s>>>(keys, vals, pin, n, dshift, dmask, bucket_off,
+  kern<<<(unsigned)grid, kTileThreads, smem, s>>>(keys, vals, pin, (uint32_t)n, dshift, dmask, bucket_off,
                                                   tile_off, nb, cursor, op, ok, ov);
   return after_launch(ctx, "k_tile_pass", s);
 }
 
-template <int kDigit>
+// kHashOut: the tuples leave with fmix32(key) in place of the key (the
+// partitioned join's layout; AoS output only), and the passes take their
+// digits from that word.
+template <int kDigit, bool kHashOut>
 int partition_impl(gbj_ctx *ctx, const int32_t *keys, const int32_t *vals, uint64_t n, int shift,
                    int bits, int2 *out_pairs, int32_t *out_keys, int32_t *out_vals,
                    uint64_t *offsets, cudaStream_t s, int passes) {
   if ((passes == 1 && bits > 8) || (passes == 2 && bits < 2) || passes < 0 || passes > 2)
     return set_error(ctx, GBJ_ERR_UNSUPPORTED,
                      "partition: one pass takes at most 8 radix bits, two passes at least 2");
+  if (n >= (1ull << 31)) return set_error(ctx, GBJ_ERR_INVALID, "partition: n >= 2^31");
+  if (kHashOut && !out_pairs) return set_error(ctx, GBJ_ERR_INVALID, "partition: hashed tuples are AoS only");
+  // digit function of the tile passes: of the loaded key, or of the hash word
+  constexpr int kPass = kHashOut ? kDigitPre : kDigit;
   const uint32_t P = 1u << bits, pmask = P - 1;
   Scratch scratch(ctx, s);
   uint32_t *hist, *cursor2;
@@ -650,11 +685,11 @@ int partition_impl(gbj_ctx *ctx, const int32_t *keys, const int32_t *vals, uint6
     k_cursors<<<(P + 255) / 256, 256, 0, s>>>(off, P, 0, nullptr, cursor2, nullptr);
     GBJ_TRY(after_launch(ctx, "k_cursors", s));
     if (out_pairs)
-      GBJ_TRY((launch_tile_pass<kDigit, false, true>(ctx, keys, vals, nullptr, n, shift, pmask, nullptr,
-                                                     nullptr, 1, cursor2, out_pairs, nullptr, nullptr, s)));
+      GBJ_TRY((launch_tile_pass<kPass, false, true, kHashOut>(ctx, keys, vals, nullptr, n, shift, pmask, nullptr,
+                                                              nullptr, 1, cursor2, out_pairs, nullptr, nullptr, s)));
     else
-      GBJ_TRY((launch_tile_pass<kDigit, false, false>(ctx, keys, vals, nullptr, n, shift, pmask, nullptr,
-                                                      nullptr, 1, cursor2, nullptr, out_keys, out_vals, s)));
+      GBJ_TRY((launch_tile_pass<kPass, false, false, false>(ctx, keys, vals, nullptr, n, shift, pmask, nullptr,
+                                                            nullptr, 1, cursor2, nullptr, out_keys, out_vals, s)));
   } else {
     const int bits2 = bits / 2, bits1 = bits - bits2;
     const uint32_t B1 = 1u << bits1;
@@ -667,18 +702,19 @@ int partition_impl(gbj_ctx *ctx, const int32_t *keys, const int32_t *vals, uint6
     GBJ_TRY(scratch.get(n + 1, &tmp));
     k_cursors<<<(P + 255) / 256, 256, 0, s>>>(off, P, bits2, cursor1, cursor2, bucket_off);
     GBJ_TRY(after_launch(ctx, "k_cursors", s));
-    GBJ_TRY((launch_tile_pass<kDigit, false, true>(ctx, keys, vals, nullptr, n, shift + bits2, B1 - 1,
-                                                   nullptr, nullptr, 1, cursor1, tmp, nullptr, nullptr, s)));
+    GBJ_TRY((launch_tile_pass<kPass, false, true, kHashOut>(ctx, keys, vals, nullptr, n, shift + bits2, B1 - 1,
+                                                            nullptr, nullptr, 1, cursor1, tmp, nullptr, nullptr,
+                                                            s)));
     k_bucket_tiles<<<(B1 + 255) / 256, 256, 0, s>>>(bucket_off, B1, tiles);
     GBJ_TRY(after_launch(ctx, "k_bucket_tiles", s));
     GBJ_TRY(scan_u64(ctx, tiles, tiles, B1, s));
     const uint32_t m2 = (1u << bits2) - 1;
     if (out_pairs)
-      GBJ_TRY((launch_tile_pass<kDigit, true, true>(ctx, nullptr, nullptr, tmp, n, shift, m2, bucket_off,
-                                                    tiles, B1, cursor2, out_pairs, nullptr, nullptr, s)));
+      GBJ_TRY((launch_tile_pass<kPass, true, true, false>(ctx, nullptr, nullptr, tmp, n, shift, m2, bucket_off,
+                                                          tiles, B1, cursor2, out_pairs, nullptr, nullptr, s)));
     else
-      GBJ_TRY((launch_tile_pass<kDigit, true, false>(ctx, nullptr, nullptr, tmp, n, shift, m2, bucket_off,
-                                                     tiles, B1, cursor2, nullptr, out_keys, out_vals, s)));
+      GBJ_TRY((launch_tile_pass<kPass, true, false, false>(ctx, nullptr, nullptr, tmp, n, shift, m2, bucket_off,
+                                                           tiles, B1, cursor2, nullptr, out_keys, out_vals, s)));
   }
   if (offsets) GBJ_CHECK_CUDA(ctx, cudaMemcpyAsync(offsets, off, sizeof(uint64_t) * (P + 1),
                                                    cudaMemcpyDeviceToDevice, s));
@@ -691,12 +727,17 @@ namespace gbj {
 
 int partition_tuples(gbj_ctx *ctx, const int32_t *keys, const int32_t *vals, uint64_t n,
                      int digit, int shift, int bits, int2 *out_pairs, int32_t *out_keys,
-                     int32_t *out_vals, uint64_t *offsets, cudaStream_t s, int passes) {
+                     int32_t *out_vals, uint64_t *offsets, cudaStream_t s, int passes, bool hash_out) {
+  if (hash_out) {
+    if (digit != GBJ_DIGIT_HASH) return set_error(ctx, GBJ_ERR_INVALID, "partition: hashed tuples need hash digits");
+    return partition_impl<GBJ_DIGIT_HASH, true>(ctx, keys, vals, n, shift, bits, out_pairs, out_keys, out_vals,
+                                                offsets, s, passes);
+  }
   if (digit == GBJ_DIGIT_HASH)
-    return partition_impl<GBJ_DIGIT_HASH>(ctx, keys, vals, n, shift, bits, out_pairs, out_keys,
-                                          out_vals, offsets, s, passes);
-  return partition_impl<GBJ_DIGIT_KEY>(ctx, keys, vals, n, shift, bits, out_pairs, out_keys,
-                                       out_vals, offsets, s, passes);
+    return partition_impl<GBJ_DIGIT_HASH, false>(ctx, keys, vals, n, shift, bits, out_pairs, out_keys,
+                                                 out_vals, offsets, s, passes);
+  return partition_impl<GBJ_DIGIT_KEY, false>(ctx, keys, vals, n, shift, bits, out_pairs, out_keys,
+                                              out_vals, offsets, s, passes);
 }
 
 }  // namespace gbj
@@ -805,7 +846,9 @@ static int radix_join_impl(gbj_ctx *ctx, const int32_t *d_build_keys, const int3
                      "radix_join: one pass takes at most 8 radix bits, two passes at least 2");
   const uint32_t P = 1u << bits;
   const uint64_t w = 1u << 17;  // probe tuples per work item
-  const uint32_t sentinel_part = gbjd::fmix32((uint32_t)INT32_MIN) & (P - 1);
+  // tuples carry fmix32(key); the partition of the hash equal to the empty
+  // marker takes the index-table path
+  const uint32_t sentinel_part = (uint32_t)kEmpty & (P - 1);
 
   Scratch scratch(ctx, s);
   int2 *R, *S;
@@ -818,9 +861,9 @@ static int radix_join_impl(gbj_ctx *ctx, const int32_t *d_build_keys, const int3
   GBJ_TRY(scratch.get(P + 1, &items));
   GBJ_TRY(scratch.get(1, &ctr));
   GBJ_TRY(partition_tuples(ctx, d_build_keys, b_pay && !by_rows ? d_build_payload : nullptr, n_build,
-                           GBJ_DIGIT_HASH, 0, bits, R, nullptr, nullptr, ro, s, passes));
+                           GBJ_DIGIT_HASH, 0, bits, R, nullptr, nullptr, ro, s, passes, true));
   GBJ_TRY(partition_tuples(ctx, d_probe_keys, p_pay && !by_rows ? d_probe_payload : nullptr, n_probe,
-                           GBJ_DIGIT_HASH, 0, bits, S, nullptr, nullptr, so, s, passes));
+                           GBJ_DIGIT_HASH, 0, bits, S, nullptr, nullptr, so, s, passes, true));
   k_join_items<<<(P + 255) / 256, 256, 0, s>>>(ro, so, P, kRMax, w, items);
   GBJ_TRY(after_launch(ctx, "k_join_items", s));
   GBJ_TRY(scan_u64(ctx, items, items, P, s));
@@ -828,16 +871,16 @@ static int radix_join_impl(gbj_ctx *ctx, const int32_t *d_build_keys, const int3
   const RowCols rc{minor ? d_build_minor : nullptr, minor ? d_probe_minor : nullptr,
                    b_pay ? d_build_payload : nullptr, p_pay ? d_probe_payload : nullptr};
   if (by_rows)
-    return launch_join<kRMax, kJoinThreads, kAggRows>(ctx, R, ro, S, so, items, P, bits, w, sentinel_part,
+    return launch_join<kRMax, kJoinThreads, kAggRows>(ctx, R, ro, S, so, items, P, w, sentinel_part,
                                                       spec, rc, d_out, ctr, s);
   const bool two = spec.n == 2 && spec.op[0] == GBJ_AGG_COUNT && spec.op[1] == GBJ_AGG_SUM;
   if (two && spec.operand[1] == GBJ_VAL_ROWID_XOR)
-    return launch_join<kRMax, kJoinThreads, kAggCountXor>(ctx, R, ro, S, so, items, P, bits, w, sentinel_part,
+    return launch_join<kRMax, kJoinThreads, kAggCountXor>(ctx, R, ro, S, so, items, P, w, sentinel_part,
                                                           spec, rc, d_out, ctr, s);
   if (two && spec.operand[1] == GBJ_VAL_PRODUCT)
-    return launch_join<kRMax, kJoinThreads, kAggCountProduct>(ctx, R, ro, S, so, items, P, bits, w,
+    return launch_join<kRMax, kJoinThreads, kAggCountProduct>(ctx, R, ro, S, so, items, P, w,
                                                               sentinel_part, spec, rc, d_out, ctr, s);
-  return launch_join<kRMax, kJoinThreads, kAggGeneric>(ctx, R, ro, S, so, items, P, bits, w, sentinel_part,
+  return launch_join<kRMax, kJoinThreads, kAggGeneric>(ctx, R, ro, S, so, items, P, w, sentinel_part,
                                                        spec, rc, d_out, ctr, s);
 }
 

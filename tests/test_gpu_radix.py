@@ -215,3 +215,38 @@ def test_stream_ordering_with_torch(ctx, oracle):
         out = ctx.radix_join_agg(d_r, None, d_s, None, CONFIG2_AGGS)
         got = out.cpu().tolist()
     assert got == exp
+
+
+def _fmix32_inv(h):
+    """Inverse of murmur3's fmix32 on 32-bit values."""
+    m = (1 << 32) - 1
+    h ^= h >> 16
+    h = (h * 0x7ED1B41D) & m
+    h ^= (h >> 13) ^ (h >> 26)
+    h = (h * 0xA5CB9243) & m
+    h ^= h >> 16
+    return h
+
+
+@pytest.mark.parametrize("bits", [0, 3, 14])
+def test_radix_join_extreme_keys(ctx, oracle, bits):
+    """Keys at the int32 extremes, and the key whose fmix32 equals the
+    on-chip table's empty marker (0x80000000), which the partitioned tuples
+    carry as their hash: every one matches exactly like any other key, and
+    an aggregate reading the key gets it back unhashed."""
+    special = _fmix32_inv(0x80000000)
+    special = special - (1 << 32) if special >= 1 << 31 else special
+    rng = np.random.default_rng(bits + 5)
+    extremes = np.array([np.iinfo(np.int32).min, np.iinfo(np.int32).max, -1, 0, 1, special], np.int32)
+    rk = np.concatenate([extremes, extremes[[0, 5]],
+                         rng.integers(-(1 << 31), 1 << 31, 40000).astype(np.int32)])
+    rp = rng.integers(-1000, 1000, len(rk)).astype(np.int32)
+    sk = np.concatenate([np.repeat(extremes, 3), rng.choice(rk, 100000),
+                         rng.integers(-(1 << 31), 1 << 31, 20000).astype(np.int32)])
+    sp = rng.integers(-1000, 1000, len(sk)).astype(np.int32)
+    aggs = [(abi.AGG_COUNT, abi.VAL_ONE), (abi.AGG_SUM, abi.VAL_BUILD_KEY),
+            (abi.AGG_MIN, abi.VAL_BUILD_KEY), (abi.AGG_MAX, abi.VAL_BUILD_KEY),
+            (abi.AGG_SUM, abi.VAL_PRODUCT)]
+    out = ctx.radix_join_agg(dev(rk), dev(rp), dev(sk), dev(sp), aggs, bits=bits)
+    ctx.sync()
+    assert host(out).tolist() == oracle.join_agg(rk, rp, sk, sp, aggs)
