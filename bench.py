@@ -57,6 +57,8 @@ def parse():
     ap.add_argument("--theta", type=float, default=0.0, help="group-by Zipf exponent")
     ap.add_argument("--bits", type=int, default=0,
                     help="radix join: fixed partition bits instead of the autotuner's choice")
+    ap.add_argument("--block", type=int, default=0,
+                    help="radix join: fixed join kernel block size (512 or 1024) instead of the autotuner's")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--cpu-sample-log", type=int, default=26,
@@ -98,6 +100,7 @@ class RadixJoin:
         self.ls = args.log_s or 29
         self.nr, self.ns = 1 << self.lr, 1 << self.ls
         self.fixed_bits = args.bits
+        self.fixed_block = args.block
 
     def describe(self):
         return {"workload": f"radix-partitioned hash join R=2^{self.lr} unique int32 keys, "
@@ -125,15 +128,18 @@ class RadixJoin:
         self.outs = [torch.empty(2, dtype=torch.int64, device="cuda") for _ in self.THETAS]
         # the autotuner picks the partition bits for this shape (untimed);
         # every timed join then runs with the cached choice
-        if self.fixed_bits:
+        if self.fixed_bits or self.fixed_block:
             self.tuned_bits, self.tune_ms = self.fixed_bits, None
+            self.block = self.fixed_block
         else:
             self.tuned_bits, self.tune_ms = ctx.autotune_radix_join(self.d_r, None, self.d_s[0], None,
                                                                     self.aggs)
+            self.block = ctx.tune_lookup("radixblock", self.nr, self.ns)
 
     def step(self):
         for ds, o in zip(self.d_s, self.outs):
-            self.ctx.radix_join_agg(self.d_r, None, ds, None, self.aggs, out=o, bits=self.fixed_bits)
+            self.ctx.radix_join_agg(self.d_r, None, ds, None, self.aggs, out=o, bits=self.fixed_bits,
+                                    block=self.fixed_block)
 
     def results(self):
         return [o.cpu().tolist() for o in self.outs]
@@ -176,7 +182,8 @@ class RadixJoin:
                 ready = torch.cuda.Event()
                 ready.record(self.copy_stream)
             comp.wait_event(ready)
-            self.ctx.radix_join_agg(rb, None, self.s_bufs[b], None, self.aggs, out=o, bits=self.fixed_bits)
+            self.ctx.radix_join_agg(rb, None, self.s_bufs[b], None, self.aggs, out=o, bits=self.fixed_bits,
+                                    block=self.fixed_block)
             self.s_free[b].record(comp)
             self.h_out[i].copy_(o, non_blocking=True)
             self.joins += 1
@@ -209,8 +216,8 @@ class RadixJoin:
                 "job_frac_compulsory": round(comp / (ms / 1e3) / 1e9 / peak, 4),
                 "build_plus_probe_gtuples_s": round(len(self.THETAS) * (self.nr + self.ns) * steps
                                                     / (ms / 1e3) / 1e9, 3),
-                "radix_bits": self.tuned_bits,
-                "radix_bits_from": "fixed" if self.fixed_bits else "autotuner"}
+                "radix_bits": self.tuned_bits, "join_block": self.block,
+                "radix_bits_from": "fixed" if (self.fixed_bits or self.fixed_block) else "autotuner"}
 
     def cpu(self, threads, sample_log):
         from oracle import oracle as O

@@ -562,8 +562,11 @@ int gbj_server_unregister_table(gbj_server *srv, uint64_t table_id);
  * fastest of two timed runs, CUDA events on `stream`) and caches the winner
  * in the context under the operation and the log2 sizes of its inputs.
  * Later calls of that shape that pass no explicit sizing use it:
- *   radix join     partition bits 1..15 (bits > 8 means two passes) --
- *                  gbj_radix_join_agg with params NULL or zero bits;
+ *   radix join     join kernel block size (512: two blocks per SM with
+ *                  4608-tuple build chunks; 1024: one block, 9216) and,
+ *                  for each, partition bits 1..15 (bits > 8 means two
+ *                  passes) -- gbj_radix_join_agg with params NULL or zero
+ *                  bits / block;
  *   plain join     table size 2^hash_bits (load factor 1/2, 1/4, 1/8) --
  *                  gbj_join_build with hash_bits 0;
  *   group-by       strategy 1, or strategy 2 with its partition bits --
@@ -588,9 +591,10 @@ int gbj_autotune_groupby(gbj_ctx *ctx, const int32_t *d_keys,
                          const int32_t *d_values, uint64_t n,
                          uint64_t expected_groups, int32_t *best_strategy,
                          int32_t *best_bits, double *best_ms, void *stream);
-/* Cached decision for op "radix" (a = n_build, b = n_probe), "join"
- * (a = n_build, b = 0) or "groupby" (a = n, b = expected_groups; value =
- * strategy << 8 | bits); -1 when none. */
+/* Cached decision for op "radixblock" (a = n_build, b = n_probe; the join
+ * kernel's block size), "radix" / "radix512" (the partition bits used with
+ * 1024 / 512 threads), "join" (a = n_build, b = 0) or "groupby" (a = n,
+ * b = expected_groups; value = strategy << 8 | bits); -1 when none. */
 int gbj_tune_lookup(gbj_ctx *ctx, const char *op, uint64_t a, uint64_t b,
                     int32_t *value);
 int gbj_tune_clear(gbj_ctx *ctx);

@@ -47,10 +47,6 @@ constexpr int kTile = 4096;          // tuples per tile of a partition pass
 constexpr int kTileThreads = 512;
 constexpr int kTilePer = kTile / kTileThreads;  // tuples per thread
 constexpr int kTileCtas = 2;                    // CTAs per SM (register budget)
-// Join kernel: largest build chunk held on chip, threads and CTAs per SM.
-constexpr int kJoinRMax = 9216;
-constexpr int kJoinThreads = 1024;
-constexpr int kJoinCtas = 1;
 constexpr int kTileWarps = kTileThreads / 32;
 constexpr int kMaxDigits = 256;      // <= 8 digit bits per pass
 constexpr int32_t kEmpty = INT32_MIN;
@@ -166,8 +162,9 @@ __global__ void __launch_bounds__(kTileThreads, kTileCtas)
         if (kPairsIn) {
           tup[j] = __ldcs(pin + i);
         } else {
-          const int32_t k = __ldcs(keys + i);
-          tup[j].x = kHashLoad ? (int32_t)gbjd::fmix32((uint32_t)k) : k;
+          // (kHashLoad: hashed when the tile is consumed, so this prefetch
+          // stays in flight through the previous tile's write phase)
+          tup[j].x = __ldcs(keys + i);
           tup[j].y = vals ? __ldcs(vals + i) : (int32_t)i;
         }
       }
@@ -189,6 +186,7 @@ __global__ void __launch_bounds__(kTileThreads, kTileCtas)
     uint32_t dg[kTilePer], rk[kTilePer];
 #pragma unroll
     for (int j = 0; j < kTilePer; ++j) {
+      if (kHashLoad) tup[j].x = (int32_t)gbjd::fmix32((uint32_t)tup[j].x);
       if (tid + j * kTileThreads < cnt) {
         dg[j] = digit_of<kDigit>(tup[j].x, dshift, dmask);
         rk[j] = atomicAdd(&S.whist[warp][dg[j]], 1u);
@@ -393,10 +391,11 @@ struct JoinItem {
 // build chunk of m tuples (nb = ceil(2m / 4) buckets rounded up to 16):
 //   keys[4 nb] + values[4 nb]            (every partition but one), or
 //   pairs[kRMax] + index[4 nb] (16-bit) (the partition whose tuples may hash
-//                                         to the empty marker).
-// followed by the per-warp probe queues.
-template <int kRMax, int kThreads, int kAgg>
-__global__ void __launch_bounds__(kThreads, 1)
+//                                         to the empty marker),
+// followed by the per-warp probe queues.  kCtas blocks share an SM, so one
+// block's clear / build / barriers overlap another's probes.
+template <int kRMax, int kThreads, int kCtas, int kAgg>
+__global__ void __launch_bounds__(kThreads, kCtas)
     k_radix_join(const int2 *__restrict__ R, const uint64_t *__restrict__ ro,
                  const int2 *__restrict__ S, const uint64_t *__restrict__ so,
                  const uint64_t *__restrict__ item_off, uint32_t P, uint32_t w,
@@ -421,20 +420,19 @@ __global__ void __launch_bounds__(kThreads, 1)
   // thread 0: claims the next item and resolves its extent
   auto fetch = [&]() {
     const unsigned long long item = atomicAdd(item_ctr, 1ull);
-    JoinItem it{};
-    it.valid = item < total;
-    if (it.valid) {
+    s_it.valid = item < total;
+    if (item < total) {
       const uint32_t p = item_partition(item_off, P, total, item);
       const uint64_t r0 = ro[p], r1 = ro[p + 1], s0 = so[p], s1 = so[p + 1];
       const uint64_t nrc = (r1 - r0 + kRMax - 1) / kRMax;
       const uint64_t local = item - item_off[p];
-      it.rb = r0 + (local % nrc) * kRMax;
-      it.m = (uint32_t)((it.rb + kRMax < r1 ? it.rb + kRMax : r1) - it.rb);
-      it.sb = s0 + (local / nrc) * w;
-      it.ns = (uint32_t)((it.sb + w < s1 ? it.sb + w : s1) - it.sb);
-      it.part = p;
+      const uint64_t rb = r0 + (local % nrc) * kRMax, sb = s0 + (local / nrc) * w;
+      s_it.rb = rb;
+      s_it.m = (uint32_t)((rb + kRMax < r1 ? rb + kRMax : r1) - rb);
+      s_it.sb = sb;
+      s_it.ns = (uint32_t)((sb + w < s1 ? sb + w : s1) - sb);
+      s_it.part = p;
     }
-    s_it = it;
   };
   if (threadIdx.x == 0) fetch();
   __syncthreads();
@@ -442,14 +440,13 @@ __global__ void __launch_bounds__(kThreads, 1)
   const unsigned lt = (1u << lane) - 1u;
   int4 *wq = queue + (threadIdx.x >> 5) * (4 * 32);
   for (;;) {
-    const JoinItem it = s_it;
-    if (!it.valid) break;
-    const int2 *Rp = R + it.rb;
-    const int2 *Sp = S + it.sb;
-    const uint32_t m = it.m, ns = it.ns;
+    if (!s_it.valid) break;
+    const int2 *Rp = R + s_it.rb;
+    const int2 *Sp = S + s_it.sb;
+    const uint32_t m = s_it.m, ns = s_it.ns;
+    const bool fast = s_it.part != sentinel_part;
     const uint32_t nb = ((2 * m + 3) / 4 + 15) & ~15u;  // buckets
     const uint32_t cap = 4 * nb;
-    const bool fast = it.part != sentinel_part;
     if (threadIdx.x == 0) s_dup = 0;
     if (fast) {
       // ---- keys + values table of 4-slot buckets ----
@@ -457,22 +454,25 @@ __global__ void __launch_bounds__(kThreads, 1)
       for (uint32_t i = threadIdx.x; i < nb; i += kThreads) tk4[i] = make_int4(kEmpty, kEmpty, kEmpty, kEmpty);
       __syncthreads();
       bool dup = false;
+      // An insert reads its bucket and claims the first empty slot with one
+      // CAS; a lost race re-reads the bucket, a full bucket passes to the
+      // next.  Every failed CAS fills a slot, so 5 nb reads bound the loop.
       auto insert = [&](int2 t) {
-        const uint32_t h = (uint32_t)t.x;
-        uint32_t b = home_bucket(h, nb);
-        const uint32_t o = h >> 16;  // start slot in the bucket (spreads the CASes)
-        for (uint32_t step = 0; step < nb; ++step) {
-#pragma unroll
-          for (uint32_t j = 0; j < 4; ++j) {
-            const uint32_t sl = 4 * b + ((o + j) & 3);
-            const int32_t old = atomicCAS(&tkey[sl], kEmpty, t.x);
-            if (old == kEmpty) {
-              tval[sl] = t.y;
-              return;
-            }
-            dup |= (old == t.x);
+        uint32_t b = home_bucket((uint32_t)t.x, nb);
+        for (uint32_t step = 0; step < 5 * nb; ++step) {
+          const int4 kk = tk4[b];
+          dup |= (kk.x == t.x) | (kk.y == t.x) | (kk.z == t.x) | (kk.w == t.x);
+          const int j = kk.x == kEmpty ? 0 : kk.y == kEmpty ? 1 : kk.z == kEmpty ? 2 : kk.w == kEmpty ? 3 : 4;
+          if (j == 4) {
+            b = b + 1 == nb ? 0 : b + 1;
+            continue;
           }
-          b = b + 1 == nb ? 0 : b + 1;
+          const int32_t old = atomicCAS(&tkey[4 * b + j], kEmpty, t.x);
+          if (old == kEmpty) {
+            tval[4 * b + j] = t.y;
+            return;
+          }
+          dup |= old == t.x;
         }
       };
       // the whole chunk's loads in flight at once (8 per thread per round)
@@ -509,12 +509,13 @@ __global__ void __launch_bounds__(kThreads, 1)
     }
     __syncthreads();
     const bool unique = s_dup == 0;
-    // next item: fetched now, consumed after the closing barrier
+    // next item: fetched now, consumed after the closing barrier (every
+    // thread has read this item's extent above)
     if (threadIdx.x == 0) fetch();
     if (fast) {
       const int4 *tk4 = reinterpret_cast<const int4 *>(tkey);
-      // One bucket: matches among its four slots; true when the probe is done
-      // (a match of a unique key, or a bucket with an empty slot).
+      // One bucket, general form (duplicate build keys, queued probes):
+      // every match; true when the probe is done.
       auto bucket = [&](uint32_t h, int32_t v, uint32_t b) -> bool {
         const int4 kk = tk4[b];
         const int32_t k = (int32_t)h;
@@ -530,7 +531,8 @@ __global__ void __launch_bounds__(kThreads, 1)
       // Probe rounds of 4 tuples per thread: every probe checks its home
       // bucket; the few that must continue go to the warp's own queue, which
       // the warp's lanes then drain together.  The next round's tuples are
-      // loaded while this round is probed.
+      // loaded while this round is probed.  With unique build keys a home
+      // bucket resolves a probe without a loop: at most one slot matches.
       int2 nxt[4];
 #pragma unroll
       for (int u = 0; u < 4; ++u) {
@@ -548,26 +550,39 @@ __global__ void __launch_bounds__(kThreads, 1)
         uint32_t qn = 0;  // warp-uniform queue length
 #pragma unroll
         for (int u = 0; u < 4; ++u) {
-          bool more = false;
-          uint32_t b = 0;
-          if (j0 + threadIdx.x + u * kThreads < ns) {
-            b = home_bucket((uint32_t)t[u].x, nb);
-            more = !bucket((uint32_t)t[u].x, t[u].y, b);
+          const bool valid = j0 + threadIdx.x + u * kThreads < ns;
+          const uint32_t h = (uint32_t)t[u].x;
+          const uint32_t b = home_bucket(h, nb);
+          bool more;
+          if (unique) {
+            const int4 kk = tk4[b];
+            const bool e0 = kk.x == t[u].x, e1 = kk.y == t[u].x, e2 = kk.z == t[u].x, e3 = kk.w == t[u].x;
+            const bool room = (kk.x == kEmpty) | (kk.y == kEmpty) | (kk.z == kEmpty) | (kk.w == kEmpty);
+            const bool found = valid & (e0 | e1 | e2 | e3);
+            if (found) {
+              const uint32_t idx = e0 ? 0 : e1 ? 1 : e2 ? 2 : 3;
+              join_match<kAgg>(spec, rc, acc, a_cnt, a_sum, h, tval[4 * b + idx], t[u].y);
+            }
+            more = valid & !found & !room;
+          } else {
+            more = valid && !bucket(h, t[u].y, b);
           }
           const unsigned bal = __ballot_sync(0xffffffffu, more);
           if (more) wq[qn + __popc(bal & lt)] = make_int4(t[u].x, t[u].y, (int)(b + 1 == nb ? 0 : b + 1), 0);
           qn += __popc(bal);
         }
-        __syncwarp();
-        for (uint32_t i = lane; i < qn; i += 32) {
-          const int4 e = wq[i];
-          uint32_t b = (uint32_t)e.z;
-          for (uint32_t step = 1; step < nb; ++step) {
-            if (bucket((uint32_t)e.x, e.y, b)) break;
-            b = b + 1 == nb ? 0 : b + 1;
+        if (qn) {
+          __syncwarp();
+          for (uint32_t i = lane; i < qn; i += 32) {
+            const int4 e = wq[i];
+            uint32_t b = (uint32_t)e.z;
+            for (uint32_t step = 1; step < nb; ++step) {
+              if (bucket((uint32_t)e.x, e.y, b)) break;
+              b = b + 1 == nb ? 0 : b + 1;
+            }
           }
+          __syncwarp();
         }
-        __syncwarp();
       }
     } else {
       // index table: plain linear probing, one slot per step
@@ -612,13 +627,13 @@ constexpr size_t join_smem() {
   return (size_t)2 * (2 * kRMax + 64) * sizeof(int32_t) + (size_t)4 * kThreads * sizeof(int4);
 }
 
-template <int kRMax, int kThreads, int kAgg>
+template <int kRMax, int kThreads, int kCtas, int kAgg>
 int launch_join(gbj_ctx *ctx, const int2 *R, const uint64_t *ro, const int2 *S,
                 const uint64_t *so, const uint64_t *item_off, uint32_t P,
                 uint32_t w, uint32_t sentinel_part, const AggSpec &spec, const RowCols &rc,
                 int64_t *out, unsigned long long *ctr, cudaStream_t s) {
   const size_t smem = join_smem<kRMax, kThreads>();
-  auto kern = k_radix_join<kRMax, kThreads, kAgg>;
+  auto kern = k_radix_join<kRMax, kThreads, kCtas, kAgg>;
   GBJ_CHECK_CUDA(ctx, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                            (int)smem));
   int per_sm = 0;
@@ -627,6 +642,34 @@ int launch_join(gbj_ctx *ctx, const int2 *R, const uint64_t *ro, const int2 *S,
   kern<<<ctx->sm_count * per_sm, kThreads, smem, s>>>(R, ro, S, so, item_off, P, w,
                                                      sentinel_part, spec, rc, out, ctr);
   return after_launch(ctx, "k_radix_join", s);
+}
+
+// The two join kernel shapes: 1024 threads with build chunks of 9216 tuples
+// (one block per SM), or 512 threads with chunks of 4608 (two blocks per
+// SM; partitions then need one more radix bit).
+struct JoinShape {
+  int threads, rmax;
+};
+constexpr JoinShape kJoinWide{1024, 9216};
+constexpr JoinShape kJoinPair{512, 4608};
+
+template <int kRMax, int kThreads, int kCtas>
+int launch_join_agg(gbj_ctx *ctx, bool by_rows, const AggSpec &spec, const int2 *R, const uint64_t *ro,
+                    const int2 *S, const uint64_t *so, const uint64_t *items, uint32_t P, uint32_t w,
+                    uint32_t sentinel_part, const RowCols &rc, int64_t *d_out, unsigned long long *ctr,
+                    cudaStream_t s) {
+  if (by_rows)
+    return launch_join<kRMax, kThreads, kCtas, kAggRows>(ctx, R, ro, S, so, items, P, w, sentinel_part, spec, rc,
+                                                         d_out, ctr, s);
+  const bool two = spec.n == 2 && spec.op[0] == GBJ_AGG_COUNT && spec.op[1] == GBJ_AGG_SUM;
+  if (two && spec.operand[1] == GBJ_VAL_ROWID_XOR)
+    return launch_join<kRMax, kThreads, kCtas, kAggCountXor>(ctx, R, ro, S, so, items, P, w, sentinel_part, spec,
+                                                             rc, d_out, ctr, s);
+  if (two && spec.operand[1] == GBJ_VAL_PRODUCT)
+    return launch_join<kRMax, kThreads, kCtas, kAggCountProduct>(ctx, R, ro, S, so, items, P, w, sentinel_part,
+                                                                 spec, rc, d_out, ctr, s);
+  return launch_join<kRMax, kThreads, kCtas, kAggGeneric>(ctx, R, ro, S, so, items, P, w, sentinel_part, spec, rc,
+                                                          d_out, ctr, s);
 }
 
 template <int kDigit, bool kPairsIn, bool kAoSOut, bool kHashLoad>
@@ -792,9 +835,9 @@ static int radix_join_impl(gbj_ctx *ctx, const int32_t *d_build_keys, const int3
       return set_error(ctx, GBJ_ERR_UNSUPPORTED, "radix_join: radix bits must be in [0, 15]");
     if (params->passes < 0 || params->passes > 2)
       return set_error(ctx, GBJ_ERR_UNSUPPORTED, "radix_join: passes must be 0 (auto), 1 or 2");
-    if (params->block != 0 && params->block != kJoinThreads)
+    if (params->block != 0 && params->block != kJoinWide.threads && params->block != kJoinPair.threads)
       return set_error(ctx, GBJ_ERR_UNSUPPORTED,
-                       "radix_join: the join kernel runs 1024 threads per block (block 0 or 1024)");
+                       "radix_join: the join kernel runs 512 or 1024 threads per block (block 0, 512 or 1024)");
   }
   AggSpec spec = make_spec(aggs, n_aggs);
   // Which value each side carries into the partitions.
@@ -823,8 +866,16 @@ static int radix_join_impl(gbj_ctx *ctx, const int32_t *d_build_keys, const int3
 
   // ---- plan: fewest radix bits whose largest expected build partition
   //      (mean + 5 sd) fits the on-chip table; explicit params override ----
-  constexpr int kRMax = kJoinRMax;
   const int passes = params ? params->passes : 0;
+  // join kernel shape: the caller's block size, else an autotuned one, else
+  // two 512-thread blocks per SM
+  int block = params ? params->block : 0;
+  if (!block) {
+    const int32_t tb = tuned_value(ctx, tune_key("radixblock", n_build, n_probe));
+    block = tb > 0 ? tb : kJoinPair.threads;
+  }
+  const JoinShape shape = block == kJoinWide.threads ? kJoinWide : kJoinPair;
+  const uint32_t kRMax = (uint32_t)shape.rmax;
   int bits = 1;
   while (bits < kMaxPartBits) {
     const double mean = (double)n_build / (double)(1u << bits);
@@ -833,7 +884,8 @@ static int radix_join_impl(gbj_ctx *ctx, const int32_t *d_build_keys, const int3
   }
   const bool explicit_bits = params && (params->log_parts > 0 || params->bits > 0);
   if (!explicit_bits) {  // an autotuned choice for this size bucket, if any
-    const int32_t tb = tuned_value(ctx, tune_key("radix", n_build, n_probe));
+    const int32_t tb = tuned_value(ctx, tune_key(shape.threads == kJoinWide.threads ? "radix" : "radix512",
+                                                 n_build, n_probe));
     if (tb > 0) bits = std::min<int>(tb, kMaxPartBits);
     // a pinned pass count bounds the automatic choice
     if (passes == 1) bits = std::min(bits, 8);
@@ -870,18 +922,11 @@ static int radix_join_impl(gbj_ctx *ctx, const int32_t *d_build_keys, const int3
   GBJ_CHECK_CUDA(ctx, cudaMemsetAsync(ctr, 0, sizeof(unsigned long long), s));
   const RowCols rc{minor ? d_build_minor : nullptr, minor ? d_probe_minor : nullptr,
                    b_pay ? d_build_payload : nullptr, p_pay ? d_probe_payload : nullptr};
-  if (by_rows)
-    return launch_join<kRMax, kJoinThreads, kAggRows>(ctx, R, ro, S, so, items, P, w, sentinel_part,
-                                                      spec, rc, d_out, ctr, s);
-  const bool two = spec.n == 2 && spec.op[0] == GBJ_AGG_COUNT && spec.op[1] == GBJ_AGG_SUM;
-  if (two && spec.operand[1] == GBJ_VAL_ROWID_XOR)
-    return launch_join<kRMax, kJoinThreads, kAggCountXor>(ctx, R, ro, S, so, items, P, w, sentinel_part,
-                                                          spec, rc, d_out, ctr, s);
-  if (two && spec.operand[1] == GBJ_VAL_PRODUCT)
-    return launch_join<kRMax, kJoinThreads, kAggCountProduct>(ctx, R, ro, S, so, items, P, w,
-                                                              sentinel_part, spec, rc, d_out, ctr, s);
-  return launch_join<kRMax, kJoinThreads, kAggGeneric>(ctx, R, ro, S, so, items, P, w, sentinel_part,
-                                                       spec, rc, d_out, ctr, s);
+  if (shape.threads == kJoinWide.threads)
+    return launch_join_agg<kJoinWide.rmax, kJoinWide.threads, 1>(ctx, by_rows, spec, R, ro, S, so, items, P, w,
+                                                                 sentinel_part, rc, d_out, ctr, s);
+  return launch_join_agg<kJoinPair.rmax, kJoinPair.threads, 2>(ctx, by_rows, spec, R, ro, S, so, items, P, w,
+                                                               sentinel_part, rc, d_out, ctr, s);
 }
 
 extern "C" {

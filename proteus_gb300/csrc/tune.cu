@@ -1,5 +1,6 @@
-// Autotuner: times candidate plans of the radix join (partition bits, which
-// also fixes one or two partitioning passes), the plain join (hash-table
+// Autotuner: times candidate plans of the radix join (join kernel block size
+// and partition bits, which also fix one or two partitioning passes), the
+// plain join (hash-table
 // size, i.e. load factor) and the group-by (strategy and partition bits) on
 // the caller's own inputs, and caches the fastest per size bucket in the
 // context.  Entry points called without explicit sizing read the cache
@@ -96,19 +97,41 @@ extern "C" int gbj_autotune_radix_join(gbj_ctx *ctx, const int32_t *d_build_keys
   if (!ctx) return GBJ_ERR_INVALID;
   if (n_build == 0 || n_probe == 0) return set_error(ctx, GBJ_ERR_INVALID, "autotune: empty input");
   cudaStream_t s = pick_stream(ctx, stream);
-  // around the default: fewest bits whose mean partition fits the on-chip table
-  int d = 1;
-  while (d < 15 && (double)n_build / (double)(1u << d) > 9216.0) ++d;
-  std::vector<int32_t> cands;
-  for (int b = std::max(1, d - 2); b <= std::min(15, d + 2); ++b) cands.push_back(b);
   int64_t *out = nullptr;
   GBJ_TRY(pool_alloc(ctx, GBJ_MAX_AGGS * sizeof(int64_t), s, reinterpret_cast<void **>(&out)));
-  const int rc = tune(ctx, s, tune_key("radix", n_build, n_probe), cands, [&] {
-    return gbj_radix_join_agg(ctx, d_build_keys, d_build_payload, n_build, d_probe_keys, d_probe_payload, n_probe,
-                              nullptr, aggs, n_aggs, out, s);
-  }, best_bits, best_ms);
+  // both join kernel shapes (512 threads, two blocks per SM, chunks of 4608
+  // build tuples; 1024 threads, one block, chunks of 9216), each with the
+  // radix bits around its default: fewest bits whose mean partition fits
+  const std::string kblock = tune_key("radixblock", n_build, n_probe);
+  const int32_t prev_block = tuned_value(ctx, kblock);
+  int rc = GBJ_OK;
+  int32_t best_block = -1, best_b = -1;
+  double best_t = 1e30;
+  for (const int32_t block : {512, 1024}) {
+    const double rmax = block == 1024 ? 9216.0 : 4608.0;
+    int d = 1;
+    while (d < 15 && (double)n_build / (double)(1u << d) > rmax) ++d;
+    std::vector<int32_t> cands;
+    for (int b = std::max(1, d - 2); b <= std::min(15, d + 2); ++b) cands.push_back(b);
+    set_tuned(ctx, kblock, block);
+    int32_t bits = -1;
+    double t = 0;
+    rc = tune(ctx, s, tune_key(block == 1024 ? "radix" : "radix512", n_build, n_probe), cands, [&] {
+      return gbj_radix_join_agg(ctx, d_build_keys, d_build_payload, n_build, d_probe_keys, d_probe_payload,
+                                n_probe, nullptr, aggs, n_aggs, out, s);
+    }, &bits, &t);
+    if (rc != GBJ_OK) break;
+    if (t < best_t) best_t = t, best_block = block, best_b = bits;
+  }
   pool_release(ctx, out, s);
-  return rc;
+  if (rc != GBJ_OK) {
+    set_tuned(ctx, kblock, prev_block);
+    return rc;
+  }
+  set_tuned(ctx, kblock, best_block);
+  if (best_bits) *best_bits = best_b;
+  if (best_ms) *best_ms = best_t;
+  return GBJ_OK;
 }
 
 extern "C" int gbj_autotune_join(gbj_ctx *ctx, const int32_t *d_build_keys, const int32_t *d_build_payload,

@@ -55,12 +55,13 @@ def test_partition_empty_and_invalid(ctx):
         ctx.partition(dev(np.arange(10, dtype=np.int32)), None, 16)
 
 
+@pytest.mark.parametrize("block", [512, 1024])
 @pytest.mark.parametrize("theta", [0.0, 0.5, 1.0])
 @pytest.mark.parametrize("nr,ns", [(1 << 12, 1 << 16), (1 << 18, 1 << 21)])
-def test_radix_join_zipf(ctx, oracle, theta, nr, ns):
+def test_radix_join_zipf(ctx, oracle, theta, nr, ns, block):
     rk, _ = engine.gen_build_side(31, nr, payload=False)
     sk, _ = engine.gen_probe_zipf(31, ns, nr, theta, 0.5)
-    out = ctx.radix_join_agg(dev(rk), None, dev(sk), None, CONFIG2_AGGS)
+    out = ctx.radix_join_agg(dev(rk), None, dev(sk), None, CONFIG2_AGGS, block=block)
     ctx.sync()
     exp = oracle.radix_join_agg(rk, None, sk, None, CONFIG2_AGGS, threads=cpu_threads())
     assert host(out).tolist() == exp
@@ -77,14 +78,15 @@ def test_radix_join_payload_aggregates(ctx, oracle):
     assert host(out).tolist() == oracle.join_agg(rk, rp, sk, sp, aggs, threads=cpu_threads())
 
 
-def test_radix_join_heavy_duplicates(ctx, oracle):
+@pytest.mark.parametrize("block", [512, 1024])
+def test_radix_join_heavy_duplicates(ctx, oracle, block):
     """A build partition larger than the on-chip table is split into chunks."""
     rng = np.random.default_rng(3)
     rk = np.concatenate([np.full(30000, 77, dtype=np.int32),
                          rng.integers(0, 1 << 20, 100000).astype(np.int32)])
     sk = np.concatenate([np.full(500, 77, dtype=np.int32),
                          rng.integers(0, 1 << 20, 200000).astype(np.int32)])
-    out = ctx.radix_join_agg(dev(rk), None, dev(sk), None, CONFIG2_AGGS, bits=4)
+    out = ctx.radix_join_agg(dev(rk), None, dev(sk), None, CONFIG2_AGGS, bits=4, block=block)
     ctx.sync()
     assert host(out).tolist() == oracle.join_agg(rk, None, sk, None, CONFIG2_AGGS)
 
@@ -146,7 +148,7 @@ def test_radix_join_minor_key_needs_both_sides(ctx):
     assert err.value.code == abi.ERR_INVALID
 
 
-@pytest.mark.parametrize("kw", [dict(block=512), dict(passes=3), dict(passes=1, bits=9),
+@pytest.mark.parametrize("kw", [dict(block=256), dict(passes=3), dict(passes=1, bits=9),
                                 dict(passes=2, bits=1), dict(bits=16)])
 def test_radix_params_refused(ctx, kw):
     """Parameters the join cannot honour are refused, never ignored."""
@@ -156,12 +158,13 @@ def test_radix_params_refused(ctx, kw):
     assert e.value.code == abi.ERR_UNSUPPORTED
 
 
-@pytest.mark.parametrize("passes,bits", [(1, 0), (1, 6), (2, 4), (2, 0), (0, 9)])
-def test_radix_params_passes_honoured(ctx, oracle, passes, bits):
+@pytest.mark.parametrize("passes,bits,block", [(1, 0, 0), (1, 6, 1024), (2, 4, 512), (2, 0, 512),
+                                               (0, 9, 1024), (0, 13, 512)])
+def test_radix_params_passes_honoured(ctx, oracle, passes, bits, block):
     rk, _ = engine.gen_build_side(4, 1 << 16, payload=False)
     sk, _ = engine.gen_probe_zipf(4, 1 << 19, 1 << 16, 0.5, 0.5)
     out = ctx.radix_join_agg(dev(rk), None, dev(sk), None, CONFIG2_AGGS, bits=bits, passes=passes,
-                             block=1024 if bits else 0)
+                             block=block)
     ctx.sync()
     assert host(out).tolist() == oracle.radix_join_agg(rk, None, sk, None, CONFIG2_AGGS,
                                                        threads=cpu_threads())

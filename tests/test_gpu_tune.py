@@ -15,10 +15,14 @@ def test_tune_radix_join(ctx, oracle):
     pk, _ = engine.gen_probe_zipf(32, 1 << 22, 1 << 20, 0.5)
     dbk, dpk = dev(bk), dev(pk)
     assert ctx.tune_lookup("radix", 1 << 20, 1 << 22) == -1
+    assert ctx.tune_lookup("radixblock", 1 << 20, 1 << 22) == -1
     bits, ms = ctx.autotune_radix_join(dbk, None, dpk, None, CONFIG2_AGGS)
     assert 1 <= bits <= 15 and ms > 0
-    assert ctx.tune_lookup("radix", 1 << 20, 1 << 22) == bits
-    out = ctx.radix_join_agg(dbk, None, dpk, None, CONFIG2_AGGS)  # uses the tuned bits
+    # the block size and, for it, the bits: both decided, both cached
+    block = ctx.tune_lookup("radixblock", 1 << 20, 1 << 22)
+    assert block in (512, 1024)
+    assert ctx.tune_lookup("radix" if block == 1024 else "radix512", 1 << 20, 1 << 22) == bits
+    out = ctx.radix_join_agg(dbk, None, dpk, None, CONFIG2_AGGS)  # uses the tuned shape and bits
     ctx.sync()
     exp = oracle.radix_join_agg(bk, None, pk, None, CONFIG2_AGGS, threads=cpu_threads())
     assert host(out).tolist() == list(exp)
