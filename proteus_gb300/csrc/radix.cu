@@ -454,25 +454,27 @@ __global__ void __launch_bounds__(kThreads, kCtas)
       for (uint32_t i = threadIdx.x; i < nb; i += kThreads) tk4[i] = make_int4(kEmpty, kEmpty, kEmpty, kEmpty);
       __syncthreads();
       bool dup = false;
-      // An insert reads its bucket and claims the first empty slot with one
-      // CAS; a lost race re-reads the bucket, a full bucket passes to the
-      // next.  Every failed CAS fills a slot, so 5 nb reads bound the loop.
+      // An insert CASes the slots of its home bucket, starting at a slot
+      // chosen by hash bits and wrapping within the bucket, then passes to
+      // the next bucket.  No read of the bucket first: a CAS is as cheap as
+      // a shared load and returns the slot's key, which also reveals a
+      // duplicate (equal keys try slots in the same order, so a later one
+      // meets the earlier one before any empty slot).
       auto insert = [&](int2 t) {
         uint32_t b = home_bucket((uint32_t)t.x, nb);
-        for (uint32_t step = 0; step < 5 * nb; ++step) {
-          const int4 kk = tk4[b];
-          dup |= (kk.x == t.x) | (kk.y == t.x) | (kk.z == t.x) | (kk.w == t.x);
-          const int j = kk.x == kEmpty ? 0 : kk.y == kEmpty ? 1 : kk.z == kEmpty ? 2 : kk.w == kEmpty ? 3 : 4;
-          if (j == 4) {
-            b = b + 1 == nb ? 0 : b + 1;
-            continue;
+        const uint32_t o = ((uint32_t)t.x >> 16) & 3u;
+        for (uint32_t step = 0; step < nb; ++step) {
+#pragma unroll
+          for (uint32_t j = 0; j < 4; ++j) {
+            const uint32_t sl = 4 * b + ((o + j) & 3u);
+            const int32_t old = atomicCAS(&tkey[sl], kEmpty, t.x);
+            if (old == kEmpty) {
+              tval[sl] = t.y;
+              return;
+            }
+            dup |= old == t.x;
           }
-          const int32_t old = atomicCAS(&tkey[4 * b + j], kEmpty, t.x);
-          if (old == kEmpty) {
-            tval[4 * b + j] = t.y;
-            return;
-          }
-          dup |= old == t.x;
+          b = b + 1 == nb ? 0 : b + 1;
         }
       };
       // the whole chunk's loads in flight at once (8 per thread per round)
