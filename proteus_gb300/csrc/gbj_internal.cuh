@@ -72,12 +72,14 @@ struct gbj_ctx {
 };
 
 struct gbj_table {
-  // wide: 16-byte slots {key, row+1, payload, 0}; else 8-byte {key, row+1};
-  // row+1 == 0 marks an empty slot.  The table metadata word follows the
-  // slots.
+  // 32-byte buckets of four slots (keys, then payloads or rows + 1), the
+  // rows of a payload table, the metadata words and the INT32_MIN side
+  // list, in one pool block starting at `slots`.
   void *slots = nullptr;
-  bool wide = false;
-  uint64_t mask = 0;          // slots - 1
+  int4 *rows = nullptr;
+  uint32_t *meta = nullptr;
+  int32_t *side = nullptr;
+  uint64_t mask = 0;          // slots - 1 (4 slots per bucket)
   const int32_t *keys = nullptr;
   const int32_t *payload = nullptr;
   uint64_t n = 0;

@@ -4,11 +4,13 @@
 // Replaces the JIT'd build / probe loops of HashJoinChained and
 // GpuHashJoinChained (core/olap/lib/operators/hash-join-chained.cpp:262-566,
 // core/olap/lib/operators/gpu/gpu-hash-join-chained.cpp:31-73).  The
-// reference chains entries behind a head array; here the table is an
-// open-addressing array of 64-bit slots {key, row+1} (0 = empty) sized to a
-// power of two with load factor <= 1/2, so a probe is one L2 sector in the
-// common case and the table for a 2^20-row build side (16 MiB) stays
-// resident in the 129 MB L2 while the probe side streams from HBM.
+// reference chains entries behind a head array; here the table is an array
+// of 32-byte buckets of four slots (keys, then payloads or rows + 1) sized
+// to a power of two with load factor <= 1/2, so a probe is one L2 sector in
+// the common case and the table for a 2^20-row build side (16 MiB) stays
+// resident in the 129 MB L2 while the probe side streams from HBM.  The
+// allocation-free entry point keeps a plain open-addressing array of 64-bit
+// {key, row + 1} slots in a static device array.
 // Semantics are the reference's: every build row is inserted (duplicates
 // allowed) and a probe row meets every build row with an equal key.
 #include <cooperative_groups.h>
@@ -28,107 +30,69 @@ __device__ __forceinline__ uint64_t make_slot(int32_t key, uint64_t row) {
   return ((row + 1) << 32) | (uint32_t)key;
 }
 
-// One table slot as a probe sees it: narrow tables hold {key, row+1} in 8
-// bytes; wide tables (build sides with a payload) hold {key, row+1,
-// payload, 0} in 16 bytes, so a match needs no second, dependent load of
-// the build payload.  row1 == 0 marks an empty slot in both layouts.
-struct SlotView {
-  int32_t key;
-  uint32_t row1;
-  int32_t pay;
-};
-
-template <bool kWide>
-__device__ __forceinline__ SlotView slot_at(const void *__restrict__ slots, uint64_t h) {
-  if (kWide) {
-    const int4 e = __ldg(reinterpret_cast<const int4 *>(slots) + h);
-    return {e.x, (uint32_t)e.y, e.z};
-  }
-  const uint64_t e = __ldg(reinterpret_cast<const uint64_t *>(slots) + h);
-  return {(int32_t)(uint32_t)e, (uint32_t)(e >> 32), 0};
-}
-
-// meta[0] = 1 once a duplicate build key was seen (probes may then not stop
-// at the first match).  A row that finds no free slot latches
-// GBJ_DEV_CAPACITY into *status (status may be null where the table has 2n
-// slots and cannot fill).  The claim is a CAS on the {key, row+1} word; a
-// wide slot's payload is written after it (the probe runs in a later kernel).
-template <bool kWide>
+// Build of the allocation-free entry point's table: 64-bit slots {key,
+// row + 1}, 0 = empty, linear probing; meta[0] = 1 once a duplicate build key
+// was seen (probes may then not stop at the first match).  The table has at
+// least 2n slots, so every row finds one.
 __global__ void __launch_bounds__(kThreads)
-    k_join_build(const int32_t *__restrict__ keys, const int32_t *__restrict__ payload, uint64_t n,
-                 void *__restrict__ slots, uint64_t mask, uint32_t *__restrict__ meta, uint32_t *status) {
+    k_join_build(const int32_t *__restrict__ keys, uint64_t n, uint64_t *__restrict__ slots, uint64_t mask,
+                 uint32_t *__restrict__ meta) {
   const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  bool dup = false;
   for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += stride) {
     const int32_t k = keys[i];
     const uint64_t entry = make_slot(k, i);
     uint64_t h = gbjd::fmix32((uint32_t)k) & mask;
-    bool dup = false, placed = false;
     for (uint64_t probe = 0; probe <= mask; ++probe) {
-      unsigned long long *w = kWide ? reinterpret_cast<unsigned long long *>(reinterpret_cast<int4 *>(slots) + h)
-                                    : reinterpret_cast<unsigned long long *>(slots) + h;
+      unsigned long long *w = reinterpret_cast<unsigned long long *>(slots) + h;
       uint64_t cur = *(volatile uint64_t *)w;
       if (cur == 0) {
         cur = atomicCAS(w, 0ull, (unsigned long long)entry);
-        if (cur == 0) {
-          if (kWide) reinterpret_cast<int32_t *>(w)[2] = payload[i];
-          placed = true;
-          break;
-        }
+        if (cur == 0) break;
       }
       dup |= ((int32_t)(uint32_t)cur == k);
       h = (h + 1) & mask;
     }
-    if (dup) meta[0] = 1;
-    if (!placed && status) gbjd::latch(status, GBJ_DEV_CAPACITY);
   }
+  if (dup) meta[0] = 1;
 }
 
 enum : int { kAggGeneric = 0, kAggCountXor = 1, kAggCountProduct = 2 };
 
-// Probe with fused aggregate.  Eight probe keys per thread walk their slot
-// chains in lockstep: every round checks the slot each still-open probe
-// holds and issues the next slot loads of all of them together, so a warp
-// waits for the longest chain once per round instead of once per probe and
-// keeps up to eight L2 requests per thread in flight.  kAgg selects a
-// specialised accumulator for the two aggregate lists the workloads use.
-template <bool kVec, int kAgg, bool kWide>
+// Probe with fused aggregate over the allocation-free entry point's table.
+// Eight probe keys per thread walk their slot chains in lockstep: every
+// round checks the slot each still-open probe holds and issues the next
+// slot loads of all of them together, so a warp waits for the longest chain
+// once per round instead of once per probe and keeps up to eight L2
+// requests per thread in flight.  kAgg selects a specialised accumulator
+// for the two aggregate lists the workloads use.
+template <bool kVec, int kAgg>
 __global__ void __launch_bounds__(kThreads)
-    k_join_probe_agg(const int32_t *__restrict__ keys,
-                     const int32_t *__restrict__ pay, uint64_t n,
-                     const void *__restrict__ slots, uint64_t mask,
-                     const int32_t *__restrict__ bpay,
-                     const uint32_t *__restrict__ meta, gbj::AggSpec spec,
-                     int64_t *out) {
+    k_join_probe_agg(const int32_t *__restrict__ keys, const int32_t *__restrict__ pay, uint64_t n,
+                     const uint64_t *__restrict__ slots, uint64_t mask, const int32_t *__restrict__ bpay,
+                     const uint32_t *__restrict__ meta, gbj::AggSpec spec, int64_t *out) {
   __shared__ int64_t red[32 * GBJ_MAX_AGGS];
   gbjd::Acc acc;
   acc.init(spec);
   int64_t a_cnt = 0, a_sum = 0;
   const bool unique = meta[0] == 0;
   const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
-  auto match = [&](int32_t k, int64_t pv, uint64_t prow, const SlotView &e) {
-    const uint32_t r = e.row1 - 1;
+  // a slot is {key (low word), row + 1 (high word)}; row + 1 == 0: empty
+  auto skey = [](uint64_t e) { return (int32_t)(uint32_t)e; };
+  auto srow1 = [](uint64_t e) { return (uint32_t)(e >> 32); };
+  auto match = [&](int32_t k, int64_t pv, uint64_t prow, uint64_t e) {
+    const uint32_t r = srow1(e) - 1;
     if (kAgg == kAggCountXor) {
       a_cnt += 1;
       a_sum += (int64_t)r ^ (int64_t)prow;
     } else {
-      const int64_t bv = kWide ? (int64_t)e.pay : (bpay ? (int64_t)__ldg(&bpay[r]) : 0);
+      const int64_t bv = bpay ? (int64_t)__ldg(&bpay[r]) : 0;
       if (kAgg == kAggCountProduct) {
         a_cnt += 1;
         a_sum += bv * pv;
       } else {
         acc.update(spec, k, bv, pv, r, prow);
       }
-    }
-  };
-  auto probe_one = [&](int32_t k, int64_t pv, uint64_t prow, uint64_t h, SlotView e) {
-    for (uint64_t step = 0; step <= mask; ++step) {
-      if (e.row1 == 0) break;
-      if (e.key == k) {
-        match(k, pv, prow, e);
-        if (unique) break;
-      }
-      h = (h + 1) & mask;
-      e = slot_at<kWide>(slots, h);
     }
   };
   uint64_t done = 0;
@@ -145,23 +109,23 @@ __global__ void __launch_bounds__(kThreads)
       }
       const int32_t kk[8] = {ka.x, ka.y, ka.z, ka.w, kb.x, kb.y, kb.z, kb.w};
       const int32_t pp[8] = {pa.x, pa.y, pa.z, pa.w, pb.x, pb.y, pb.z, pb.w};
-      // slot indices fit 32 bits: tables hold at most 2^32 slots
+      // slot indices fit 32 bits: the table holds at most 2^21 slots
       const uint32_t m32 = (uint32_t)mask;
       uint32_t h[8];
-      SlotView e[8];
+      uint64_t e[8];
 #pragma unroll
       for (int j = 0; j < 8; ++j) {
         h[j] = gbjd::fmix32((uint32_t)kk[j]) & m32;
-        e[j] = slot_at<kWide>(slots, h[j]);
+        e[j] = __ldg(slots + h[j]);
       }
       uint32_t open = 0xffu;  // probes whose chain is not finished
       for (uint64_t step = 0; open && step <= mask; ++step) {
 #pragma unroll
         for (int j = 0; j < 8; ++j) {
           if (open >> j & 1u) {
-            if (e[j].row1 == 0) {
+            if (srow1(e[j]) == 0) {
               open &= ~(1u << j);
-            } else if (e[j].key == kk[j]) {
+            } else if (skey(e[j]) == kk[j]) {
               match(kk[j], pp[j], q * 8 + j, e[j]);
               if (unique) open &= ~(1u << j);
             }
@@ -171,7 +135,7 @@ __global__ void __launch_bounds__(kThreads)
         for (int j = 0; j < 8; ++j) {
           if (open >> j & 1u) {
             h[j] = (h[j] + 1) & m32;
-            e[j] = slot_at<kWide>(slots, h[j]);
+            e[j] = __ldg(slots + h[j]);
           }
         }
       }
@@ -181,8 +145,17 @@ __global__ void __launch_bounds__(kThreads)
   // rows the vector loop did not cover (all of them without kVec)
   for (uint64_t i = done + blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += stride) {
     const int32_t k = keys[i];
-    const uint64_t h = gbjd::fmix32((uint32_t)k) & mask;
-    probe_one(k, pay ? pay[i] : 0, i, h, slot_at<kWide>(slots, h));
+    const int64_t pv = pay ? pay[i] : 0;
+    uint64_t h = gbjd::fmix32((uint32_t)k) & mask;
+    for (uint64_t step = 0; step <= mask; ++step) {
+      const uint64_t e = __ldg(slots + h);
+      if (srow1(e) == 0) break;
+      if (skey(e) == k) {
+        match(k, pv, i, e);
+        if (unique) break;
+      }
+      h = (h + 1) & mask;
+    }
   }
   if (kAgg != kAggGeneric) {
     acc.v[0] = a_cnt;
@@ -191,40 +164,293 @@ __global__ void __launch_bounds__(kThreads)
   gbjd::block_flush(spec, acc, red, out);
 }
 
-// Probe emitting (build row, probe row) pairs through warp-aggregated
-// reservations of the output cursor.
-template <bool kWide>
+// ------------------------------------------------ bucketed join table
+// The table gbj_join_build makes: buckets of four slots, 32 bytes each --
+// four keys then four values (the build payload, or row + 1 when the build
+// side has none) -- so a probe reads one L2 sector per bucket and finds the
+// key and its payload without a second, dependent load.  Keys are stored
+// xor INT32_MIN, so the all-zero word of a cleared table marks an empty
+// slot; build rows whose key is INT32_MIN (stored word 0) go to a side list
+// instead.  A table with a payload keeps row + 1 of every slot in a
+// parallel array of 16-byte bucket rows, read only when an aggregate or the
+// pair output needs the build row.  A key sits in its home bucket (fmix32
+// bits) or, when that bucket was full at insert time, in a later one; a
+// probe stops at the first bucket with an empty slot.
+// Probe shape: kJbGroup probes per thread at a time (a multiple of 4), and
+// the CTAs per SM the specialised probe kernels are compiled for (512
+// threads each).  Measured on GB300 for the plain join (2^20 build rows,
+// 2^24 probes): 4 probes x 2 CTAs ahead of 8 x 2 (register spills), 8 x 1
+// and 4 x 3.
+#ifndef GBJ_JB_MIN_BLOCKS
+#define GBJ_JB_MIN_BLOCKS 2
+#endif
+#ifndef GBJ_JB_GROUP
+#define GBJ_JB_GROUP 4
+#endif
+constexpr int kJbGroup = GBJ_JB_GROUP;
+struct __align__(32) JBucket {
+  int4 k;  // key ^ INT32_MIN, 0 = empty
+  int4 x;  // payload, or row + 1
+};
+
+// One bucket in a single 256-bit load (ld.global.nc.v8, sm_100 and later):
+// one L2 request per bucket instead of two.
+__device__ __forceinline__ JBucket ld_bucket(const JBucket *p) {
+  JBucket r;
+  asm("ld.global.nc.v8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+      : "=r"(r.k.x), "=r"(r.k.y), "=r"(r.k.z), "=r"(r.k.w), "=r"(r.x.x), "=r"(r.x.y), "=r"(r.x.z), "=r"(r.x.w)
+      : "l"(p));
+  return r;
+}
+constexpr int32_t kKeyFlip = INT32_MIN;
+
+__device__ __forceinline__ int32_t lane4(const int4 &v, uint32_t i) {
+  return i == 0 ? v.x : i == 1 ? v.y : i == 2 ? v.z : v.w;
+}
+__device__ __forceinline__ uint32_t hits4(const int4 &k, int32_t kf) {
+  return (uint32_t)(k.x == kf) | ((uint32_t)(k.y == kf) << 1) | ((uint32_t)(k.z == kf) << 2) |
+         ((uint32_t)(k.w == kf) << 3);
+}
+__device__ __forceinline__ bool room4(const int4 &k) { return (k.x == 0) | (k.y == 0) | (k.z == 0) | (k.w == 0); }
+
+// meta[0]: a duplicate build key was seen; meta[1]: side-list length.  A
+// row claims the first free slot of its home bucket, starting at a slot
+// chosen by the top hash bits, then of the following buckets.
 __global__ void __launch_bounds__(kThreads)
-    k_join_probe_pairs(const int32_t *__restrict__ keys,
-                       const int32_t *__restrict__ prows, uint64_t n,
-                       const void *__restrict__ slots, uint64_t mask,
-                       const uint32_t *__restrict__ meta,
-                       int32_t *__restrict__ out_b, int32_t *__restrict__ out_p,
-                       uint64_t cap, unsigned long long *count,
-                       uint32_t *status) {
-  const bool unique = meta[0] == 0;
+    k_jb_build(const int32_t *__restrict__ keys, const int32_t *__restrict__ payload, uint64_t n,
+               JBucket *__restrict__ bk, int4 *__restrict__ rows, uint32_t bmask, uint32_t *__restrict__ meta,
+               int32_t *__restrict__ side, uint32_t *status) {
   const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  bool dup = false;
+  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += stride) {
+    const int32_t key = keys[i];
+    const int32_t pv = payload ? payload[i] : (int32_t)(i + 1);
+    const int32_t kf = key ^ kKeyFlip;
+    if (kf == 0) {  // INT32_MIN: the side list
+      side[atomicAdd(&meta[1], 1u)] = (int32_t)i;
+      continue;
+    }
+    const uint32_t h = gbjd::fmix32((uint32_t)key);
+    uint32_t b = h & bmask;
+    const uint32_t o = h >> 30;  // start slot (high bits, independent of the bucket for 2^30 buckets or fewer)
+    bool placed = false;
+    for (uint32_t step = 0; step <= bmask && !placed; ++step) {
+      int32_t *kw = reinterpret_cast<int32_t *>(&bk[b].k);
+#pragma unroll
+      for (uint32_t j = 0; j < 4; ++j) {
+        if (placed) break;
+        const uint32_t sl = (o + j) & 3u;
+        const int32_t old = atomicCAS(&kw[sl], 0, kf);
+        if (old == 0) {
+          reinterpret_cast<int32_t *>(&bk[b].x)[sl] = pv;
+          if (rows) reinterpret_cast<int32_t *>(&rows[b])[sl] = (int32_t)(i + 1);
+          placed = true;
+        } else {
+          dup |= old == kf;
+        }
+      }
+      b = (b + 1) & bmask;
+    }
+    if (!placed) gbjd::latch(status, GBJ_DEV_CAPACITY);
+  }
+  if (dup) meta[0] = 1;
+}
+
+// Probe with fused aggregate over the bucketed table.  A probe visits its
+// home bucket and folds every slot whose key matches into the aggregate
+// without branching (a count of the matches and, for the specialised
+// aggregate lists, a select-and-sum of their values); it moves on to the
+// next bucket only when the bucket is full and either has no match or the
+// build keys are not unique -- the rare case, taken out of line.  Each
+// thread handles kJbGroup probes at a time: their bucket loads (one 256-bit
+// load each) are issued together, and the next group's probe keys and
+// payloads are loaded while they are in flight.  kPay: the values are build
+// payloads and build rows come from the row array.
+template <bool kVec, int kAgg, bool kPay>
+__global__ void __launch_bounds__(kThreads, kAgg == kAggGeneric ? 1 : GBJ_JB_MIN_BLOCKS)
+    k_jb_probe_agg(const int32_t *__restrict__ keys, const int32_t *__restrict__ pay, uint64_t n,
+                   const JBucket *__restrict__ bk, const int4 *__restrict__ rows, uint32_t bmask,
+                   const int32_t *__restrict__ bpay, const uint32_t *__restrict__ meta,
+                   const int32_t *__restrict__ side, gbj::AggSpec spec, int64_t *out) {
+  __shared__ int64_t red[32 * GBJ_MAX_AGGS];
+  gbjd::Acc acc;  // the specialised accumulators fill it only at the end
+  if (kAgg == kAggGeneric) acc.init(spec);
+  int64_t a_cnt = 0, a_sum = 0;
+  const bool unique = meta[0] == 0;
+  const uint32_t nside = meta[1];
+  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  // does the generic aggregate list read build rows? (payload tables keep them apart)
+  bool need_row = !kPay;
+  if (kPay && kAgg == kAggGeneric)
+    for (int j = 0; j < spec.n; ++j)
+      need_row |= spec.operand[j] == GBJ_VAL_BUILD_ROWID || spec.operand[j] == GBJ_VAL_ROWID_XOR;
+  // folds the matching slots of bucket b (contents e) into the aggregate;
+  // returns the number of matches
+  auto visit = [&](int32_t k, int32_t kf, int64_t pv, uint64_t prow, uint32_t b, const JBucket &e) -> uint32_t {
+    const bool m0 = e.k.x == kf, m1 = e.k.y == kf, m2 = e.k.z == kf, m3 = e.k.w == kf;
+    const uint32_t c = (uint32_t)m0 + (uint32_t)m1 + (uint32_t)m2 + (uint32_t)m3;
+    if (kAgg == kAggCountProduct) {
+      a_cnt += c;
+      if (kPay)
+        a_sum += ((int64_t)(m0 ? e.x.x : 0) + (m1 ? e.x.y : 0) + (int64_t)(m2 ? e.x.z : 0) + (m3 ? e.x.w : 0)) * pv;
+    } else if (kAgg == kAggCountXor && !kPay) {
+      a_cnt += c;
+      const int64_t pr = (int64_t)prow;
+      a_sum += (m0 ? ((int64_t)(e.x.x - 1) ^ pr) : 0) + (m1 ? ((int64_t)(e.x.y - 1) ^ pr) : 0) +
+               (m2 ? ((int64_t)(e.x.z - 1) ^ pr) : 0) + (m3 ? ((int64_t)(e.x.w - 1) ^ pr) : 0);
+    } else if (c) {
+      const bool rows_needed = kAgg == kAggCountXor || need_row;
+      const int4 rw = kPay && rows_needed ? __ldg(&rows[b]) : e.x;
+      uint32_t hits = (uint32_t)m0 | ((uint32_t)m1 << 1) | ((uint32_t)m2 << 2) | ((uint32_t)m3 << 3);
+      while (hits) {
+        const uint32_t idx = __ffs(hits) - 1;
+        const int64_t bv = kPay ? lane4(e.x, idx) : 0;
+        const int64_t brow = (kPay && !rows_needed) ? 0 : lane4(rw, idx) - 1;
+        if (kAgg == kAggCountXor) {
+          a_cnt += 1;
+          a_sum += brow ^ (int64_t)prow;
+        } else {
+          acc.update(spec, k, bv, pv, brow, prow);
+        }
+        hits &= hits - 1;
+      }
+    }
+    return c;
+  };
+  // the buckets after a full home bucket (out of line, rare)
+  auto walk = [&](int32_t k, int32_t kf, int64_t pv, uint64_t prow, uint32_t b, uint32_t matched) {
+    for (uint32_t step = 1; step <= bmask; ++step) {
+      b = (b + 1) & bmask;
+      const JBucket e = ld_bucket(&bk[b]);
+      matched += visit(k, kf, pv, prow, b, e);
+      if (room4(e.k) || (unique && matched)) return;
+    }
+  };
+  // a probe key INT32_MIN meets the side list
+  auto side_probe = [&](int32_t k, int64_t pv, uint64_t prow) {
+    for (uint32_t s = 0; s < nside; ++s) {
+      const int32_t r = side[s];
+      const int64_t bv = kPay ? (int64_t)bpay[r] : 0;
+      if (kAgg == kAggCountProduct) {
+        a_cnt += 1;
+        a_sum += bv * pv;
+      } else if (kAgg == kAggCountXor) {
+        a_cnt += 1;
+        a_sum += (int64_t)r ^ (int64_t)prow;
+      } else {
+        acc.update(spec, k, bv, pv, r, prow);
+      }
+      if (unique) break;
+    }
+  };
+  auto finish = [&](int32_t k, int64_t pv, uint64_t prow, uint32_t b, const JBucket &e) {
+    const int32_t kf = k ^ kKeyFlip;
+    if (kf == 0) {
+      side_probe(k, pv, prow);
+      return;
+    }
+    const uint32_t c = visit(k, kf, pv, prow, b, e);
+    if (!room4(e.k) && !(unique && c)) walk(k, kf, pv, prow, b, c);
+  };
+  uint64_t done = 0;
+  if (kVec) {
+    constexpr int G = kJbGroup;  // probes per thread at a time (a multiple of 4)
+    const uint64_t ng = n / G;
+    const int4 *k4 = reinterpret_cast<const int4 *>(keys);
+    const int4 *p4 = reinterpret_cast<const int4 *>(pay);
+    int4 nk[G / 4], np[G / 4];
+    auto load_group = [&](uint64_t qq) {
+#pragma unroll
+      for (int v = 0; v < G / 4; ++v) {
+        nk[v] = __ldcs(k4 + (G / 4) * qq + v);
+        np[v] = pay ? __ldcs(p4 + (G / 4) * qq + v) : make_int4(0, 0, 0, 0);
+      }
+    };
+    uint64_t q = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+    if (q < ng) load_group(q);
+    for (; q < ng; q += stride) {
+      int32_t kk[G], pp[G];
+#pragma unroll
+      for (int v = 0; v < G / 4; ++v) {
+        kk[4 * v] = nk[v].x, kk[4 * v + 1] = nk[v].y, kk[4 * v + 2] = nk[v].z, kk[4 * v + 3] = nk[v].w;
+        pp[4 * v] = np[v].x, pp[4 * v + 1] = np[v].y, pp[4 * v + 2] = np[v].z, pp[4 * v + 3] = np[v].w;
+      }
+      uint32_t b[G];
+      JBucket e[G];
+#pragma unroll
+      for (int j = 0; j < G; ++j) {
+        b[j] = gbjd::fmix32((uint32_t)kk[j]) & bmask;
+        e[j] = ld_bucket(&bk[b[j]]);
+      }
+      if (q + stride < ng) load_group(q + stride);
+#pragma unroll
+      for (int j = 0; j < G; ++j) finish(kk[j], pp[j], q * G + j, b[j], e[j]);
+    }
+    done = ng * G;
+  }
+  for (uint64_t i = done + blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += stride) {
+    const int32_t k = keys[i];
+    const uint32_t b = gbjd::fmix32((uint32_t)k) & bmask;
+    finish(k, pay ? pay[i] : 0, i, b, ld_bucket(&bk[b]));
+  }
+  if (kAgg != kAggGeneric) {
+    acc.init(spec);
+    acc.v[0] = a_cnt;
+    acc.v[1] = a_sum;
+  }
+  gbjd::block_flush(spec, acc, red, out);
+}
+
+// Pair output over the bucketed table (warp-aggregated output reservations).
+template <bool kPay>
+__global__ void __launch_bounds__(kThreads)
+    k_jb_probe_pairs(const int32_t *__restrict__ keys, const int32_t *__restrict__ prows, uint64_t n,
+                     const JBucket *__restrict__ bk, const int4 *__restrict__ rows, uint32_t bmask,
+                     const uint32_t *__restrict__ meta, const int32_t *__restrict__ side,
+                     int32_t *__restrict__ out_b, int32_t *__restrict__ out_p, uint64_t cap,
+                     unsigned long long *count, uint32_t *status) {
+  const bool unique = meta[0] == 0;
+  const uint32_t nside = meta[1];
+  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  auto emit = [&](int32_t br, int32_t pr) {
+    cg::coalesced_group g = cg::coalesced_threads();
+    unsigned long long base = 0;
+    if (g.thread_rank() == 0) base = atomicAdd(count, (unsigned long long)g.size());
+    base = g.shfl(base, 0) + g.thread_rank();
+    if (base < cap) {
+      out_b[base] = br;
+      out_p[base] = pr;
+    } else {
+      gbjd::latch(status, GBJ_DEV_CAPACITY);
+    }
+  };
   for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += stride) {
     const int32_t k = keys[i];
     const int32_t pr = prows ? prows[i] : (int32_t)i;
-    uint64_t h = gbjd::fmix32((uint32_t)k) & mask;
-    for (uint64_t step = 0; step <= mask; ++step) {
-      const SlotView e = slot_at<kWide>(slots, h);
-      if (e.row1 == 0) break;
-      if (e.key == k) {
-        cg::coalesced_group g = cg::coalesced_threads();
-        unsigned long long base = 0;
-        if (g.thread_rank() == 0) base = atomicAdd(count, (unsigned long long)g.size());
-        base = g.shfl(base, 0) + g.thread_rank();
-        if (base < cap) {
-          out_b[base] = (int32_t)(e.row1 - 1);
-          out_p[base] = pr;
-        } else {
-          gbjd::latch(status, GBJ_DEV_CAPACITY);
-        }
+    const int32_t kf = k ^ kKeyFlip;
+    if (kf == 0) {
+      for (uint32_t s = 0; s < nside; ++s) {
+        emit(side[s], pr);
         if (unique) break;
       }
-      h = (h + 1) & mask;
+      continue;
+    }
+    uint32_t b = gbjd::fmix32((uint32_t)k) & bmask;
+    for (uint32_t step = 0; step <= bmask; ++step) {
+      const JBucket e = ld_bucket(&bk[b]);
+      uint32_t hits = hits4(e.k, kf);
+      bool stop = room4(e.k);
+      while (hits) {
+        const uint32_t idx = __ffs(hits) - 1;
+        emit(lane4(kPay ? __ldg(&rows[b]) : e.x, idx) - 1, pr);
+        if (unique) {
+          stop = true;
+          break;
+        }
+        hits &= hits - 1;
+      }
+      if (stop) break;
+      b = (b + 1) & bmask;
     }
   }
 }
@@ -275,13 +501,12 @@ int grid_for(gbj_ctx *ctx, uint64_t work, int threads, int per_sm = 4) {
   return grid_for_sms(ctx->sm_count, work, threads, per_sm);
 }
 
-// Picks the probe kernel: 16-byte loads when both probe columns are
-// 16-byte aligned, a specialised accumulator for COUNT + SUM(product / xor),
-// and the slot layout of the table.
-template <bool kWide>
-void launch_probe_t(int sm_count, const int32_t *keys, const int32_t *pay, uint64_t n, const void *slots,
-                    uint64_t mask, const int32_t *bpay, const uint32_t *meta, const gbj::AggSpec &spec,
-                    int64_t *out, cudaStream_t s) {
+// Probe kernel of the allocation-free entry point: 16-byte loads when both
+// probe columns are 16-byte aligned, a specialised accumulator for COUNT +
+// SUM(product / xor).
+void launch_probe(int sm_count, const int32_t *keys, const int32_t *pay, uint64_t n, const uint64_t *slots,
+                  uint64_t mask, const int32_t *bpay, const uint32_t *meta, const gbj::AggSpec &spec,
+                  int64_t *out, cudaStream_t s) {
   const bool vec = ((uintptr_t)keys % 16 == 0) && (!pay || (uintptr_t)pay % 16 == 0);
   const bool two = spec.n == 2 && spec.op[0] == GBJ_AGG_COUNT && spec.op[1] == GBJ_AGG_SUM;
   const int agg = two && spec.operand[1] == GBJ_VAL_ROWID_XOR ? kAggCountXor
@@ -289,9 +514,8 @@ void launch_probe_t(int sm_count, const int32_t *keys, const int32_t *pay, uint6
                                                               : kAggGeneric;
   const int gv = grid_for_sms(sm_count, (n + 7) / 8, kThreads);
   const int gs = grid_for_sms(sm_count, n, kThreads);
-#define GBJ_PROBE(V, A)                                                                                  \
-  k_join_probe_agg<V, A, kWide><<<V ? gv : gs, kThreads, 0, s>>>(keys, pay, n, slots, mask, bpay, meta, \
-                                                                 spec, out)
+#define GBJ_PROBE(V, A) \
+  k_join_probe_agg<V, A><<<V ? gv : gs, kThreads, 0, s>>>(keys, pay, n, slots, mask, bpay, meta, spec, out)
   if (vec) {
     if (agg == kAggCountXor) GBJ_PROBE(true, kAggCountXor);
     else if (agg == kAggCountProduct) GBJ_PROBE(true, kAggCountProduct);
@@ -304,11 +528,39 @@ void launch_probe_t(int sm_count, const int32_t *keys, const int32_t *pay, uint6
 #undef GBJ_PROBE
 }
 
-void launch_probe(int sm_count, bool wide, const int32_t *keys, const int32_t *pay, uint64_t n, const void *slots,
-                  uint64_t mask, const int32_t *bpay, const uint32_t *meta, const gbj::AggSpec &spec,
-                  int64_t *out, cudaStream_t s) {
-  if (wide) launch_probe_t<true>(sm_count, keys, pay, n, slots, mask, bpay, meta, spec, out, s);
-  else launch_probe_t<false>(sm_count, keys, pay, n, slots, mask, bpay, meta, spec, out, s);
+// Probe kernel over a bucketed table: 16-byte probe loads when both probe
+// columns are aligned, the specialised accumulators, the table's layout.
+template <bool kPay>
+void launch_jb_probe_t(int sm_count, const gbj_table *t, const int32_t *keys, const int32_t *pay, uint64_t n,
+                       const gbj::AggSpec &spec, int64_t *out, cudaStream_t s) {
+  const bool vec = ((uintptr_t)keys % 16 == 0) && (!pay || (uintptr_t)pay % 16 == 0);
+  const bool two = spec.n == 2 && spec.op[0] == GBJ_AGG_COUNT && spec.op[1] == GBJ_AGG_SUM;
+  const int agg = two && spec.operand[1] == GBJ_VAL_ROWID_XOR ? kAggCountXor
+                  : two && spec.operand[1] == GBJ_VAL_PRODUCT ? kAggCountProduct
+                                                              : kAggGeneric;
+  const JBucket *bk = static_cast<const JBucket *>(t->slots);
+  const uint32_t bmask = (uint32_t)((t->mask + 1) / 4 - 1);
+  const int gv = grid_for_sms(sm_count, (n + kJbGroup - 1) / kJbGroup, kThreads, 2);
+  const int gs = grid_for_sms(sm_count, n, kThreads);
+#define GBJ_JB_PROBE(V, A)                                                                               \
+  k_jb_probe_agg<V, A, kPay><<<V ? gv : gs, kThreads, 0, s>>>(keys, pay, n, bk, t->rows, bmask, t->payload, \
+                                                              t->meta, t->side, spec, out)
+  if (vec) {
+    if (agg == kAggCountXor) GBJ_JB_PROBE(true, kAggCountXor);
+    else if (agg == kAggCountProduct) GBJ_JB_PROBE(true, kAggCountProduct);
+    else GBJ_JB_PROBE(true, kAggGeneric);
+  } else {
+    if (agg == kAggCountXor) GBJ_JB_PROBE(false, kAggCountXor);
+    else if (agg == kAggCountProduct) GBJ_JB_PROBE(false, kAggCountProduct);
+    else GBJ_JB_PROBE(false, kAggGeneric);
+  }
+#undef GBJ_JB_PROBE
+}
+
+void launch_jb_probe(int sm_count, const gbj_table *t, const int32_t *keys, const int32_t *pay, uint64_t n,
+                     const gbj::AggSpec &spec, int64_t *out, cudaStream_t s) {
+  if (t->rows) launch_jb_probe_t<true>(sm_count, t, keys, pay, n, spec, out, s);
+  else launch_jb_probe_t<false>(sm_count, t, keys, pay, n, spec, out, s);
 }
 
 // ------------------------------------------------ allocation-free variant
@@ -370,12 +622,6 @@ int noalloc_fail(int code, const char *msg) {
   return code;
 }
 
-// The metadata word after a table's slots.
-const uint32_t *table_meta(const gbj_table *t) {
-  return reinterpret_cast<const uint32_t *>(static_cast<const char *>(t->slots) +
-                                            (t->mask + 1) * (t->wide ? 16 : 8));
-}
-
 }  // namespace
 
 namespace gbj {
@@ -405,36 +651,39 @@ int gbj_join_build(gbj_ctx *ctx, const int32_t *d_keys,
   }
   if (hash_bits && (1ULL << hash_bits) > slots) slots = 1ULL << hash_bits;
   if (slots < 64) slots = 64;
+  if (slots > (1ULL << 32)) return set_error(ctx, GBJ_ERR_INVALID, "join_build: table above 2^32 slots");
+  const uint64_t nbk = slots / 4;
+  const bool with_pay = d_payload != nullptr;
+  // buckets | rows (payload tables) | metadata | INT32_MIN side list
+  const uint64_t b_bytes = nbk * sizeof(JBucket), r_bytes = with_pay ? nbk * sizeof(int4) : 0;
+  const uint64_t clear_bytes = b_bytes + r_bytes + 256;
   gbj_table *t = new gbj_table();
   void *mem = nullptr;
-  // a build side with a payload gets 16-byte slots that carry it
-  const bool wide = d_payload != nullptr;
-  const uint64_t slot_bytes = wide ? 16 : 8;
-  int rc = pool_alloc(ctx, slots * slot_bytes + 256, s, &mem);
+  int rc = pool_alloc(ctx, clear_bytes + (n + 4) * sizeof(int32_t), s, &mem);
   if (rc) {
     delete t;
     return rc;
   }
+  char *base = static_cast<char *>(mem);
   t->slots = mem;
-  t->wide = wide;
+  t->rows = with_pay ? reinterpret_cast<int4 *>(base + b_bytes) : nullptr;
+  t->meta = reinterpret_cast<uint32_t *>(base + b_bytes + r_bytes);
+  t->side = reinterpret_cast<int32_t *>(base + clear_bytes);
   t->mask = slots - 1;
   t->keys = d_keys;
   t->payload = d_payload;
   t->n = n;
-  uint32_t *meta = (uint32_t *)((char *)mem + slots * slot_bytes);
-  cudaError_t e = cudaMemsetAsync(mem, 0, slots * slot_bytes + 256, s);
+  cudaError_t e = cudaMemsetAsync(mem, 0, clear_bytes, s);
   if (e != cudaSuccess) {
     pool_release(ctx, mem, s);
     delete t;
     return cuda_error(ctx, e, "cudaMemsetAsync(table)");
   }
   if (n) {
-    if (wide)
-      k_join_build<true><<<grid_for(ctx, n, kThreads), kThreads, 0, s>>>(d_keys, d_payload, n, t->slots,
-                                                                       t->mask, meta, ctx->d_status);
-    else
-      k_join_build<false><<<grid_for(ctx, n, kThreads), kThreads, 0, s>>>(d_keys, nullptr, n, t->slots,
-                                                                        t->mask, meta, ctx->d_status);
+    k_jb_build<<<grid_for(ctx, n, kThreads), kThreads, 0, s>>>(d_keys, d_payload, n,
+                                                                reinterpret_cast<JBucket *>(mem), t->rows,
+                                                                (uint32_t)(nbk - 1), t->meta, t->side,
+                                                                ctx->d_status);
     rc = after_launch(ctx, "k_join_build", s);
     if (rc) {
       pool_release(ctx, mem, s);
@@ -473,9 +722,7 @@ int gbj_join_probe_agg(gbj_ctx *ctx, const gbj_table *t, const int32_t *d_keys,
   prof_mark(ctx, s);
   GBJ_TRY(init_agg_out(ctx, spec, d_out, s));
   if (n == 0) return GBJ_OK;
-  const uint32_t *meta = table_meta(t);
-  launch_probe(ctx->sm_count, t->wide, d_keys, d_payload, n, t->slots, t->mask, t->payload, meta, spec,
-               d_out, s);
+  launch_jb_probe(ctx->sm_count, t, d_keys, d_payload, n, spec, d_out, s);
   return after_launch(ctx, "k_join_probe_agg", s);
 }
 
@@ -490,14 +737,15 @@ int gbj_join_probe_pairs(gbj_ctx *ctx, const gbj_table *t, const int32_t *d_keys
   prof_mark(ctx, s);
   GBJ_CHECK_CUDA(ctx, cudaMemsetAsync(d_count, 0, sizeof(uint64_t), s));
   if (n == 0) return GBJ_OK;
-  const uint32_t *meta = table_meta(t);
-  if (t->wide)
-    k_join_probe_pairs<true><<<grid_for(ctx, n, kThreads), kThreads, 0, s>>>(
-        d_keys, d_probe_rows, n, t->slots, t->mask, meta, d_build_rows, d_out_probe_rows, capacity,
+  const JBucket *bk = static_cast<const JBucket *>(t->slots);
+  const uint32_t bmask = (uint32_t)((t->mask + 1) / 4 - 1);
+  if (t->rows)
+    k_jb_probe_pairs<true><<<grid_for(ctx, n, kThreads), kThreads, 0, s>>>(
+        d_keys, d_probe_rows, n, bk, t->rows, bmask, t->meta, t->side, d_build_rows, d_out_probe_rows, capacity,
         (unsigned long long *)d_count, ctx->d_status);
   else
-    k_join_probe_pairs<false><<<grid_for(ctx, n, kThreads), kThreads, 0, s>>>(
-        d_keys, d_probe_rows, n, t->slots, t->mask, meta, d_build_rows, d_out_probe_rows, capacity,
+    k_jb_probe_pairs<false><<<grid_for(ctx, n, kThreads), kThreads, 0, s>>>(
+        d_keys, d_probe_rows, n, bk, nullptr, bmask, t->meta, t->side, d_build_rows, d_out_probe_rows, capacity,
         (unsigned long long *)d_count, ctx->d_status);
   return after_launch(ctx, "k_join_probe_pairs", s);
 }
@@ -610,10 +858,10 @@ int gbj_join_agg_noalloc(const int32_t *d_build_keys, const int32_t *d_build_pay
   }
   k_noalloc_init_out<<<1, 32, 0, s>>>(spec, d_out);
   if (n_build)
-    k_join_build<false><<<grid_for_sms(d.sm_count, n_build, kThreads), kThreads, 0, s>>>(
-        d_build_keys, nullptr, n_build, table, slots - 1, meta, nullptr);
+    k_join_build<<<grid_for_sms(d.sm_count, n_build, kThreads), kThreads, 0, s>>>(d_build_keys, n_build, table,
+                                                                                   slots - 1, meta);
   if (n_probe)
-    launch_probe(d.sm_count, false, d_probe_keys, d_probe_payload, n_probe, table, slots - 1,
+    launch_probe(d.sm_count, d_probe_keys, d_probe_payload, n_probe, table, slots - 1,
                  d_build_payload, meta, spec, d_out, s);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return noalloc_fail(GBJ_ERR_CUDA, cudaGetErrorString(e));
