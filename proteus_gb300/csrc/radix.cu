@@ -38,6 +38,7 @@
 #include "gbj_internal.cuh"
 #include "radix.cuh"
 #include "scan.cuh"
+#include "tma.cuh"
 
 using namespace gbj;
 
@@ -49,6 +50,15 @@ constexpr int kTilePer = kTile / kTileThreads;  // tuples per thread
 constexpr int kTileCtas = 2;                    // CTAs per SM (register budget)
 constexpr int kTileWarps = kTileThreads / 32;
 constexpr int kMaxDigits = 256;      // <= 8 digit bits per pass
+#ifndef GBJ_TILE_TMA
+#define GBJ_TILE_TMA 0
+#endif
+// Tile passes load through bulk copies when set.  Measured on GB300 (radix
+// join, R 2^27, S 2^29, 14 bits): 77.3 ms of tile passes per 60 launches with
+// bulk copies against 70.0 ms through registers -- the copies add a shared
+// read of every tuple to a kernel bound by its shared-memory pipe, and the
+// pair passes have only one 32 KB stage -- so registers are the default.
+constexpr bool kTileTma = GBJ_TILE_TMA;
 constexpr int32_t kEmpty = INT32_MIN;
 
 // Digit functions: of the key itself (GBJ_DIGIT_KEY), of fmix32(key)
@@ -123,15 +133,27 @@ struct TileSmem {
 // replaced by fmix32(key) as they are loaded (the tuples then carry the
 // hash and kDigit is kDigitPre).  Row positions are below 2^31, so tile
 // arithmetic is 32-bit.
-template <int kDigit, bool kPairsIn, bool kAoSOut, bool kHashLoad>
+//
+// kTma: the input tiles arrive by bulk copies (cp.async.bulk) into a 32 KB
+// shared-memory ring behind TileSmem -- two 16 KB stages (key columns
+// without values: two tiles ahead) or one 32 KB stage (pairs, or keys and
+// values: one tile ahead) -- instead of through registers.  A copy covers
+// the 16-byte aligned middle of the tile; the (at most three) tuples either
+// side of it are loaded directly.  Input columns must be 16-byte aligned.
+constexpr uint32_t kRingBytes = kTile * 8;
+template <int kDigit, bool kPairsIn, bool kAoSOut, bool kHashLoad, bool kTma>
 __global__ void __launch_bounds__(kTileThreads, kTileCtas)
     k_tile_pass(const int32_t *__restrict__ keys, const int32_t *__restrict__ vals,
                 const int2 *__restrict__ pin, uint32_t n, int dshift, uint32_t dmask,
                 const uint64_t *__restrict__ bucket_off, const uint64_t *__restrict__ tile_off,
                 uint32_t nb, uint32_t *__restrict__ cursor, int2 *__restrict__ out_pairs,
-                int32_t *__restrict__ out_k, int32_t *__restrict__ out_v) {
+                int32_t *__restrict__ out_k, int32_t *__restrict__ out_v, uint32_t *status) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   TileSmem &S = *reinterpret_cast<TileSmem *>(smem_raw);
+  unsigned char *ring = smem_raw + sizeof(TileSmem);
+  uint64_t *bars = reinterpret_cast<uint64_t *>(ring + kRingBytes);
+  const uint32_t stage_bytes = (kPairsIn || vals) ? kRingBytes : kRingBytes / 2;
+  const uint32_t nst = kRingBytes / stage_bytes;  // stages: 1 or 2
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const uint32_t ndig = dmask + 1;
   const uint32_t ntiles = kPairsIn ? (uint32_t)tile_off[nb] : (n + kTile - 1) / kTile;
@@ -170,16 +192,93 @@ __global__ void __launch_bounds__(kTileThreads, kTileCtas)
       }
     }
   };
+  // kTma: the bulk-copied range [a, e) of the tile [lo, hi)
+  auto tma_range = [&](uint32_t l, uint32_t h, uint32_t &a, uint32_t &e) {
+    if (kPairsIn) {  // 8-byte tuples: even positions are 16-byte aligned
+      a = (l + 1) & ~1u;
+      e = h & ~1u;
+    } else {  // 4-byte columns: tiles start at multiples of kTile
+      a = l;
+      e = l + ((h - l) & ~3u);
+    }
+    if (e < a) e = a;
+  };
+  auto issue = [&](uint32_t tt, uint32_t st) {
+    uint32_t l, h, bb, a, e;
+    tile_range(tt, l, h, bb);
+    tma_range(l, h, a, e);
+    unsigned char *dst = ring + st * stage_bytes;
+    const uint32_t cols = kPairsIn ? 2 : (vals ? 2 : 1);
+    gbjd::mbar_arrive_expect_tx(&bars[st], (e - a) * 4 * cols);
+    if (e > a) {
+      if (kPairsIn) {
+        gbjd::bulk_load(dst, pin + a, (e - a) * 8, &bars[st]);
+      } else {
+        gbjd::bulk_load(dst, keys + a, (e - a) * 4, &bars[st]);
+        if (vals) gbjd::bulk_load(dst + kTile * 4, vals + a, (e - a) * 4, &bars[st]);
+      }
+    }
+  };
+  auto read_tile = [&](uint32_t l, uint32_t h, uint32_t st) {
+    uint32_t a, e;
+    tma_range(l, h, a, e);
+    const unsigned char *src = ring + st * stage_bytes;
+#pragma unroll
+    for (int j = 0; j < kTilePer; ++j) {
+      const uint32_t i = l + tid + j * kTileThreads;
+      if (i < h) {
+        if (i >= a && i < e) {
+          if (kPairsIn) {
+            tup[j] = reinterpret_cast<const int2 *>(src)[i - a];
+          } else {
+            tup[j].x = reinterpret_cast<const int32_t *>(src)[i - a];
+            tup[j].y = vals ? reinterpret_cast<const int32_t *>(src + kTile * 4)[i - a] : (int32_t)i;
+          }
+        } else if (kPairsIn) {
+          tup[j] = __ldcs(pin + i);
+        } else {
+          tup[j].x = __ldcs(keys + i);
+          tup[j].y = vals ? __ldcs(vals + i) : (int32_t)i;
+        }
+      }
+    }
+  };
   uint32_t t = blockIdx.x, lo = 0, hi = 0;
-  uint32_t b = 0;
-  if (t < ntiles) {
+  uint32_t b = 0, it = 0;
+  if (kTma) {
+    if (tid == 0) {
+      gbjd::mbar_init(&bars[0], 1);
+      gbjd::mbar_init(&bars[1], 1);
+      gbjd::mbar_init_fence();
+    }
+    __syncthreads();
+    if (tid == 0)
+      for (uint32_t k = 0; k < nst; ++k)
+        if (t + k * gridDim.x < ntiles) issue(t + k * gridDim.x, k);
+  } else if (t < ntiles) {
     tile_range(t, lo, hi, b);
     load_tile(lo, hi);
   }
   // Software pipeline: the next tile's loads are issued once this tile's
   // tuples sit in shared memory, so their DRAM latency overlaps the write
   // phase; the cursor atomic's L2 round trip overlaps the shared scatter.
-  for (; t < ntiles; t += gridDim.x) {
+  for (; t < ntiles; t += gridDim.x, ++it) {
+    if (kTma) {
+      tile_range(t, lo, hi, b);
+      const uint32_t st = it % nst;
+      const bool ok = gbjd::mbar_wait(&bars[st], (it / nst) & 1, kSpinLimit);
+      if (__syncthreads_or(!ok)) {
+        // a copy did not complete: report, wait (bounded) for the other
+        // stage's copy, and stop
+        if (tid == 0) {
+          gbjd::latch(status, GBJ_DEV_TIMEOUT);
+          if (nst == 2 && t + gridDim.x < ntiles)
+            gbjd::mbar_wait(&bars[(it + 1) % nst], ((it + 1) / nst) & 1, kSpinLimit);
+        }
+        return;
+      }
+      read_tile(lo, hi, st);
+    }
     for (uint32_t d = lane; d < ndig; d += 32) S.whist[warp][d] = 0;
     __syncwarp();
     const uint32_t cnt = hi - lo;
@@ -193,6 +292,8 @@ __global__ void __launch_bounds__(kTileThreads, kTileCtas)
       }
     }
     __syncthreads();
+    // kTma: every thread has read this stage; refill it two tiles ahead
+    if (kTma && tid == 0 && t + nst * gridDim.x < ntiles) issue(t + nst * gridDim.x, it % nst);
     // per digit: the tile total (the per-warp starts follow the digit scan)
     uint32_t tot = 0;
     if ((uint32_t)tid < ndig) {
@@ -240,7 +341,7 @@ __global__ void __launch_bounds__(kTileThreads, kTileCtas)
     // (modulo 2^32: gdelta + i is the output position)
     if ((uint32_t)tid < ndig) S.gdelta[tid] = gpos - my_start;
     const uint32_t tn = t + gridDim.x;
-    if (tn < ntiles) {
+    if (!kTma && tn < ntiles) {
       tile_range(tn, lo, hi, b);
       load_tile(lo, hi);
     }
@@ -679,8 +780,12 @@ int launch_tile_pass(gbj_ctx *ctx, const int32_t *keys, const int32_t *vals, con
                      uint64_t n, int dshift, uint32_t dmask, const uint64_t *bucket_off,
                      const uint64_t *tile_off, uint32_t nb, uint32_t *cursor, int2 *op, int32_t *ok,
                      int32_t *ov, cudaStream_t s) {
-  auto kern = k_tile_pass<kDigit, kPairsIn, kAoSOut, kHashLoad>;
-  const size_t smem = sizeof(TileSmem);
+  // bulk-copy loads when the input columns are 16-byte aligned
+  auto al16 = [](const void *p) { return (reinterpret_cast<uintptr_t>(p) & 15) == 0; };
+  const bool tma = kTileTma && (kPairsIn ? al16(pin) : (al16(keys) && (!vals || al16(vals))));
+  auto kern = tma ? k_tile_pass<kDigit, kPairsIn, kAoSOut, kHashLoad, true>
+                  : k_tile_pass<kDigit, kPairsIn, kAoSOut, kHashLoad, false>;
+  const size_t smem = sizeof(TileSmem) + (tma ? kRingBytes + 16 : 0);
   GBJ_CHECK_CUDA(ctx, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   int per_sm = 0;
   GBJ_CHECK_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kTileThreads, smem));
@@ -688,7 +793,7 @@ int launch_tile_pass(gbj_ctx *ctx, const int32_t *keys, const int32_t *vals, con
   const uint64_t tiles_hint = (n + kTile - 1) / kTile + nb;
   const uint64_t grid = std::max<uint64_t>(1, std::min<uint64_t>((uint64_t)ctx->sm_count * per_sm, tiles_hint));
   kern<<<(unsigned)grid, kTileThreads, smem, s>>>(keys, vals, pin, (uint32_t)n, dshift, dmask, bucket_off,
-                                                  tile_off, nb, cursor, op, ok, ov);
+                                                  tile_off, nb, cursor, op, ok, ov, ctx->d_status);
   return after_launch(ctx, "k_tile_pass", s);
 }
 
