@@ -164,6 +164,25 @@ int gbj_join_probe_pairs(gbj_ctx *ctx, const gbj_table *table,
                          int32_t *d_out_probe_rows, uint64_t capacity,
                          uint64_t *d_count, void *stream);
 
+/* The same three calls over int64 keys: HashJoinChained with an int64 join
+ * key, placed by the reference's int64 hash (the murmur3 64-bit finaliser,
+ * core/olap/lib/expressions/expressions-hasher.cpp:66-84).  Payloads and
+ * row ids stay int32; GBJ_VAL_BUILD_KEY gives the int64 key.  A table built
+ * here is probed only by the _i64 probes (and the other way round): a
+ * mismatch gives GBJ_ERR_INVALID. */
+int gbj_join_build_i64(gbj_ctx *ctx, const int64_t *d_keys,
+                       const int32_t *d_payload, uint64_t n, int32_t hash_bits,
+                       uint64_t max_build, void *stream, gbj_table **out);
+int gbj_join_probe_agg_i64(gbj_ctx *ctx, const gbj_table *table,
+                           const int64_t *d_keys, const int32_t *d_payload,
+                           uint64_t n, const gbj_agg *aggs, int32_t n_aggs,
+                           int64_t *d_out, void *stream);
+int gbj_join_probe_pairs_i64(gbj_ctx *ctx, const gbj_table *table,
+                             const int64_t *d_keys, const int32_t *d_probe_rows,
+                             uint64_t n, int32_t *d_build_rows,
+                             int32_t *d_out_probe_rows, uint64_t capacity,
+                             uint64_t *d_count, void *stream);
+
 int gbj_table_destroy(gbj_ctx *ctx, gbj_table *table);
 /* Number of slots of the table (host query). */
 uint64_t gbj_table_slots(const gbj_table *table);
@@ -291,6 +310,18 @@ int gbj_groupby(gbj_ctx *ctx, const int32_t *d_keys, const int32_t *d_values,
                 int32_t *d_out_keys, int64_t *d_out_count, int64_t *d_out_sum,
                 int32_t *d_out_min, int32_t *d_out_max, uint64_t out_capacity,
                 uint64_t *d_n_groups, void *stream);
+
+/* gbj_groupby over int64 keys (a HashGroupByChained whose key expression is
+ * int64, placed by the reference's int64 hash, expressions-hasher.cpp:
+ * 66-84): one output row per distinct key with COUNT, SUM (int64) and MIN /
+ * MAX (int32) of the int32 value column.  params as for gbj_groupby;
+ * strategy 2 (radix-partitioned) is not offered for int64 keys and gives
+ * GBJ_ERR_UNSUPPORTED.  The grouping engine is the one gbj_nest_i64 uses. */
+int gbj_groupby_i64(gbj_ctx *ctx, const int64_t *d_keys, const int32_t *d_values,
+                    uint64_t n, const gbj_groupby_params *params,
+                    int64_t *d_out_keys, int64_t *d_out_count, int64_t *d_out_sum,
+                    int32_t *d_out_min, int32_t *d_out_max, uint64_t out_capacity,
+                    uint64_t *d_n_groups, void *stream);
 
 /* ------------------------------------------------------------ bloom filter */
 /* BloomFilterBuild / BloomFilterProbe (core/olap/lib/operators/bloom-filter/

@@ -38,6 +38,17 @@ uint64_t orc_hash_int32(int32_t key) {
   return h;
 }
 
+/* hashInt64 (expressions-hasher.cpp:66-84): the murmur3 64-bit finaliser. */
+uint64_t orc_hash_int64(int64_t key) {
+  uint64_t h = (uint64_t)key;
+  h ^= h >> 33;
+  h *= 0xff51afd7ed558ccdULL;
+  h ^= h >> 33;
+  h *= 0xc4ceb9fe1a85ec53ULL;
+  h ^= h >> 33;
+  return h;
+}
+
 /* gpu-partitioned-hash-join-chained-helpers.cpp:49-56 (32-bit wrap). */
 uint32_t orc_hashd(int32_t key) {
   uint32_t h = (uint32_t)key;
@@ -74,6 +85,7 @@ int orc_join_build(const int32_t *keys, const int32_t *payload, uint64_t n,
   if (!t->head || !t->next) return -1;
   memset(t->head, 0xff, nb * sizeof(int32_t)); /* open_build: memset -1 */
   t->key = keys;
+  t->key64 = 0;
   t->payload = payload;
   t->n = n;
   t->hash_bits = hash_bits;
@@ -123,6 +135,7 @@ int orc_join_build_mt(const int32_t *keys, const int32_t *payload, uint64_t n,
   if (!t->head || !t->next) return -1;
   memset(t->head, 0xff, nb * sizeof(int32_t));
   t->key = keys;
+  t->key64 = 0;
   t->payload = payload;
   t->n = n;
   t->hash_bits = hash_bits;
@@ -171,7 +184,7 @@ static void acc_init(acc8 *a, const int32_t *ops, int n_aggs) {
   }
 }
 
-static inline int64_t operand_value(int operand, int32_t bkey, int64_t bval,
+static inline int64_t operand_value(int operand, int64_t bkey, int64_t bval,
                                     int64_t pval, int64_t brow, int64_t prow) {
   switch (operand) {
     case V_ONE: return 1;
@@ -188,7 +201,7 @@ static inline int64_t operand_value(int operand, int32_t bkey, int64_t bval,
 
 static inline void acc_update(acc8 *a, const int32_t *ops,
                               const int32_t *operands, int n_aggs,
-                              int32_t bkey, int64_t bval, int64_t pval,
+                              int64_t bkey, int64_t bval, int64_t pval,
                               int64_t brow, int64_t prow) {
   for (int j = 0; j < n_aggs; ++j) {
     int64_t x = operand_value(operands[j], bkey, bval, pval, brow, prow);
@@ -310,6 +323,82 @@ int64_t orc_join_probe_pairs(const orc_chained_table *t, const int32_t *keys,
     for (int32_t cur = t->head[bucket_of(k, t->hash_bits)]; cur != -1;
          cur = t->next[cur]) {
       if (t->key[cur] == k) {
+        if ((uint64_t)m < cap) {
+          if (build_rows) build_rows[m] = cur;
+          if (probe_rows) probe_rows[m] = (int32_t)i;
+        }
+        ++m;
+      }
+    }
+  }
+  return m;
+}
+
+/* ------------------------------------------------ hash join, int64 keys */
+
+static inline uint64_t bucket_of64(int64_t key, int hash_bits) {
+  return orc_hash_int64(key) & ((1ULL << hash_bits) - 1);
+}
+
+/* generate_build (hash-join-chained.cpp:262-319) with an int64 key. */
+int orc_join_build_i64(const int64_t *keys, const int32_t *payload, uint64_t n,
+                       int32_t hash_bits, orc_chained_table *t) {
+  if (!t || (n && !keys) || n > 0x7fffffffULL) return -1;
+  if (hash_bits <= 0) hash_bits = auto_hash_bits(n);
+  if (hash_bits > 32) return -1;
+  uint64_t nb = 1ULL << hash_bits;
+  t->head = (int32_t *)malloc(nb * sizeof(int32_t));
+  t->next = (int32_t *)malloc((n ? n : 1) * sizeof(int32_t));
+  if (!t->head || !t->next) return -1;
+  memset(t->head, 0xff, nb * sizeof(int32_t));
+  t->key = 0;
+  t->key64 = keys;
+  t->payload = payload;
+  t->n = n;
+  t->hash_bits = hash_bits;
+  for (uint64_t i = 0; i < n; ++i) {
+    uint64_t h = bucket_of64(keys[i], hash_bits);
+    t->next[i] = t->head[h];
+    t->head[h] = (int32_t)i;
+  }
+  return 0;
+}
+
+/* generate_probe (hash-join-chained.cpp:321-566) with an int64 key. */
+int orc_join_probe_agg_i64(const orc_chained_table *t, const int64_t *keys,
+                           const int32_t *payload, uint64_t n,
+                           const int32_t *ops, const int32_t *operands,
+                           int32_t n_aggs, int64_t *out) {
+  if (!t || !t->key64 || (n && !keys) || !out || check_aggs(ops, operands, n_aggs))
+    return -1;
+  acc8 acc;
+  acc_init(&acc, ops, n_aggs);
+  for (uint64_t i = 0; i < n; ++i) {
+    int64_t k = keys[i];
+    int64_t pv = payload ? payload[i] : 0;
+    for (int32_t cur = t->head[bucket_of64(k, t->hash_bits)]; cur != -1;
+         cur = t->next[cur]) {
+      if (t->key64[cur] == k) {
+        int64_t bv = t->payload ? t->payload[cur] : 0;
+        acc_update(&acc, ops, operands, n_aggs, k, bv, pv, cur, (int64_t)i);
+      }
+    }
+  }
+  for (int j = 0; j < n_aggs; ++j) out[j] = acc.v[j];
+  return 0;
+}
+
+int64_t orc_join_probe_pairs_i64(const orc_chained_table *t,
+                                 const int64_t *keys, uint64_t n,
+                                 int32_t *build_rows, int32_t *probe_rows,
+                                 uint64_t cap) {
+  if (!t || !t->key64 || (n && !keys)) return -1;
+  int64_t m = 0;
+  for (uint64_t i = 0; i < n; ++i) {
+    int64_t k = keys[i];
+    for (int32_t cur = t->head[bucket_of64(k, t->hash_bits)]; cur != -1;
+         cur = t->next[cur]) {
+      if (t->key64[cur] == k) {
         if ((uint64_t)m < cap) {
           if (build_rows) build_rows[m] = cur;
           if (probe_rows) probe_rows[m] = (int32_t)i;

@@ -38,6 +38,7 @@ typedef struct orc_chained_table {
   const int32_t *payload; /* per entry payload (further packets), may be 0   */
   uint64_t n;
   int32_t hash_bits;
+  const int64_t *key64;   /* int64 keys (orc_join_build_i64), else 0     */
 } orc_chained_table;
 
 int orc_join_build(const int32_t *keys, const int32_t *payload, uint64_t n,
@@ -61,6 +62,20 @@ int orc_join_probe_agg(const orc_chained_table *t, const int32_t *keys,
 int64_t orc_join_probe_pairs(const orc_chained_table *t, const int32_t *keys,
                              uint64_t n, int32_t *build_rows,
                              int32_t *probe_rows, uint64_t cap);
+
+/* The same join over int64 keys, chains placed by the reference's int64
+ * hash (expressions-hasher.cpp:66-84, murmur3's 64-bit finaliser). */
+uint64_t orc_hash_int64(int64_t key);
+int orc_join_build_i64(const int64_t *keys, const int32_t *payload, uint64_t n,
+                       int32_t hash_bits, orc_chained_table *t);
+int orc_join_probe_agg_i64(const orc_chained_table *t, const int64_t *keys,
+                           const int32_t *payload, uint64_t n,
+                           const int32_t *ops, const int32_t *operands,
+                           int32_t n_aggs, int64_t *out);
+int64_t orc_join_probe_pairs_i64(const orc_chained_table *t,
+                                 const int64_t *keys, uint64_t n,
+                                 int32_t *build_rows, int32_t *probe_rows,
+                                 uint64_t cap);
 
 /* ---- radix clustering (core/platform/lib/util/radix/joins/radix-join.cpp) */
 /* Stable counting-sort cluster on digit = (f(key) & (((1<<D)-1)<<R)) >> R,

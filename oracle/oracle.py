@@ -20,7 +20,7 @@ vp, u64, i32, i64 = C.c_void_p, C.c_uint64, C.c_int32, C.c_int64
 
 class ChainedTable(C.Structure):
     _fields_ = [("head", vp), ("next", vp), ("key", vp), ("payload", vp), ("n", u64),
-                ("hash_bits", i32)]
+                ("hash_bits", i32), ("key64", vp)]
 
 
 _lib = None
@@ -59,6 +59,13 @@ def lib():
                                          C.c_int]
         L.orc_join_probe_pairs.restype = i64
         L.orc_join_probe_pairs.argtypes = [C.POINTER(ChainedTable), vp, u64, vp, vp, u64]
+        L.orc_hash_int64.restype, L.orc_hash_int64.argtypes = u64, [i64]
+        L.orc_join_build_i64.restype = C.c_int
+        L.orc_join_build_i64.argtypes = [vp, vp, u64, i32, C.POINTER(ChainedTable)]
+        L.orc_join_probe_agg_i64.restype = C.c_int
+        L.orc_join_probe_agg_i64.argtypes = [C.POINTER(ChainedTable), vp, vp, u64, vp, vp, i32, vp]
+        L.orc_join_probe_pairs_i64.restype = i64
+        L.orc_join_probe_pairs_i64.argtypes = [C.POINTER(ChainedTable), vp, u64, vp, vp, u64]
         L.orc_radix_cluster.restype = None
         L.orc_radix_cluster.argtypes = [vp, vp, u64, i32, i32, i32, vp, vp, vp]
         L.orc_rj_stepwise.restype, L.orc_rj_stepwise.argtypes = i64, [vp, u64, vp, u64]
@@ -142,6 +149,35 @@ def join_agg(bkeys, bpay, pkeys, ppay, aggs, hash_bits=0, threads=1):
     L.orc_join_free(C.byref(t))
     assert rc == 0
     return [int(x) for x in out]
+
+
+def join_agg_i64(bkeys, bpay, pkeys, ppay, aggs, hash_bits=0):
+    """HashJoinChained over int64 keys (hashInt64 placement) -> int64 list."""
+    L = lib()
+    bkeys, pkeys = np.ascontiguousarray(bkeys, dtype=np.int64), np.ascontiguousarray(pkeys, dtype=np.int64)
+    bpay, ppay = _i32(bpay), _i32(ppay)
+    t = ChainedTable()
+    assert L.orc_join_build_i64(_p(bkeys), _p(bpay), len(bkeys), hash_bits, C.byref(t)) == 0
+    ops, opd = _aggs(aggs)
+    out = np.zeros(len(aggs), dtype=np.int64)
+    rc = L.orc_join_probe_agg_i64(C.byref(t), _p(pkeys), _p(ppay), len(pkeys), _p(ops), _p(opd),
+                                  len(aggs), _p(out))
+    L.orc_join_free(C.byref(t))
+    assert rc == 0
+    return [int(x) for x in out]
+
+
+def join_pairs_i64(bkeys, pkeys, hash_bits=0):
+    L = lib()
+    bkeys, pkeys = np.ascontiguousarray(bkeys, dtype=np.int64), np.ascontiguousarray(pkeys, dtype=np.int64)
+    t = ChainedTable()
+    assert L.orc_join_build_i64(_p(bkeys), None, len(bkeys), hash_bits, C.byref(t)) == 0
+    m = L.orc_join_probe_pairs_i64(C.byref(t), _p(pkeys), len(pkeys), None, None, 0)
+    b = np.empty(max(m, 1), dtype=np.int32)
+    p = np.empty(max(m, 1), dtype=np.int32)
+    L.orc_join_probe_pairs_i64(C.byref(t), _p(pkeys), len(pkeys), _p(b), _p(p), m)
+    L.orc_join_free(C.byref(t))
+    return b[:m], p[:m]
 
 
 def join_pairs(bkeys, pkeys, hash_bits=0):

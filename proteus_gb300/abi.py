@@ -103,6 +103,9 @@ SIGNATURES = {
     "gbj_join_build": (C.c_int, [vp, vp, vp, u64, i32, u64, vp, P(vp)]),
     "gbj_join_probe_agg": (C.c_int, [vp, vp, vp, vp, u64, P(Agg), i32, vp, vp]),
     "gbj_join_probe_pairs": (C.c_int, [vp, vp, vp, vp, u64, vp, vp, u64, vp, vp]),
+    "gbj_join_build_i64": (C.c_int, [vp, vp, vp, u64, i32, u64, vp, P(vp)]),
+    "gbj_join_probe_agg_i64": (C.c_int, [vp, vp, vp, vp, u64, P(Agg), i32, vp, vp]),
+    "gbj_join_probe_pairs_i64": (C.c_int, [vp, vp, vp, vp, u64, vp, vp, u64, vp, vp]),
     "gbj_table_destroy": (C.c_int, [vp, vp]),
     "gbj_table_slots": (u64, [vp]),
     "gbj_partition": (C.c_int, [vp, vp, vp, u64, i32, i32, i32, vp, vp, vp, vp]),
@@ -112,6 +115,8 @@ SIGNATURES = {
                                            P(Agg), i32, vp, vp]),
     "gbj_groupby": (C.c_int, [vp, vp, vp, u64, P(GroupbyParams), vp, vp, vp, vp, vp, u64, vp,
                               vp]),
+    "gbj_groupby_i64": (C.c_int, [vp, vp, vp, u64, P(GroupbyParams), vp, vp, vp, vp, vp, u64, vp,
+                                  vp]),
     "gbj_reduce": (C.c_int, [vp, vp, vp, u64, P(Agg), i32, vp, vp]),
     "gbj_gather": (C.c_int, [vp, vp, vp, u64, vp, vp]),
     "gbj_select_range": (C.c_int, [vp, vp, u64, i32, i32, vp, vp, vp]),

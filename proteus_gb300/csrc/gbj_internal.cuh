@@ -83,6 +83,7 @@ struct gbj_table {
   const int32_t *keys = nullptr;
   const int32_t *payload = nullptr;
   uint64_t n = 0;
+  bool i64 = false;  // int64 keys (gbj_join_build_i64): 2-slot buckets
 };
 
 // ------------------------------------------------------------ host helpers
@@ -190,7 +191,7 @@ __device__ __forceinline__ void latch(uint32_t *status, uint32_t bit) {
   atomicOr(status, bit);
 }
 
-__device__ __forceinline__ int64_t operand_value(int operand, int32_t key,
+__device__ __forceinline__ int64_t operand_value(int operand, int64_t key,
                                                  int64_t bval, int64_t pval,
                                                  int64_t brow, int64_t prow) {
   switch (operand) {
@@ -221,7 +222,7 @@ struct Acc {
   }
   // Branch-free: operand and op are selected with predicated moves, so a
   // match costs a few instructions per aggregate and no jump tables.
-  __device__ __forceinline__ void update(const gbj::AggSpec &s, int32_t key,
+  __device__ __forceinline__ void update(const gbj::AggSpec &s, int64_t key,
                                          int64_t bval, int64_t pval,
                                          int64_t brow, int64_t prow) {
     const int64_t prod = bval * pval, xr = brow ^ prow;

@@ -455,6 +455,202 @@ __global__ void __launch_bounds__(kThreads)
   }
 }
 
+// ------------------------------------------------ int64-key table
+// gbj_join_build_i64's table: 32-byte buckets of two slots -- two keys
+// (xor 2^63, so zero marks an empty slot; INT64_MIN goes to the side list),
+// their build payloads and their rows + 1 -- read with one 256-bit load.
+// Placement is the reference's int64 hash, the murmur3 64-bit finaliser
+// (core/olap/lib/expressions/expressions-hasher.cpp:66-84).
+struct __align__(32) JBucket64 {
+  unsigned long long k[2];
+  int32_t x[2];  // build payload (0 without one)
+  int32_t r[2];  // row + 1
+};
+constexpr unsigned long long kFlip64 = 0x8000000000000000ull;
+
+__device__ __forceinline__ uint64_t fmix64(uint64_t k) {
+  k ^= k >> 33;
+  k *= 0xff51afd7ed558ccdull;
+  k ^= k >> 33;
+  k *= 0xc4ceb9fe1a85ec53ull;
+  k ^= k >> 33;
+  return k;
+}
+
+__device__ __forceinline__ JBucket64 ld_bucket64(const JBucket64 *p) {
+  uint32_t w[8];
+  asm("ld.global.nc.v8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+      : "=r"(w[0]), "=r"(w[1]), "=r"(w[2]), "=r"(w[3]), "=r"(w[4]), "=r"(w[5]), "=r"(w[6]), "=r"(w[7])
+      : "l"(p));
+  JBucket64 b;
+  b.k[0] = ((unsigned long long)w[1] << 32) | w[0];
+  b.k[1] = ((unsigned long long)w[3] << 32) | w[2];
+  b.x[0] = (int32_t)w[4], b.x[1] = (int32_t)w[5];
+  b.r[0] = (int32_t)w[6], b.r[1] = (int32_t)w[7];
+  return b;
+}
+
+// meta[0]: a duplicate build key was seen; meta[1]: side-list length.
+__global__ void __launch_bounds__(kThreads)
+    k_jb64_build(const int64_t *__restrict__ keys, const int32_t *__restrict__ payload, uint64_t n,
+                 JBucket64 *__restrict__ bk, uint64_t bmask, uint32_t *__restrict__ meta,
+                 int32_t *__restrict__ side, uint32_t *status) {
+  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  bool dup = false;
+  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += stride) {
+    const int64_t key = keys[i];
+    const int32_t pv = payload ? payload[i] : 0;
+    const unsigned long long kf = (unsigned long long)key ^ kFlip64;
+    if (kf == 0) {
+      side[atomicAdd(&meta[1], 1u)] = (int32_t)i;
+      continue;
+    }
+    const uint64_t h = fmix64((uint64_t)key);
+    uint64_t b = h & bmask;
+    const uint32_t o = (uint32_t)(h >> 63);
+    bool placed = false;
+    for (uint64_t step = 0; step <= bmask && !placed; ++step) {
+#pragma unroll
+      for (uint32_t j = 0; j < 2; ++j) {
+        if (placed) break;
+        const uint32_t sl = (o + j) & 1u;
+        const unsigned long long old = atomicCAS(&bk[b].k[sl], 0ull, kf);
+        if (old == 0) {
+          bk[b].x[sl] = pv;
+          bk[b].r[sl] = (int32_t)(i + 1);
+          placed = true;
+        } else {
+          dup |= old == kf;
+        }
+      }
+      b = (b + 1) & bmask;
+    }
+    if (!placed) gbjd::latch(status, GBJ_DEV_CAPACITY);
+  }
+  if (dup) meta[0] = 1;
+}
+
+// Probe with fused aggregate over the int64-key table: four probes per
+// thread, their bucket loads issued together; a probe moves past its home
+// bucket only when it is full and (for unique build keys) has no match.
+__global__ void __launch_bounds__(kThreads)
+    k_jb64_probe_agg(const int64_t *__restrict__ keys, const int32_t *__restrict__ pay, uint64_t n,
+                     const JBucket64 *__restrict__ bk, uint64_t bmask, const int32_t *__restrict__ bpay,
+                     const uint32_t *__restrict__ meta, const int32_t *__restrict__ side, gbj::AggSpec spec,
+                     int64_t *out) {
+  __shared__ int64_t red[32 * GBJ_MAX_AGGS];
+  gbjd::Acc acc;
+  acc.init(spec);
+  const bool unique = meta[0] == 0;
+  const uint32_t nside = meta[1];
+  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  auto visit = [&](int64_t k, unsigned long long kf, int64_t pv, uint64_t prow, const JBucket64 &e) -> uint32_t {
+    uint32_t c = 0;
+#pragma unroll
+    for (int j = 0; j < 2; ++j) {
+      if (e.k[j] == kf) {
+        acc.update(spec, k, e.x[j], pv, (int64_t)e.r[j] - 1, (int64_t)prow);
+        ++c;
+      }
+    }
+    return c;
+  };
+  auto room = [](const JBucket64 &e) { return e.k[0] == 0 || e.k[1] == 0; };
+  auto finish = [&](int64_t k, int64_t pv, uint64_t prow, uint64_t b, const JBucket64 &e0) {
+    const unsigned long long kf = (unsigned long long)k ^ kFlip64;
+    if (kf == 0) {  // INT64_MIN meets the side list
+      for (uint32_t s = 0; s < nside; ++s) {
+        const int32_t r = side[s];
+        acc.update(spec, k, bpay ? (int64_t)bpay[r] : 0, pv, r, (int64_t)prow);
+        if (unique) break;
+      }
+      return;
+    }
+    uint32_t matched = visit(k, kf, pv, prow, e0);
+    if (room(e0) || (unique && matched)) return;
+    for (uint64_t step = 1; step <= bmask; ++step) {
+      b = (b + 1) & bmask;
+      const JBucket64 e = ld_bucket64(&bk[b]);
+      matched += visit(k, kf, pv, prow, e);
+      if (room(e) || (unique && matched)) return;
+    }
+  };
+  constexpr int G = 4;
+  const uint64_t ng = n / G;
+  for (uint64_t q = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; q < ng; q += stride) {
+    int64_t kk[G];
+    int64_t pp[G];
+    uint64_t b[G];
+    JBucket64 e[G];
+#pragma unroll
+    for (int j = 0; j < G; ++j) {
+      kk[j] = __ldcs(keys + q * G + j);
+      pp[j] = pay ? __ldcs(pay + q * G + j) : 0;
+    }
+#pragma unroll
+    for (int j = 0; j < G; ++j) {
+      b[j] = fmix64((uint64_t)kk[j]) & bmask;
+      e[j] = ld_bucket64(&bk[b[j]]);
+    }
+#pragma unroll
+    for (int j = 0; j < G; ++j) finish(kk[j], pp[j], q * G + j, b[j], e[j]);
+  }
+  for (uint64_t i = ng * G + blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += stride) {
+    const int64_t k = keys[i];
+    const uint64_t b = fmix64((uint64_t)k) & bmask;
+    finish(k, pay ? pay[i] : 0, i, b, ld_bucket64(&bk[b]));
+  }
+  gbjd::block_flush(spec, acc, red, out);
+}
+
+// Pair output over the int64-key table (warp-aggregated output reservations).
+__global__ void __launch_bounds__(kThreads)
+    k_jb64_probe_pairs(const int64_t *__restrict__ keys, const int32_t *__restrict__ prows, uint64_t n,
+                       const JBucket64 *__restrict__ bk, uint64_t bmask, const uint32_t *__restrict__ meta,
+                       const int32_t *__restrict__ side, int32_t *__restrict__ out_b,
+                       int32_t *__restrict__ out_p, uint64_t cap, unsigned long long *count, uint32_t *status) {
+  const bool unique = meta[0] == 0;
+  const uint32_t nside = meta[1];
+  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  auto emit = [&](int32_t br, int32_t pr) {
+    cg::coalesced_group g = cg::coalesced_threads();
+    unsigned long long base = 0;
+    if (g.thread_rank() == 0) base = atomicAdd(count, (unsigned long long)g.size());
+    base = g.shfl(base, 0) + g.thread_rank();
+    if (base < cap) {
+      out_b[base] = br;
+      out_p[base] = pr;
+    } else {
+      gbjd::latch(status, GBJ_DEV_CAPACITY);
+    }
+  };
+  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += stride) {
+    const int64_t k = keys[i];
+    const int32_t pr = prows ? prows[i] : (int32_t)i;
+    const unsigned long long kf = (unsigned long long)k ^ kFlip64;
+    if (kf == 0) {
+      for (uint32_t s = 0; s < nside; ++s) {
+        emit(side[s], pr);
+        if (unique) break;
+      }
+      continue;
+    }
+    uint64_t b = fmix64((uint64_t)k) & bmask;
+    for (uint64_t step = 0; step <= bmask; ++step) {
+      const JBucket64 e = ld_bucket64(&bk[b]);
+      bool stop = e.k[0] == 0 || e.k[1] == 0;
+      for (int j = 0; j < 2; ++j) {
+        if (e.k[j] == kf) {
+          emit(e.r[j] - 1, pr);
+          if (unique) stop = true;
+        }
+      }
+      if (stop) break;
+      b = (b + 1) & bmask;
+    }
+  }
+}
+
 // Column reduce (Reduce over one column, optional row list).
 __global__ void __launch_bounds__(kThreads)
     k_reduce(const int32_t *__restrict__ col, const int32_t *__restrict__ rows,
@@ -708,6 +904,7 @@ int gbj_join_probe_agg(gbj_ctx *ctx, const gbj_table *t, const int32_t *d_keys,
                        const int32_t *d_payload, uint64_t n, const gbj_agg *aggs,
                        int32_t n_aggs, int64_t *d_out, void *stream) {
   if (!ctx || !t || !d_out) return GBJ_ERR_INVALID;
+  if (t->i64) return set_error(ctx, GBJ_ERR_INVALID, "join_probe: the table has int64 keys (use the _i64 probe)");
   if (n && !d_keys) return set_error(ctx, GBJ_ERR_INVALID, "join_probe: null keys");
   GBJ_TRY(validate_aggs(ctx, aggs, n_aggs));
   AggSpec spec = make_spec(aggs, n_aggs);
@@ -732,6 +929,7 @@ int gbj_join_probe_pairs(gbj_ctx *ctx, const gbj_table *t, const int32_t *d_keys
                          uint64_t capacity, uint64_t *d_count, void *stream) {
   if (!ctx || !t || !d_count || !d_build_rows || !d_out_probe_rows)
     return GBJ_ERR_INVALID;
+  if (t->i64) return set_error(ctx, GBJ_ERR_INVALID, "join_probe: the table has int64 keys (use the _i64 probe)");
   if (n && !d_keys) return set_error(ctx, GBJ_ERR_INVALID, "join_probe: null keys");
   cudaStream_t s = pick_stream(ctx, stream);
   prof_mark(ctx, s);
@@ -747,6 +945,99 @@ int gbj_join_probe_pairs(gbj_ctx *ctx, const gbj_table *t, const int32_t *d_keys
     k_jb_probe_pairs<false><<<grid_for(ctx, n, kThreads), kThreads, 0, s>>>(
         d_keys, d_probe_rows, n, bk, nullptr, bmask, t->meta, t->side, d_build_rows, d_out_probe_rows, capacity,
         (unsigned long long *)d_count, ctx->d_status);
+  return after_launch(ctx, "k_join_probe_pairs", s);
+}
+
+int gbj_join_build_i64(gbj_ctx *ctx, const int64_t *d_keys, const int32_t *d_payload, uint64_t n,
+                       int32_t hash_bits, uint64_t max_build, void *stream, gbj_table **out) {
+  if (!ctx || !out) return GBJ_ERR_INVALID;
+  *out = nullptr;
+  if (n && !d_keys) return set_error(ctx, GBJ_ERR_INVALID, "join_build: null keys");
+  if (n >= (1ULL << 31)) return set_error(ctx, GBJ_ERR_INVALID, "join_build: n >= 2^31");
+  if (hash_bits < 0 || hash_bits > 32)
+    return set_error(ctx, GBJ_ERR_INVALID, "join_build: hash_bits out of range");
+  if (max_build && n > max_build)
+    return set_error(ctx, GBJ_ERR_CAPACITY, "Build input size exceeded given parameter (maxBuildInputSize)");
+  cudaStream_t s = pick_stream(ctx, stream);
+  prof_mark(ctx, s);
+  uint64_t slots = next_pow2(2 * (n ? n : 1));
+  if (hash_bits && (1ULL << hash_bits) > slots) slots = 1ULL << hash_bits;
+  if (slots < 64) slots = 64;
+  const uint64_t nbk = slots / 2;
+  const uint64_t clear_bytes = nbk * sizeof(JBucket64) + 256;
+  gbj_table *t = new gbj_table();
+  void *mem = nullptr;
+  int rc = pool_alloc(ctx, clear_bytes + (n + 4) * sizeof(int32_t), s, &mem);
+  if (rc) {
+    delete t;
+    return rc;
+  }
+  char *base = static_cast<char *>(mem);
+  t->slots = mem;
+  t->meta = reinterpret_cast<uint32_t *>(base + nbk * sizeof(JBucket64));
+  t->side = reinterpret_cast<int32_t *>(base + clear_bytes);
+  t->mask = slots - 1;
+  t->payload = d_payload;
+  t->n = n;
+  t->i64 = true;
+  cudaError_t e = cudaMemsetAsync(mem, 0, clear_bytes, s);
+  if (e != cudaSuccess) {
+    pool_release(ctx, mem, s);
+    delete t;
+    return cuda_error(ctx, e, "cudaMemsetAsync(table)");
+  }
+  if (n) {
+    k_jb64_build<<<grid_for(ctx, n, kThreads), kThreads, 0, s>>>(d_keys, d_payload, n,
+                                                                  reinterpret_cast<JBucket64 *>(mem), nbk - 1,
+                                                                  t->meta, t->side, ctx->d_status);
+    rc = after_launch(ctx, "k_join_build", s);
+    if (rc) {
+      pool_release(ctx, mem, s);
+      delete t;
+      return rc;
+    }
+  }
+  *out = t;
+  return GBJ_OK;
+}
+
+int gbj_join_probe_agg_i64(gbj_ctx *ctx, const gbj_table *t, const int64_t *d_keys, const int32_t *d_payload,
+                           uint64_t n, const gbj_agg *aggs, int32_t n_aggs, int64_t *d_out, void *stream) {
+  if (!ctx || !t || !d_out) return GBJ_ERR_INVALID;
+  if (!t->i64) return set_error(ctx, GBJ_ERR_INVALID, "join_probe_i64: the table has int32 keys");
+  if (n && !d_keys) return set_error(ctx, GBJ_ERR_INVALID, "join_probe: null keys");
+  GBJ_TRY(validate_aggs(ctx, aggs, n_aggs));
+  AggSpec spec = make_spec(aggs, n_aggs);
+  for (int j = 0; j < n_aggs; ++j) {
+    int o = spec.operand[j];
+    if ((o == GBJ_VAL_BUILD || o == GBJ_VAL_PRODUCT) && !t->payload && t->n)
+      return set_error(ctx, GBJ_ERR_INVALID, "aggregate reads the build payload, table has none");
+    if ((o == GBJ_VAL_PROBE || o == GBJ_VAL_PRODUCT) && !d_payload && n)
+      return set_error(ctx, GBJ_ERR_INVALID, "aggregate reads the probe payload, none given");
+  }
+  cudaStream_t s = pick_stream(ctx, stream);
+  prof_mark(ctx, s);
+  GBJ_TRY(init_agg_out(ctx, spec, d_out, s));
+  if (n == 0) return GBJ_OK;
+  k_jb64_probe_agg<<<grid_for(ctx, (n + 3) / 4, kThreads, 2), kThreads, 0, s>>>(
+      d_keys, d_payload, n, static_cast<const JBucket64 *>(t->slots), (t->mask + 1) / 2 - 1, t->payload, t->meta,
+      t->side, spec, d_out);
+  return after_launch(ctx, "k_join_probe_agg", s);
+}
+
+int gbj_join_probe_pairs_i64(gbj_ctx *ctx, const gbj_table *t, const int64_t *d_keys,
+                             const int32_t *d_probe_rows, uint64_t n, int32_t *d_build_rows,
+                             int32_t *d_out_probe_rows, uint64_t capacity, uint64_t *d_count, void *stream) {
+  if (!ctx || !t || !d_count || !d_build_rows || !d_out_probe_rows) return GBJ_ERR_INVALID;
+  if (!t->i64) return set_error(ctx, GBJ_ERR_INVALID, "join_probe_i64: the table has int32 keys");
+  if (n && !d_keys) return set_error(ctx, GBJ_ERR_INVALID, "join_probe: null keys");
+  cudaStream_t s = pick_stream(ctx, stream);
+  prof_mark(ctx, s);
+  GBJ_CHECK_CUDA(ctx, cudaMemsetAsync(d_count, 0, sizeof(uint64_t), s));
+  if (n == 0) return GBJ_OK;
+  k_jb64_probe_pairs<<<grid_for(ctx, n, kThreads), kThreads, 0, s>>>(
+      d_keys, d_probe_rows, n, static_cast<const JBucket64 *>(t->slots), (t->mask + 1) / 2 - 1, t->meta, t->side,
+      d_build_rows, d_out_probe_rows, capacity, (unsigned long long *)d_count, ctx->d_status);
   return after_launch(ctx, "k_join_probe_pairs", s);
 }
 

@@ -92,14 +92,17 @@ __device__ __forceinline__ void add_kv(const Table64 &t, int64_t k, int64_t v, b
   }
 }
 
-__device__ __forceinline__ void add_row(const Table64 &t, int64_t k, const int64_t *vals, uint64_t i,
+template <typename V>
+__device__ __forceinline__ void add_row(const Table64 &t, int64_t k, const V *vals, uint64_t i,
                                         uint32_t *status) {
-  add_kv(t, k, vals ? __ldcs(vals + i) : 0, vals != nullptr, status);
+  add_kv(t, k, vals ? (int64_t)__ldcs(vals + i) : 0, vals != nullptr, status);
 }
 
-// Every row into its group (vals null: counts only).
+// Every row into its group (vals null: counts only); V is the value
+// column's type (int64 for the nest, int32 for the int64-key group-by).
+template <typename V>
 __global__ void __launch_bounds__(kThreads)
-    k_nest_build(const int64_t *__restrict__ keys, const int64_t *__restrict__ vals, uint64_t n, Table64 t,
+    k_nest_build(const int64_t *__restrict__ keys, const V *__restrict__ vals, uint64_t n, Table64 t,
                  uint32_t *status) {
   const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
   for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += stride)
@@ -260,8 +263,9 @@ __device__ __forceinline__ void l1n_flush_slot(const L1N &t, const Table64 &g, u
 
 // Raw int64 rows in items of kL1Chunk; level 1 persists for the CTA's
 // lifetime and goes to the global table when the CTA finishes.
+template <typename V>
 __global__ void __launch_bounds__(kL1Threads, 1)
-    k_nest_l1(const int64_t *__restrict__ keys, const int64_t *__restrict__ vals, uint64_t n, uint32_t tslots,
+    k_nest_l1(const int64_t *__restrict__ keys, const V *__restrict__ vals, uint64_t n, uint32_t tslots,
               uint32_t rlog, Table64 g, unsigned long long *item_ctr, uint32_t *status) {
   extern __shared__ __align__(16) unsigned char smem[];
   __shared__ unsigned long long s_item;
@@ -318,7 +322,7 @@ __global__ void __launch_bounds__(kL1Threads, 1)
       for (int u = 0; u < 4; ++u) {
         const uint64_t i = b0 + threadIdx.x + (uint64_t)u * kL1Threads;
         nk[u] = i < hi ? __ldcs(keys + i) : 0;
-        nv[u] = (i < hi && has_v) ? __ldcs(vals + i) : 0;
+        nv[u] = (i < hi && has_v) ? (int64_t)__ldcs(vals + i) : 0;
       }
     };
     load(lo);
@@ -341,9 +345,10 @@ __global__ void __launch_bounds__(kL1Threads, 1)
 
 // The occupied slots (and INT64_MIN's) to the output; one output
 // reservation per warp.
+template <typename M>
 __global__ void __launch_bounds__(kThreads)
     k_nest_emit(Table64 t, bool with_vals, int64_t *__restrict__ ok, int64_t *__restrict__ oc,
-                int64_t *__restrict__ os, int64_t *__restrict__ omn, int64_t *__restrict__ omx, uint64_t cap,
+                int64_t *__restrict__ os, M *__restrict__ omn, M *__restrict__ omx, uint64_t cap,
                 unsigned long long *__restrict__ n_out, uint32_t *status) {
   const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
   const uint64_t slots = t.mask + 2;
@@ -371,8 +376,8 @@ __global__ void __launch_bounds__(kThreads)
     if (ok) ok[pos] = key;
     if (oc) oc[pos] = (int64_t)t.cnt[i];
     if (os) os[pos] = with_vals ? (int64_t)t.sum[i] : 0;
-    if (omn) omn[pos] = with_vals ? (int64_t)(~t.mn[i] ^ kFlip64) : 0;
-    if (omx) omx[pos] = with_vals ? (int64_t)(t.mx[i] ^ kFlip64) : 0;
+    if (omn) omn[pos] = with_vals ? (M)(int64_t)(~t.mn[i] ^ kFlip64) : 0;
+    if (omx) omx[pos] = with_vals ? (M)(int64_t)(t.mx[i] ^ kFlip64) : 0;
   }
 }
 
@@ -417,6 +422,44 @@ unsigned grid_for(gbj_ctx *ctx, uint64_t n) {
                                                             (uint64_t)ctx->sm_count * 8));
 }
 
+
+// Grouping over int64 keys: the nest's (V = M = int64) and the int64-key
+// group-by's (V = M = int32).  `groups` sizes the global table; an expected
+// group count up to kL1MaxGroups (use_l1) puts the on-chip level in front.
+template <typename V, typename M>
+int nest_impl(gbj_ctx *ctx, const int64_t *d_keys, const V *d_vals, uint64_t n, uint64_t groups, bool use_l1,
+              uint64_t expected_groups, int64_t *d_out_keys, int64_t *d_out_count, int64_t *d_out_sum,
+              M *d_out_min, M *d_out_max, uint64_t out_capacity, uint64_t *d_n_groups, cudaStream_t s) {
+  Scratch scratch(ctx, s);
+  Table64 t;
+  GBJ_TRY(make_table(ctx, scratch, next_pow2(2 * groups), d_vals != nullptr, s, &t));
+  if (use_l1) {
+    // few groups: the on-chip level first (tables at 8 x groups)
+    const uint32_t tslots =
+        (uint32_t)std::min<uint64_t>(kL1MaxSlots, std::max<uint64_t>(64, next_pow2(8 * expected_groups)));
+    uint32_t rlog = 0;  // as many accumulator columns (<= 32) as the budget allows
+    while (rlog < 5 && (size_t)tslots * l1_slot_bytes(rlog + 1) <= kL1Budget) ++rlog;
+    const size_t smem = (size_t)tslots * l1_slot_bytes(rlog);
+    unsigned long long *ctr;
+    GBJ_TRY(scratch.get(1, &ctr));
+    GBJ_CHECK_CUDA(ctx, cudaMemsetAsync(ctr, 0, sizeof(unsigned long long), s));
+    auto kern = k_nest_l1<V>;
+    GBJ_CHECK_CUDA(ctx, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    int per_sm = 1;
+    GBJ_CHECK_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kL1Threads, smem));
+    per_sm = std::max(per_sm, 1);
+    kern<<<ctx->sm_count * per_sm, kL1Threads, smem, s>>>(d_keys, d_vals, n, tslots, rlog, t, ctr, ctx->d_status);
+    GBJ_TRY(after_launch(ctx, "k_nest_l1", s));
+  } else {
+    k_nest_build<V><<<grid_for(ctx, n), kThreads, 0, s>>>(d_keys, d_vals, n, t, ctx->d_status);
+    GBJ_TRY(after_launch(ctx, "k_nest_build", s));
+  }
+  k_nest_emit<M><<<grid_for(ctx, t.mask + 2), kThreads, 0, s>>>(
+      t, d_vals != nullptr, d_out_keys, d_out_count, d_out_sum, d_out_min, d_out_max, out_capacity,
+      reinterpret_cast<unsigned long long *>(d_n_groups), ctx->d_status);
+  return after_launch(ctx, "k_nest_emit", s);
+}
+
 }  // namespace
 
 extern "C" int gbj_nest_i64(gbj_ctx *ctx, const int64_t *d_keys, const int64_t *d_vals, uint64_t n,
@@ -433,34 +476,40 @@ extern "C" int gbj_nest_i64(gbj_ctx *ctx, const int64_t *d_keys, const int64_t *
   if (n == 0) return GBJ_OK;
   const uint64_t groups = std::max<uint64_t>(1024, expected_groups ? std::min(expected_groups, n)
                                                                    : std::min<uint64_t>(n, 1ull << 24));
-  Scratch scratch(ctx, s);
-  Table64 t;
-  GBJ_TRY(make_table(ctx, scratch, next_pow2(2 * groups), d_vals != nullptr, s, &t));
-  if (expected_groups && expected_groups <= kL1MaxGroups) {
-    // few groups: the on-chip level first (tables at 8 x groups)
-    const uint32_t tslots =
-        (uint32_t)std::min<uint64_t>(kL1MaxSlots, std::max<uint64_t>(64, next_pow2(8 * expected_groups)));
-    uint32_t rlog = 0;  // as many accumulator columns (<= 32) as the budget allows
-    while (rlog < 5 && (size_t)tslots * l1_slot_bytes(rlog + 1) <= kL1Budget) ++rlog;
-    const size_t smem = (size_t)tslots * l1_slot_bytes(rlog);
-    unsigned long long *ctr;
-    GBJ_TRY(scratch.get(1, &ctr));
-    GBJ_CHECK_CUDA(ctx, cudaMemsetAsync(ctr, 0, sizeof(unsigned long long), s));
-    GBJ_CHECK_CUDA(ctx, cudaFuncSetAttribute(k_nest_l1, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    int per_sm = 1;
-    GBJ_CHECK_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_nest_l1, kL1Threads, smem));
-    per_sm = std::max(per_sm, 1);
-    k_nest_l1<<<ctx->sm_count * per_sm, kL1Threads, smem, s>>>(d_keys, d_vals, n, tslots, rlog, t, ctr,
-                                                              ctx->d_status);
-    GBJ_TRY(after_launch(ctx, "k_nest_l1", s));
-  } else {
-    k_nest_build<<<grid_for(ctx, n), kThreads, 0, s>>>(d_keys, d_vals, n, t, ctx->d_status);
-    GBJ_TRY(after_launch(ctx, "k_nest_build", s));
+  return nest_impl<int64_t, int64_t>(ctx, d_keys, d_vals, n, groups,
+                                     expected_groups && expected_groups <= kL1MaxGroups, expected_groups,
+                                     d_out_keys, d_out_count, d_out_sum, d_out_min, d_out_max, out_capacity,
+                                     d_n_groups, s);
+}
+
+extern "C" int gbj_groupby_i64(gbj_ctx *ctx, const int64_t *d_keys, const int32_t *d_values, uint64_t n,
+                               const gbj_groupby_params *params, int64_t *d_out_keys, int64_t *d_out_count,
+                               int64_t *d_out_sum, int32_t *d_out_min, int32_t *d_out_max, uint64_t out_capacity,
+                               uint64_t *d_n_groups, void *stream) {
+  if (!ctx || !d_n_groups) return GBJ_ERR_INVALID;
+  if (n && (!d_keys || !d_values)) return set_error(ctx, GBJ_ERR_INVALID, "groupby_i64: null column");
+  if (n >= (1ULL << 31)) return set_error(ctx, GBJ_ERR_INVALID, "groupby_i64: n >= 2^31");
+  uint64_t hint = 0;
+  int32_t hash_bits = 0;
+  int strategy = 0;
+  if (params) {
+    hint = params->expected_groups ? params->expected_groups : params->max_input_size;
+    hash_bits = params->hash_bits;
+    strategy = params->strategy;
   }
-  k_nest_emit<<<grid_for(ctx, t.mask + 2), kThreads, 0, s>>>(
-      t, d_vals != nullptr, d_out_keys, d_out_count, d_out_sum, d_out_min, d_out_max, out_capacity,
-      reinterpret_cast<unsigned long long *>(d_n_groups), ctx->d_status);
-  return after_launch(ctx, "k_nest_emit", s);
+  if (hash_bits < 0 || hash_bits > 32) return set_error(ctx, GBJ_ERR_INVALID, "groupby_i64: bad hash_bits");
+  if (strategy < 0 || strategy > 2) return set_error(ctx, GBJ_ERR_INVALID, "groupby_i64: bad strategy");
+  if (strategy == 2)
+    return set_error(ctx, GBJ_ERR_UNSUPPORTED, "groupby_i64: no radix-partitioned strategy for int64 keys");
+  cudaStream_t s = pick_stream(ctx, stream);
+  prof_mark(ctx, s);
+  GBJ_CHECK_CUDA(ctx, cudaMemsetAsync(d_n_groups, 0, sizeof(uint64_t), s));
+  if (n == 0) return GBJ_OK;
+  uint64_t groups = std::max<uint64_t>(1024, hint ? std::min(hint, n) : std::min<uint64_t>(n, 1ull << 24));
+  if (hash_bits) groups = std::max<uint64_t>(groups, (1ULL << hash_bits) / 2);  // the table holds 2^hash_bits slots
+  return nest_impl<int32_t, int32_t>(ctx, d_keys, d_values, n, groups, hint && hint <= kL1MaxGroups, hint,
+                                     d_out_keys, d_out_count, d_out_sum, d_out_min, d_out_max, out_capacity,
+                                     d_n_groups, s);
 }
 
 extern "C" int gbj_radix_join_count_i64(gbj_ctx *ctx, const int64_t *d_r_keys, uint64_t nr,
@@ -476,7 +525,7 @@ extern "C" int gbj_radix_join_count_i64(gbj_ctx *ctx, const int64_t *d_r_keys, u
   Scratch scratch(ctx, s);
   Table64 t;
   GBJ_TRY(make_table(ctx, scratch, next_pow2(std::max<uint64_t>(2 * nr, 1024)), false, s, &t));
-  k_nest_build<<<grid_for(ctx, nr), kThreads, 0, s>>>(d_r_keys, nullptr, nr, t, ctx->d_status);
+  k_nest_build<int64_t><<<grid_for(ctx, nr), kThreads, 0, s>>>(d_r_keys, nullptr, nr, t, ctx->d_status);
   GBJ_TRY(after_launch(ctx, "k_nest_build", s));
   k_join_count_probe<<<grid_for(ctx, ns), kThreads, 0, s>>>(d_s_keys, ns, t,
                                                             reinterpret_cast<unsigned long long *>(d_count));

@@ -35,8 +35,8 @@ def _cur_stream():
 class Table:
     """A built join hash table (gbj_table); keeps its input tensors alive."""
 
-    def __init__(self, ctx: "Context", handle: int, keep):
-        self.ctx, self.handle, self._keep = ctx, handle, keep
+    def __init__(self, ctx: "Context", handle: int, keep, i64: bool = False):
+        self.ctx, self.handle, self._keep, self.i64 = ctx, handle, keep, i64
 
     @property
     def slots(self) -> int:
@@ -119,10 +119,15 @@ class Context:
 
     # ------------------------------------------------------------- joins
     def join_build(self, keys, payload=None, hash_bits=0, max_build=0, stream=None) -> Table:
+        """int32 keys -> gbj_join_build, int64 keys -> gbj_join_build_i64."""
+        import torch
+
+        i64 = keys.dtype == torch.int64
+        fn = self.lib.gbj_join_build_i64 if i64 else self.lib.gbj_join_build
         h = C.c_void_p()
-        self.check(self.lib.gbj_join_build(self.handle, _ptr(keys), _ptr(payload), keys.numel(),
-                                           hash_bits, max_build, self._s(stream), C.byref(h)))
-        return Table(self, h.value, (keys, payload))
+        self.check(fn(self.handle, _ptr(keys), _ptr(payload), keys.numel(), hash_bits, max_build,
+                      self._s(stream), C.byref(h)))
+        return Table(self, h.value, (keys, payload), i64)
 
     def join_probe_agg(self, table: Table, keys, payload, aggs, out=None, stream=None):
         import torch
@@ -130,9 +135,9 @@ class Context:
         if out is None:
             out = torch.empty(len(aggs), dtype=torch.int64, device=keys.device)
         arr = abi.aggs_array(aggs)
-        self.check(self.lib.gbj_join_probe_agg(self.handle, table.handle, _ptr(keys), _ptr(payload),
-                                               keys.numel(), arr, len(aggs), _ptr(out),
-                                               self._s(stream)))
+        fn = self.lib.gbj_join_probe_agg_i64 if table.i64 else self.lib.gbj_join_probe_agg
+        self.check(fn(self.handle, table.handle, _ptr(keys), _ptr(payload), keys.numel(), arr, len(aggs),
+                      _ptr(out), self._s(stream)))
         return out
 
     def join_probe_pairs(self, table: Table, keys, capacity, probe_rows=None, stream=None):
@@ -142,9 +147,9 @@ class Context:
         b = torch.empty(max(capacity, 1), dtype=torch.int32, device=dev)
         p = torch.empty(max(capacity, 1), dtype=torch.int32, device=dev)
         cnt = torch.zeros(1, dtype=torch.int64, device=dev)
-        self.check(self.lib.gbj_join_probe_pairs(self.handle, table.handle, _ptr(keys),
-                                                 _ptr(probe_rows), keys.numel(), _ptr(b), _ptr(p),
-                                                 capacity, _ptr(cnt), self._s(stream)))
+        fn = self.lib.gbj_join_probe_pairs_i64 if table.i64 else self.lib.gbj_join_probe_pairs
+        self.check(fn(self.handle, table.handle, _ptr(keys), _ptr(probe_rows), keys.numel(), _ptr(b),
+                      _ptr(p), capacity, _ptr(cnt), self._s(stream)))
         return b, p, cnt
 
     def radix_join_agg(self, bkeys, bpay, pkeys, ppay, aggs, out=None, bits=0, passes=0,
@@ -320,16 +325,18 @@ class Context:
             raise ValueError("groupby: keys and values differ in length")
         dev = keys.device
         cap = max(out_capacity, 1)
-        ok = torch.empty(cap, dtype=torch.int32, device=dev)
+        i64 = keys.dtype == torch.int64  # int64 keys: gbj_groupby_i64
+        ok = torch.empty(cap, dtype=torch.int64 if i64 else torch.int32, device=dev)
         oc = torch.empty(cap, dtype=torch.int64, device=dev)
         osum = torch.empty(cap, dtype=torch.int64, device=dev)
         omin = torch.empty(cap, dtype=torch.int32, device=dev)
         omax = torch.empty(cap, dtype=torch.int32, device=dev)
         ng = torch.zeros(1, dtype=torch.int64, device=dev)
         prm = abi.GroupbyParams(hash_bits, strategy, max_input_size, expected_groups)
-        self.check(self.lib.gbj_groupby(self.handle, _ptr(keys), _ptr(values), keys.numel(),
-                                        C.byref(prm), _ptr(ok), _ptr(oc), _ptr(osum), _ptr(omin),
-                                        _ptr(omax), out_capacity, _ptr(ng), self._s(stream)))
+        fn = self.lib.gbj_groupby_i64 if i64 else self.lib.gbj_groupby
+        self.check(fn(self.handle, _ptr(keys), _ptr(values), keys.numel(), C.byref(prm), _ptr(ok),
+                      _ptr(oc), _ptr(osum), _ptr(omin), _ptr(omax), out_capacity, _ptr(ng),
+                      self._s(stream)))
         return ok, oc, osum, omin, omax, ng
 
     # ------------------------------------------------------------ columns

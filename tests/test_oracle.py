@@ -276,3 +276,40 @@ def test_minor_key_join_brute_force(oracle):
             exp[4] &= int(pp[j] != 0)
     for threads in (1, 3):
         assert oracle.radix_join_agg_minor(bk, bm, bp, pk, pm, pp, aggs, bits=3, threads=threads) == exp
+
+
+def test_join_i64_matches_brute_force_and_int32_join(oracle):
+    """The int64 chained join: brute force on wide keys, and equal to the
+    int32 join when every key fits 32 bits."""
+    import collections
+
+    rng = np.random.default_rng(21)
+    aggs = [(0, 0), (1, 3), (1, 6), (3, 7), (2, 4)]
+    rk = rng.integers(-(1 << 62), 1 << 62, 700).astype(np.int64)
+    rk[::7] = rk[3]  # duplicates
+    rp = rng.integers(-1000, 1000, len(rk)).astype(np.int32)
+    sk = np.concatenate([rk[rng.integers(0, len(rk), 3000)], rk[:50] ^ (1 << 33)]).astype(np.int64)
+    sp = rng.integers(-1000, 1000, len(sk)).astype(np.int32)
+    rows = collections.defaultdict(list)
+    for i, k in enumerate(rk.tolist()):
+        rows[k].append(i)
+    c = s = x = 0
+    mx, mn = -(1 << 63), (1 << 63) - 1
+    for j, k in enumerate(sk.tolist()):
+        for i in rows.get(k, []):
+            c += 1
+            s += int(rp[i]) * int(sp[j])
+            x += i ^ j
+            mx = max(mx, k)
+            mn = min(mn, i)
+    assert oracle.join_agg_i64(rk, rp, sk, sp, aggs) == [c, s, x, mx, mn]
+    b, p = oracle.join_pairs_i64(rk, sk)
+    assert len(b) == c and all(rk[bi] == sk[pi] for bi, pi in zip(b.tolist(), p.tolist()))
+    k32 = rng.integers(-5000, 5000, 4000).astype(np.int32)
+    q32 = rng.integers(-6000, 6000, 9000).astype(np.int32)
+    p32 = rng.integers(-100, 100, 4000).astype(np.int32)
+    s32 = rng.integers(-100, 100, 9000).astype(np.int32)
+    assert oracle.join_agg_i64(k32.astype(np.int64), p32, q32.astype(np.int64), s32, aggs) == \
+        oracle.join_agg(k32, p32, q32, s32, aggs)
+    # the placement hash is murmur3's 64-bit finaliser
+    assert oracle.lib().orc_hash_int64(1) == 0xB456BCFC34C2CB2C
