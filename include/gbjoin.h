@@ -401,9 +401,12 @@ int gbj_select_range(gbj_ctx *ctx, const int32_t *d_col, uint64_t n,
  * tests/inputs/plans/gpu-ssb/ *.json, have this shape).  Here every query of
  * a batch shares one read of the fact columns.
  *
- * Dimension row i has primary key key_base + i (dense keys, as the
- * reference's SSB dimensions have); a fact foreign key outside
- * [key_base, key_base + n) matches nothing.  Group keys must come from
+ * A dimension's primary keys are dense (d_keys NULL: row i has key
+ * key_base + i, and a fact foreign key outside [key_base, key_base + n)
+ * matches nothing) or a column of distinct int32 values (d_keys, e.g. the
+ * SSB date dimension's yyyymmdd keys), which the plan places in an
+ * open-addressing table at creation; a duplicate primary key fails the
+ * plan with GBJ_ERR_INVALID.  Group keys must come from
  * joined dimensions and their declared [attr_min, attr_max] domains must
  * multiply to at most GBJ_STAR_MAX_GROUPS groups; a value outside its
  * declared domain is reported as GBJ_ERR_INVALID at gbj_sync.
@@ -426,6 +429,7 @@ typedef struct gbj_star_dim {
   int32_t attr_type[GBJ_STAR_MAX_ATTRS];   /* gbj_attr_type               */
   int32_t attr_min[GBJ_STAR_MAX_ATTRS];    /* value domain (group keys)   */
   int32_t attr_max[GBJ_STAR_MAX_ATTRS];
+  const int32_t *d_keys;                   /* primary keys, NULL = dense  */
 } gbj_star_dim;
 
 typedef struct gbj_star_fact {

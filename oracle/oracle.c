@@ -1117,7 +1117,7 @@ int64_t orc_star_query(const int32_t *const *fk, int32_t n_dims, const int32_t *
         const int32_t v = star_attr(dd, pa, r);
         if (v < q->pred_lo[d] || v > q->pred_hi[d]) continue; /* Select */
       }
-      bkeys[d][m] = dd->key_base + (int32_t)r;
+      bkeys[d][m] = dd->keys ? dd->keys[r] : dd->key_base + (int32_t)r;
       brows[d][m] = (int32_t)r;
       ++m;
     }

@@ -145,6 +145,7 @@ typedef struct orc_star_dim {
   int32_t attr_type[4]; /* 0 int32, 1 int8 */
   int32_t attr_min[4];  /* unused by the oracle (same layout as gbjoin.h) */
   int32_t attr_max[4];
+  const int32_t *keys;  /* primary key of each row; 0: key_base + row    */
 } orc_star_dim;
 
 typedef struct orc_star_q {

@@ -343,7 +343,7 @@ def join_groupby(bk, bg, pk, pv, threads=1):
 
 class StarDim(C.Structure):
     _fields_ = [("n", u64), ("key_base", i32), ("n_attrs", i32), ("attr", vp * 4),
-                ("attr_type", i32 * 4), ("attr_min", i32 * 4), ("attr_max", i32 * 4)]
+                ("attr_type", i32 * 4), ("attr_min", i32 * 4), ("attr_max", i32 * 4), ("keys", vp)]
 
 
 class StarQ(C.Structure):
@@ -364,6 +364,8 @@ def star_query(data, query, threads=1, rows=None):
     dims = (StarDim * 4)()
     for d, dim in enumerate(data.dims):
         dims[d].n, dims[d].key_base, dims[d].n_attrs = dim.n, 1, len(dim.attrs)
+        if dim.keys is not None:
+            dims[d].keys = dim.keys.ctypes.data
         for a, col in enumerate(dim.attrs):
             dims[d].attr[a] = col.ctypes.data
             dims[d].attr_type[a] = 1 if col.dtype == np.int8 else 0

@@ -46,7 +46,8 @@ ATTR_I32, ATTR_I8 = 0, 1
 class StarDim(C.Structure):
     _fields_ = [("n", C.c_uint64), ("key_base", C.c_int32), ("n_attrs", C.c_int32),
                 ("d_attr", C.c_void_p * STAR_MAX_ATTRS), ("attr_type", C.c_int32 * STAR_MAX_ATTRS),
-                ("attr_min", C.c_int32 * STAR_MAX_ATTRS), ("attr_max", C.c_int32 * STAR_MAX_ATTRS)]
+                ("attr_min", C.c_int32 * STAR_MAX_ATTRS), ("attr_max", C.c_int32 * STAR_MAX_ATTRS),
+                ("d_keys", C.c_void_p)]
 
 
 class StarFact(C.Structure):

@@ -14,6 +14,10 @@
 //    does not join this dimension).  Dense primary keys make the join a
 //    direct index, so the "hash table" of a dimension is this mask array
 //    (8 B per row, ~19 MB for the workload's four dimensions: L2-resident).
+//    A dimension with explicit keys (yyyymmdd dates) gets an open-addressing
+//    table at plan creation -- slot keys, the row of each slot and the slot
+//    of each row -- and its masks are stored per slot, so a lookup probes
+//    the slot keys and reads the mask beside the match.
 //  * k_star_fact: a persistent grid streams the fact columns with 128-bit
 //    loads (4 rows per thread), gathers the masks of the row's foreign keys
 //    most-selective dimension first, and stops at the first zero AND; the
@@ -47,8 +51,24 @@ struct DimDev {
   uint32_t n;
   int32_t base;
   uint64_t row0;   // first row of this dimension in the concatenated mask pass
-  uint64_t *mask;  // [n]
+  uint64_t *mask;  // [n] (dense keys) or [ents] (explicit keys)
   int32_t smem_off;  // offset of the mask copy in the fact kernel's shared memory, -1 none
+  // Explicit keys: kind 1, a range index over [kmin, kmin + 32 * aux_words / 2)
+  // -- aux holds one {bitmap word, keys before it} pair per 32 values, and a
+  // key's entry is its rank among the keys; kind 2, a hash table -- aux holds
+  // the slot keys of `slots` slots (home slot fmix32(key) scaled to [0,
+  // slots)), empty slots hold `empty` (a value no key has).  Masks are per
+  // entry; ent_row[entry] and row_ent[row] link entries and rows.
+  int32_t kind;  // 0 dense keys
+  const int32_t *aux;
+  uint32_t aux_words;  // 4-byte words of aux
+  const int32_t *ent_row;
+  const int32_t *row_ent;
+  uint32_t ents;
+  uint32_t slots;
+  int32_t empty;
+  int32_t kmin;
+  int32_t smem_koff;  // offset of aux in the fact kernel's shared aux copy, -1 none
 };
 
 struct Dims {
@@ -126,8 +146,41 @@ __global__ void __launch_bounds__(256) k_star_mask(const Desc *__restrict__ desc
       const bool keep = !((s_join[q] >> d) & 1u) || pa < 0 || (x >= s_lo[q][d] && x <= s_hi[q][d]);
       m |= (uint64_t)keep << q;
     }
-    dd.mask[r] = m;
+    dd.mask[dd.kind ? (uint32_t)dd.row_ent[r] : r] = m;
   }
+}
+
+// Entry of key k in a dimension with explicit keys (aux from shared or
+// global memory), -1 when absent.
+__device__ __forceinline__ int32_t keyed_ent(const DimDev &dd, const int32_t *aux, int32_t k) {
+  if (dd.kind == 1) {
+    const int64_t idx = (int64_t)k - dd.kmin;
+    if (idx < 0 || idx >= (int64_t)dd.aux_words * 16) return -1;
+    const uint2 e = reinterpret_cast<const uint2 *>(aux)[idx >> 5];
+    const uint32_t b = (uint32_t)idx & 31u;
+    if (!((e.x >> b) & 1u)) return -1;
+    return (int32_t)(e.y + __popc(e.x & ((1u << b) - 1u)));
+  }
+  if (k == dd.empty) return -1;  // no key has the empty-slot value
+  uint32_t h = __umulhi(gbjd::fmix32((uint32_t)k), dd.slots);
+  for (uint32_t step = 0; step < dd.slots; ++step) {
+    const int32_t x = aux[h];
+    if (x == k) return (int32_t)h;
+    if (x == dd.empty) return -1;
+    h = h + 1 == dd.slots ? 0 : h + 1;
+  }
+  return -1;
+}
+
+// Row of key k (-1 when absent): dense or explicit keys (aux from shared
+// memory when staged there).
+__device__ __forceinline__ int64_t dim_row(const DimDev &dd, const int32_t *s_aux, int32_t k) {
+  if (dd.kind) {
+    const int32_t e = keyed_ent(dd, dd.smem_off >= 0 ? s_aux + dd.smem_koff : dd.aux, k);
+    return e < 0 ? -1 : __ldg(dd.ent_row + e);
+  }
+  const uint32_t idx = (uint32_t)(k - dd.base);
+  return idx < dd.n ? (int64_t)idx : -1;
 }
 
 struct GroupSpec {
@@ -137,12 +190,18 @@ struct GroupSpec {
 
 // The (row, query) matches of one fact row: COUNT and SUM(price * quantity)
 // into the query's dense group arrays.
-__device__ __forceinline__ void star_matches(const Dims &dims, uint64_t m, const GroupSpec *sg,
+template <bool kKeyed>
+__device__ __forceinline__ void star_matches(const Dims &dims, const int32_t *s_keys, uint64_t m,
+                                             const GroupSpec *sg,
                                              const int32_t (&fk)[kMaxDims], int32_t qty,
                                              int32_t price, unsigned long long *__restrict__ gcnt,
                                              unsigned long long *__restrict__ gsum,
                                              uint32_t *status) {
   const unsigned long long val = (unsigned long long)((int64_t)price * (int64_t)qty);
+  // the row of the last hashed dimension looked up (the fact row's key of a
+  // dimension is the same for every query)
+  int hd = -1;
+  uint32_t hrow = 0;
   while (m) {
     const int q = __ffsll((long long)m) - 1;
     m &= m - 1;
@@ -153,7 +212,18 @@ __device__ __forceinline__ void star_matches(const Dims &dims, uint64_t m, const
       const int d = gs.gd[s];
       const int32_t k = d == 0 ? fk[0] : d == 1 ? fk[1] : d == 2 ? fk[2] : fk[3];
       const DimDev &dd = dims.d[d];
-      key[s] = attr_at(dd, gs.ga[s], (uint32_t)(k - dd.base));
+      // a joined dimension passed the row, so its key is present
+      uint32_t row;
+      if (kKeyed && dd.kind) {
+        if (hd != d) {
+          hrow = (uint32_t)dim_row(dd, s_keys, k);
+          hd = d;
+        }
+        row = hrow;
+      } else {
+        row = (uint32_t)(k - dd.base);
+      }
+      key[s] = attr_at(dd, gs.ga[s], row);
     }
     const uint32_t a = (uint32_t)(key[0] - gs.gmin[0]), b = (uint32_t)(key[1] - gs.gmin[1]);
     if (a >= gs.gspan[0] || b >= gs.gspan[1]) {
@@ -169,8 +239,18 @@ __device__ __forceinline__ void star_matches(const Dims &dims, uint64_t m, const
 // Mask of dimension d for foreign key k: from shared memory for small
 // dimensions, else an L2 gather; keys outside the dimension pass only the
 // queries that do not join it.
-__device__ __forceinline__ uint64_t dim_mask(const DimDev &dd, const uint64_t *s_mask, int32_t k,
-                                             uint64_t nojoin) {
+__device__ __forceinline__ uint64_t keyed_mask(const DimDev &dd, const uint64_t *s_mask, const int32_t *s_aux,
+                                              int32_t k, uint64_t nojoin) {
+  const bool sm = dd.smem_off >= 0;
+  const int32_t e = keyed_ent(dd, sm ? s_aux + dd.smem_koff : dd.aux, k);
+  if (e < 0) return nojoin;
+  return sm ? s_mask[dd.smem_off + e] : __ldg(dd.mask + e);
+}
+
+template <bool kKeyed>
+__device__ __forceinline__ uint64_t dim_mask(const DimDev &dd, const uint64_t *s_mask, const int32_t *s_keys,
+                                             int32_t k, uint64_t nojoin) {
+  if (kKeyed && dd.kind) return keyed_mask(dd, s_mask, s_keys, k, nojoin);
   const uint32_t idx = (uint32_t)(k - dd.base);
   if (idx >= dd.n) return nojoin;
   return dd.smem_off >= 0 ? s_mask[dd.smem_off + idx] : __ldg(dd.mask + idx);
@@ -180,12 +260,13 @@ __device__ __forceinline__ uint64_t dim_mask(const DimDev &dd, const uint64_t *s
 // column) and issues every mask lookup of the 4 rows before combining them,
 // so a thread keeps up to 16 independent gathers in flight instead of
 // walking dimensions one dependent load at a time.
-template <bool kVec>
+template <bool kVec, bool kKeyed>
 __global__ void __launch_bounds__(kFactThreads)
-    k_star_fact(const Desc *__restrict__ desc, FactDev f, Dims dims,
+    k_star_fact(const Desc *__restrict__ desc, FactDev f, Dims dims, uint32_t smem_masks,
                 unsigned long long *__restrict__ gcnt, unsigned long long *__restrict__ gsum,
                 uint32_t *status) {
-  extern __shared__ uint64_t s_mask[];  // masks of the small dimensions
+  extern __shared__ uint64_t s_mask[];  // masks of the small dimensions, then slot keys of hashed ones
+  int32_t *s_keys = reinterpret_cast<int32_t *>(s_mask + smem_masks);
   __shared__ GroupSpec sg[kMaxQ];
   __shared__ uint64_t s_nojoin[kMaxDims];
   const int nq = desc->nq;
@@ -206,9 +287,13 @@ __global__ void __launch_bounds__(kFactThreads)
   }
 #pragma unroll
   for (int d = 0; d < kMaxDims; ++d) {
-    if (d < dims.nd && dims.d[d].smem_off >= 0)
-      for (uint32_t i = threadIdx.x; i < dims.d[d].n; i += blockDim.x)
-        s_mask[dims.d[d].smem_off + i] = dims.d[d].mask[i];
+    if (d < dims.nd && dims.d[d].smem_off >= 0) {
+      const DimDev &dd = dims.d[d];
+      const uint32_t cnt = kKeyed && dd.kind ? dd.ents : dd.n;
+      for (uint32_t i = threadIdx.x; i < cnt; i += blockDim.x) s_mask[dd.smem_off + i] = dd.mask[i];
+      if (kKeyed && dd.kind)
+        for (uint32_t i = threadIdx.x; i < dd.aux_words; i += blockDim.x) s_keys[dd.smem_koff + i] = dd.aux[i];
+    }
   }
   __syncthreads();
   uint64_t nojoin[kMaxDims];
@@ -230,39 +315,57 @@ __global__ void __launch_bounds__(kFactThreads)
       uint64_t m[4] = {active, active, active, active};
 #pragma unroll
       for (int d = 0; d < kMaxDims; ++d) {
-        if (d < dims.nd && d != dims.late) {
-          m[0] &= dim_mask(dims.d[d], s_mask, k4[d].x, nojoin[d]);
-          m[1] &= dim_mask(dims.d[d], s_mask, k4[d].y, nojoin[d]);
-          m[2] &= dim_mask(dims.d[d], s_mask, k4[d].z, nojoin[d]);
-          m[3] &= dim_mask(dims.d[d], s_mask, k4[d].w, nojoin[d]);
+        if (d < dims.nd && d != dims.late && (!kKeyed || dims.d[d].kind != 2)) {
+          m[0] &= dim_mask<kKeyed>(dims.d[d], s_mask, s_keys, k4[d].x, nojoin[d]);
+          m[1] &= dim_mask<kKeyed>(dims.d[d], s_mask, s_keys, k4[d].y, nojoin[d]);
+          m[2] &= dim_mask<kKeyed>(dims.d[d], s_mask, s_keys, k4[d].z, nojoin[d]);
+          m[3] &= dim_mask<kKeyed>(dims.d[d], s_mask, s_keys, k4[d].w, nojoin[d]);
         }
       }
-      // the largest gathered dimension last, only for rows some query still
-      // passes (most rows have failed every query by then)
+      // hash-table dimensions (a probe loop each), then the largest gathered
+      // dimension, only for rows some query still passes (most rows have
+      // failed every query by then).  The hash probes run in a loop over the
+      // four rows that is not unrolled, so the kernel carries one copy.
 #pragma unroll
       for (int d = 0; d < kMaxDims; ++d) {
-        if (d < dims.nd && d == dims.late) {
-          if (m[0]) m[0] &= dim_mask(dims.d[d], s_mask, k4[d].x, nojoin[d]);
-          if (m[1]) m[1] &= dim_mask(dims.d[d], s_mask, k4[d].y, nojoin[d]);
-          if (m[2]) m[2] &= dim_mask(dims.d[d], s_mask, k4[d].z, nojoin[d]);
-          if (m[3]) m[3] &= dim_mask(dims.d[d], s_mask, k4[d].w, nojoin[d]);
+        if (kKeyed && d < dims.nd && dims.d[d].kind == 2) {
+#pragma unroll 1
+          for (int r = 0; r < 4; ++r) {
+            const uint64_t mr = r == 0 ? m[0] : r == 1 ? m[1] : r == 2 ? m[2] : m[3];
+            if (!mr) continue;
+            const int32_t k = r == 0 ? k4[d].x : r == 1 ? k4[d].y : r == 2 ? k4[d].z : k4[d].w;
+            const uint64_t v = mr & keyed_mask(dims.d[d], s_mask, s_keys, k, nojoin[d]);
+            m[0] = r == 0 ? v : m[0];
+            m[1] = r == 1 ? v : m[1];
+            m[2] = r == 2 ? v : m[2];
+            m[3] = r == 3 ? v : m[3];
+          }
+        }
+      }
+#pragma unroll
+      for (int d = 0; d < kMaxDims; ++d) {
+        if (d < dims.nd && d == dims.late && (!kKeyed || !dims.d[d].kind)) {
+          if (m[0]) m[0] &= dim_mask<kKeyed>(dims.d[d], s_mask, s_keys, k4[d].x, nojoin[d]);
+          if (m[1]) m[1] &= dim_mask<kKeyed>(dims.d[d], s_mask, s_keys, k4[d].y, nojoin[d]);
+          if (m[2]) m[2] &= dim_mask<kKeyed>(dims.d[d], s_mask, s_keys, k4[d].z, nojoin[d]);
+          if (m[3]) m[3] &= dim_mask<kKeyed>(dims.d[d], s_mask, s_keys, k4[d].w, nojoin[d]);
         }
       }
       if (m[0]) {
         const int32_t fk[kMaxDims] = {k4[0].x, k4[1].x, k4[2].x, k4[3].x};
-        star_matches(dims, m[0], sg, fk, q4.x, p4.x, gcnt, gsum, status);
+        star_matches<kKeyed>(dims, s_keys, m[0], sg, fk, q4.x, p4.x, gcnt, gsum, status);
       }
       if (m[1]) {
         const int32_t fk[kMaxDims] = {k4[0].y, k4[1].y, k4[2].y, k4[3].y};
-        star_matches(dims, m[1], sg, fk, q4.y, p4.y, gcnt, gsum, status);
+        star_matches<kKeyed>(dims, s_keys, m[1], sg, fk, q4.y, p4.y, gcnt, gsum, status);
       }
       if (m[2]) {
         const int32_t fk[kMaxDims] = {k4[0].z, k4[1].z, k4[2].z, k4[3].z};
-        star_matches(dims, m[2], sg, fk, q4.z, p4.z, gcnt, gsum, status);
+        star_matches<kKeyed>(dims, s_keys, m[2], sg, fk, q4.z, p4.z, gcnt, gsum, status);
       }
       if (m[3]) {
         const int32_t fk[kMaxDims] = {k4[0].w, k4[1].w, k4[2].w, k4[3].w};
-        star_matches(dims, m[3], sg, fk, q4.w, p4.w, gcnt, gsum, status);
+        star_matches<kKeyed>(dims, s_keys, m[3], sg, fk, q4.w, p4.w, gcnt, gsum, status);
       }
     }
     done = n4 * 4;
@@ -273,9 +376,9 @@ __global__ void __launch_bounds__(kFactThreads)
 #pragma unroll
     for (int d = 0; d < kMaxDims; ++d) {
       fk[d] = d < dims.nd ? f.fk[d][r] : 0;
-      if (d < dims.nd) m &= dim_mask(dims.d[d], s_mask, fk[d], nojoin[d]);
+      if (d < dims.nd) m &= dim_mask<kKeyed>(dims.d[d], s_mask, s_keys, fk[d], nojoin[d]);
     }
-    if (m) star_matches(dims, m, sg, fk, f.qty[r], f.price[r], gcnt, gsum, status);
+    if (m) star_matches<kKeyed>(dims, s_keys, m, sg, fk, f.qty[r], f.price[r], gcnt, gsum, status);
   }
 }
 
@@ -337,6 +440,112 @@ __global__ void __launch_bounds__(kEmitThreads)
   if (threadIdx.x == 0) *qd.out_n = total;
 }
 
+// Smallest and largest key of a hashed dimension (mm = {INT32_MAX, INT32_MIN}
+// on entry).
+__global__ void k_star_key_range(const int32_t *__restrict__ keys, uint64_t n, int32_t *mm) {
+  int32_t lo = INT32_MAX, hi = INT32_MIN;
+  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+    lo = min(lo, keys[i]);
+    hi = max(hi, keys[i]);
+  }
+  lo = __reduce_min_sync(0xffffffffu, lo);
+  hi = __reduce_max_sync(0xffffffffu, hi);
+  if ((threadIdx.x & 31) == 0) {
+    atomicMin(&mm[0], lo);
+    atomicMax(&mm[1], hi);
+  }
+}
+
+__global__ void k_star_fill(int32_t *__restrict__ a, uint64_t n, int32_t v) {
+  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x)
+    a[i] = v;
+}
+
+// Places every row of a hashed dimension (linear probing from fmix32(key));
+// a key met twice latches GBJ_DEV_INVALID.
+__global__ void k_star_hash_build(const int32_t *__restrict__ keys, uint32_t n, int32_t *__restrict__ hkeys,
+                                  uint32_t slots, int32_t empty, int32_t *__restrict__ ent_row,
+                                  int32_t *__restrict__ row_ent, uint32_t *status) {
+  for (uint32_t r = blockIdx.x * blockDim.x + threadIdx.x; r < n; r += gridDim.x * blockDim.x) {
+    const int32_t k = keys[r];
+    uint32_t h = __umulhi(gbjd::fmix32((uint32_t)k), slots);
+    bool placed = false;
+    for (uint32_t step = 0; step < slots; ++step) {
+      const int32_t old = atomicCAS(&hkeys[h], empty, k);
+      if (old == empty) {
+        ent_row[h] = (int32_t)r;
+        row_ent[r] = (int32_t)h;
+        placed = true;
+        break;
+      }
+      if (old == k) {
+        gbjd::latch(status, GBJ_DEV_INVALID);
+        placed = true;
+        break;
+      }
+      h = h + 1 == slots ? 0 : h + 1;
+    }
+    if (!placed) gbjd::latch(status, GBJ_DEV_CAPACITY);
+  }
+}
+
+// Range index, step 1: the bitmap (aux[2 w] = bits of values 32 w ..
+// 32 w + 31 above kmin); a key met twice latches GBJ_DEV_INVALID.
+__global__ void k_star_range_bits(const int32_t *__restrict__ keys, uint32_t n, int32_t kmin,
+                                  uint32_t *__restrict__ aux, uint32_t *status) {
+  for (uint32_t r = blockIdx.x * blockDim.x + threadIdx.x; r < n; r += gridDim.x * blockDim.x) {
+    const uint32_t idx = (uint32_t)((int64_t)keys[r] - kmin);
+    const uint32_t bit = 1u << (idx & 31u);
+    if (atomicOr(&aux[2 * (idx >> 5)], bit) & bit) gbjd::latch(status, GBJ_DEV_INVALID);
+  }
+}
+
+// Step 2 (one CTA of 1024 threads): aux[2 w + 1] = keys in words before w.
+__global__ void __launch_bounds__(1024) k_star_range_rank(uint32_t *__restrict__ aux, uint32_t words) {
+  __shared__ uint32_t s_warp[32];
+  const uint32_t chunk = (words + 1023) / 1024;
+  const uint32_t lo = min(words, threadIdx.x * chunk), hi = min(words, lo + chunk);
+  uint32_t mine = 0;
+  for (uint32_t w = lo; w < hi; ++w) mine += __popc(aux[2 * w]);
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  uint32_t incl = mine;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+    if (lane >= o) incl += y;
+  }
+  if (lane == 31) s_warp[warp] = incl;
+  __syncthreads();
+  if (warp == 0) {
+    uint32_t v = s_warp[lane];
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t y = __shfl_up_sync(0xffffffffu, v, o);
+      if (lane >= o) v += y;
+    }
+    s_warp[lane] = v;
+  }
+  __syncthreads();
+  uint32_t run = (warp ? s_warp[warp - 1] : 0) + incl - mine;
+  for (uint32_t w = lo; w < hi; ++w) {
+    aux[2 * w + 1] = run;
+    run += __popc(aux[2 * w]);
+  }
+}
+
+// Step 3: entries (ranks) of the rows, both ways.
+__global__ void k_star_range_ent(const int32_t *__restrict__ keys, uint32_t n, int32_t kmin,
+                                 const uint32_t *__restrict__ aux, int32_t *__restrict__ ent_row,
+                                 int32_t *__restrict__ row_ent) {
+  for (uint32_t r = blockIdx.x * blockDim.x + threadIdx.x; r < n; r += gridDim.x * blockDim.x) {
+    const uint32_t idx = (uint32_t)((int64_t)keys[r] - kmin);
+    const uint32_t w = idx >> 5, b = idx & 31u;
+    const int32_t e = (int32_t)(aux[2 * w + 1] + __popc(aux[2 * w] & ((1u << b) - 1u)));
+    ent_row[e] = (int32_t)r;
+    row_ent[r] = e;
+  }
+}
+
 }  // namespace
 
 struct gbj_star_plan {
@@ -346,7 +555,10 @@ struct gbj_star_plan {
   gbj_star_dim host_dims[kMaxDims]{};
   bool vec = false;
   uint64_t *masks = nullptr;
+  int32_t *hash_mem = nullptr;  // slot keys, slot rows and row slots of hashed dimensions
   size_t fact_smem = 0;
+  uint32_t smem_masks = 0;      // 8-byte masks staged in shared memory (index words follow)
+  bool keyed = false;           // some dimension has explicit keys
   unsigned long long *gcnt = nullptr, *gsum = nullptr;
   Desc *d_desc = nullptr;
   Desc *h_desc[2] = {nullptr, nullptr};  // pinned
@@ -442,12 +654,10 @@ int star_enqueue(gbj_star_plan *p, int slot, cudaStream_t s, bool capturing) {
       1, std::min<uint64_t>((rows + 255) / 256, (uint64_t)ctx->sm_count * 8));
   k_star_mask<<<mask_grid, 256, 0, s>>>(p->d_desc, p->dims);
   GBJ_TRY(star_launched(ctx, "k_star_mask", s, capturing));
-  if (p->vec)
-    k_star_fact<true><<<p->fact_grid, kFactThreads, p->fact_smem, s>>>(p->d_desc, p->fact, p->dims,
-                                                                       p->gcnt, p->gsum, ctx->d_status);
-  else
-    k_star_fact<false><<<p->fact_grid, kFactThreads, p->fact_smem, s>>>(p->d_desc, p->fact, p->dims,
-                                                                        p->gcnt, p->gsum, ctx->d_status);
+  auto fact = p->vec ? (p->keyed ? k_star_fact<true, true> : k_star_fact<true, false>)
+                     : (p->keyed ? k_star_fact<false, true> : k_star_fact<false, false>);
+  fact<<<p->fact_grid, kFactThreads, p->fact_smem, s>>>(p->d_desc, p->fact, p->dims, p->smem_masks, p->gcnt,
+                                                        p->gsum, ctx->d_status);
   GBJ_TRY(star_launched(ctx, "k_star_fact", s, capturing));
   k_star_emit<<<kMaxQ, kEmitThreads, 0, s>>>(p->d_desc, p->gcnt, p->gsum, ctx->d_status);
   return star_launched(ctx, "k_star_emit", s, capturing);
@@ -472,7 +682,7 @@ extern "C" int gbj_star_plan_create(gbj_ctx *ctx, const gbj_star_fact *fact,
   bool aligned = (reinterpret_cast<uintptr_t>(fact->d_quantity) % 16 == 0) &&
                  (reinterpret_cast<uintptr_t>(fact->d_price) % 16 == 0);
   p->dims.nd = fact->n_dims;
-  uint64_t rows = 0;
+  uint64_t rows = 0, masks_total = 0, mask_slots[kMaxDims] = {0, 0, 0, 0};
   auto fail = [&](int rc) {
     gbj_star_plan_destroy(p);
     return rc;
@@ -499,30 +709,155 @@ extern "C" int gbj_star_plan_create(gbj_ctx *ctx, const gbj_star_fact *fact,
     dd.base = hd.key_base;
     dd.row0 = rows;
     rows += hd.n;
-    dd.smem_off = -1;
-    if (hd.n <= kSmemMaskRows && p->fact_smem / sizeof(uint64_t) + hd.n <= kSmemMaskMax) {
-      dd.smem_off = (int32_t)(p->fact_smem / sizeof(uint64_t));
-      p->fact_smem += hd.n * sizeof(uint64_t);
-    }
+    dd.smem_off = dd.smem_koff = -1;
+    dd.kind = 0;
+    dd.aux = nullptr;
   }
   p->dims.total_rows = rows;
+  cudaStream_t s = ctx->stream;
+  int rc = GBJ_OK;
+  // explicit keys: the key range picks the index -- a range index when the
+  // keys fill at least 1/64 of their range (dates: 2,557 of 61,131 values),
+  // else a hash table at load factor <= 3/4 (slots a multiple of 32) -- and
+  // gives the hash table's empty-slot value
+  int32_t *mm = nullptr;
+  for (int d = 0; d < fact->n_dims; ++d) {
+    const gbj_star_dim &hd = dims[d];
+    if (!hd.d_keys) {
+      mask_slots[d] = hd.n;
+      masks_total += hd.n;
+      continue;
+    }
+    if (!mm) {
+      rc = pool_alloc(ctx, 4 * sizeof(int32_t), s, reinterpret_cast<void **>(&mm));
+      if (rc) return fail(rc);
+    }
+    const int32_t init[2] = {INT32_MAX, INT32_MIN};
+    int32_t got[2];
+    cudaError_t e = cudaMemcpyAsync(mm, init, sizeof(init), cudaMemcpyHostToDevice, s);
+    if (e != cudaSuccess) return fail(cuda_error(ctx, e, "star: key range"));
+    const unsigned g = (unsigned)std::min<uint64_t>((hd.n + 255) / 256, (uint64_t)ctx->sm_count * 4);
+    k_star_key_range<<<g, 256, 0, s>>>(hd.d_keys, hd.n, mm);
+    rc = after_launch(ctx, "k_star_key_range", s);
+    if (rc) return fail(rc);
+    e = cudaMemcpyAsync(got, mm, sizeof(got), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) return fail(cuda_error(ctx, e, "star: key range"));
+    DimDev &dd = p->dims.d[d];
+    const int64_t range = (int64_t)got[1] - got[0] + 1;
+    dd.kmin = got[0];
+    if (range <= 64 * (int64_t)hd.n && range <= (1ll << 26)) {
+      dd.kind = 1;
+      dd.aux_words = (uint32_t)(2 * ((range + 31) / 32));
+      dd.ents = (uint32_t)hd.n;
+    } else {
+      if (got[0] != INT32_MIN) dd.empty = got[0] - 1;
+      else if (got[1] != INT32_MAX) dd.empty = got[1] + 1;
+      else return fail(set_error(ctx, GBJ_ERR_UNSUPPORTED, "star: dimension keys span the whole int32 range"));
+      dd.kind = 2;
+      dd.slots = (uint32_t)std::max<uint64_t>(64, ((4 * hd.n + 2) / 3 + 31) / 32 * 32);
+      dd.aux_words = dd.slots;
+      dd.ents = dd.slots;
+    }
+    mask_slots[d] = dd.ents;
+    masks_total += dd.ents;
+    p->keyed = true;
+  }
+  if (mm) pool_release(ctx, mm, s);
+  // small dimensions' masks (and index words) go to the fact kernel's shared
+  // memory, within kSmemMaskMax * 8 bytes
+  {
+    uint64_t mask_units = 0, key_units = 0;
+    for (int d = 0; d < fact->n_dims; ++d) {
+      DimDev &dd = p->dims.d[d];
+      const uint64_t m = mask_slots[d];
+      const uint64_t ku = dd.kind ? ((key_units + 1) & ~1ull) + dd.aux_words : key_units;  // range pairs 8-aligned
+      if (m > kSmemMaskRows) continue;
+      if ((mask_units + m) * 8 + ku * 4 > (uint64_t)kSmemMaskMax * 8) continue;
+      dd.smem_off = (int32_t)mask_units;
+      mask_units += m;
+      if (dd.kind) {
+        dd.smem_koff = (int32_t)(ku - dd.aux_words);
+        key_units = ku;
+      }
+    }
+    p->smem_masks = (uint32_t)mask_units;
+    p->fact_smem = mask_units * 8 + key_units * 4;
+  }
   // the late dimension: the largest one gathered from L2, when another
   // gathered dimension is checked before it
   p->dims.late = -1;
   {
     int gathered = 0, big = -1;
     for (int d = 0; d < fact->n_dims; ++d) {
-      if (p->dims.d[d].smem_off >= 0) continue;
+      if (p->dims.d[d].smem_off >= 0 || p->dims.d[d].kind) continue;
       ++gathered;
       if (big < 0 || p->dims.d[d].n > p->dims.d[big].n) big = d;
     }
     if (gathered >= 2) p->dims.late = big;
   }
   p->vec = aligned;
-  cudaStream_t s = ctx->stream;
-  int rc = pool_alloc(ctx, rows * sizeof(uint64_t) + 16, s, reinterpret_cast<void **>(&p->masks));
+  rc = pool_alloc(ctx, masks_total * sizeof(uint64_t) + 16, s, reinterpret_cast<void **>(&p->masks));
   if (rc) return fail(rc);
-  for (int d = 0; d < fact->n_dims; ++d) p->dims.d[d].mask = p->masks + p->dims.d[d].row0;
+  {
+    uint64_t off = 0;
+    for (int d = 0; d < fact->n_dims; ++d) {
+      p->dims.d[d].mask = p->masks + off;
+      off += mask_slots[d];
+    }
+  }
+  // the indexes of explicit keys: aux words, entry rows, row entries
+  uint64_t words = 0;
+  for (int d = 0; d < fact->n_dims; ++d)
+    if (p->dims.d[d].kind)
+      words += ((((uint64_t)p->dims.d[d].aux_words + 1) / 2 * 2 + p->dims.d[d].ents + dims[d].n) + 1) / 2 * 2;
+  if (words) {
+    rc = pool_alloc(ctx, words * sizeof(int32_t) + 16, s, reinterpret_cast<void **>(&p->hash_mem));
+    if (rc) return fail(rc);
+    uint64_t off = 0;
+    for (int d = 0; d < fact->n_dims; ++d) {
+      const gbj_star_dim &hd = dims[d];
+      DimDev &dd = p->dims.d[d];
+      if (!dd.kind) continue;
+      int32_t *aux = p->hash_mem + off;  // 8-byte aligned: every block is an even number of words
+      int32_t *erow = aux + (dd.aux_words + 1) / 2 * 2, *rent = erow + dd.ents;
+      off += (dd.aux_words + 1) / 2 * 2 + dd.ents + hd.n;
+      if (off % 2) ++off;
+      const unsigned g = (unsigned)std::min<uint64_t>((hd.n + 255) / 256, (uint64_t)ctx->sm_count * 4);
+      if (dd.kind == 1) {
+        GBJ_CHECK_CUDA(ctx, cudaMemsetAsync(aux, 0, sizeof(int32_t) * dd.aux_words, s));
+        k_star_range_bits<<<g, 256, 0, s>>>(hd.d_keys, (uint32_t)hd.n, dd.kmin, reinterpret_cast<uint32_t *>(aux),
+                                            ctx->d_status);
+        rc = after_launch(ctx, "k_star_range_bits", s);
+        if (rc) return fail(rc);
+        k_star_range_rank<<<1, 1024, 0, s>>>(reinterpret_cast<uint32_t *>(aux), dd.aux_words / 2);
+        rc = after_launch(ctx, "k_star_range_rank", s);
+        if (rc) return fail(rc);
+        k_star_range_ent<<<g, 256, 0, s>>>(hd.d_keys, (uint32_t)hd.n, dd.kmin,
+                                           reinterpret_cast<const uint32_t *>(aux), erow, rent);
+        rc = after_launch(ctx, "k_star_range_ent", s);
+        if (rc) return fail(rc);
+      } else {
+        k_star_fill<<<(unsigned)std::min<uint64_t>((dd.slots + 255) / 256, 4096), 256, 0, s>>>(aux, dd.slots,
+                                                                                               dd.empty);
+        rc = after_launch(ctx, "k_star_fill", s);
+        if (rc) return fail(rc);
+        k_star_hash_build<<<g, 256, 0, s>>>(hd.d_keys, (uint32_t)hd.n, aux, dd.slots, dd.empty, erow, rent,
+                                            ctx->d_status);
+        rc = after_launch(ctx, "k_star_hash_build", s);
+        if (rc) return fail(rc);
+      }
+      dd.aux = aux;
+      dd.ent_row = erow;
+      dd.row_ent = rent;
+    }
+    // a duplicate primary key fails the plan
+    const int src = gbj_sync(ctx, s);
+    if (src != GBJ_OK) {
+      if (src == GBJ_ERR_INVALID) set_error(ctx, GBJ_ERR_INVALID, "star: duplicate primary key in a dimension");
+      return fail(src);
+    }
+  }
   rc = pool_alloc(ctx, sizeof(unsigned long long) * kMaxQ * kMaxGroups * 2, s,
                   reinterpret_cast<void **>(&p->gcnt));
   if (rc) return fail(rc);
@@ -537,8 +872,15 @@ extern "C" int gbj_star_plan_create(gbj_ctx *ctx, const gbj_star_fact *fact,
   }
   cudaError_t e = cudaStreamCreateWithFlags(&p->cap_stream, cudaStreamNonBlocking);
   if (e != cudaSuccess) return fail(cuda_error(ctx, e, "cudaStreamCreate"));
+  // static plus dynamic shared memory may pass 48 KB: opt in
+  for (auto kern : {k_star_fact<true, false>, k_star_fact<false, false>, k_star_fact<true, true>,
+                    k_star_fact<false, true>}) {
+    e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)p->fact_smem);
+    if (e != cudaSuccess) return fail(cuda_error(ctx, e, "star: shared memory attribute"));
+  }
   int per_sm = 1;
-  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_star_fact<true>, kFactThreads, p->fact_smem);
+  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, p->keyed ? k_star_fact<true, true> : k_star_fact<true, false>,
+                                                    kFactThreads, p->fact_smem);
   if (e != cudaSuccess) return fail(cuda_error(ctx, e, "occupancy"));
   p->fact_grid = ctx->sm_count * std::max(per_sm, 1);
   // the allocations above are stream-ordered on the context stream
@@ -603,6 +945,7 @@ extern "C" void gbj_star_plan_destroy(gbj_star_plan *p) {
   }
   if (p->cap_stream) cudaStreamDestroy(p->cap_stream);
   if (p->masks) pool_release(ctx, p->masks, ctx->stream);
+  if (p->hash_mem) pool_release(ctx, p->hash_mem, ctx->stream);
   if (p->gcnt) pool_release(ctx, p->gcnt, ctx->stream);
   if (p->d_desc) pool_release(ctx, p->d_desc, ctx->stream);
   delete p;

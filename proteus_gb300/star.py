@@ -1,11 +1,13 @@
 """Batched star join: the seeded star schema, the query variants and a
 wrapper over the gbj_star_* entry points.
 
-Schema (dimension row i has primary key i + 1; every column is a pure
-function of (seed, column, row)):
+Schema (dimension row i has primary key i + 1, except the date dimension,
+keyed yyyymmdd like SSB's; every column is a pure function of (seed,
+column, row)):
 
   dim 0  customer  2^21 rows  nation int8 0..24, region int8 0..4, city int32 0..249
-  dim 1  date      2557 rows  year int32 1992.., month int8 0..11, week int32 1..53
+  dim 1  date      2557 rows  key yyyymmdd (days from 1992-01-01),
+                              year int32 1992.., month int8 0..11, week int32 1..53
   dim 2  part      2^18 rows  category int8 0..24, mfgr int8 0..4, brand int32 0..999
   dim 3  supplier  2^16 rows  nation int8 0..24, region int8 0..4
   fact   2^28 rows  fk0..fk3 uniform over each dimension's keys,
@@ -56,6 +58,22 @@ class Dim:
     names: list
     lo: list
     hi: list
+    keys: np.ndarray | None = None  # primary keys (int32); None: row i has key i + 1
+
+    def key_of_rows(self, rows: np.ndarray) -> np.ndarray:
+        """Primary keys of 0-based rows."""
+        if self.keys is None:
+            return (rows + 1).astype(np.int32)
+        return self.keys[rows]
+
+
+def yyyymmdd(n: int, start=(1992, 1, 1)) -> np.ndarray:
+    """Keys yyyymmdd of n consecutive days from `start`."""
+    import datetime
+
+    d0 = datetime.date(*start)
+    days = [d0 + datetime.timedelta(days=i) for i in range(n)]
+    return np.array([d.year * 10000 + d.month * 100 + d.day for d in days], dtype=np.int32)
 
 
 @dataclass
@@ -89,13 +107,16 @@ def gen_dims(seed: int, dim_rows=FULL_DIM_ROWS) -> list:
             names.append(an)
             los.append(int(lo))
             his.append(int(hi))
-        dims.append(Dim(name, n, cols, names, los, his))
+        dims.append(Dim(name, n, cols, names, los, his, yyyymmdd(n) if name == "date" else None))
     return dims
 
 
 def gen_star(seed: int, n_fact: int = FULL_FACT_ROWS, dim_rows=FULL_DIM_ROWS, threads=0) -> StarData:
     dims = gen_dims(seed, dim_rows)
     fk = [_uniform(seed, _S_FACT + d, n_fact, 1, dims[d].n, threads) for d in range(len(dims))]
+    for d, dim in enumerate(dims):
+        if dim.keys is not None:  # uniform over the rows, as the keys of those rows
+            fk[d] = np.ascontiguousarray(dim.keys[fk[d] - 1])
     qty = _uniform(seed, _S_FACT + 8, n_fact, 1, 50, threads)
     price = _uniform(seed, _S_FACT + 9, n_fact, 900, 110000, threads)
     return StarData(dims, fk, qty, price)
@@ -164,6 +185,7 @@ class StarPlan:
 
         self.ctx = ctx
         self.dev_dims = [[torch.from_numpy(c).to(device) for c in d.attrs] for d in data.dims]
+        self.dev_keys = [None if d.keys is None else torch.from_numpy(d.keys).to(device) for d in data.dims]
         if fact_tensors is None:
             self.dev_fk = [torch.from_numpy(c).to(device) for c in data.fk]
             self.dev_qty = torch.from_numpy(data.quantity).to(device)
@@ -188,6 +210,8 @@ class StarPlan:
         for d, dim in enumerate(self.dims):
             sd = arr[d]
             sd.n, sd.key_base, sd.n_attrs = dim.n, 1, len(dim.attrs)
+            if self.dev_keys[d] is not None:
+                sd.d_keys = self.dev_keys[d].data_ptr()
             for a, col in enumerate(self.dev_dims[d]):
                 sd.d_attr[a] = col.data_ptr()
                 sd.attr_type[a] = abi.ATTR_I8 if dim.attrs[a].dtype == np.int8 else abi.ATTR_I32

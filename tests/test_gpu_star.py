@@ -82,7 +82,8 @@ def test_star_unaligned_columns_scalar_path(ctx, data, oracle):
 def test_star_foreign_keys_outside_dimension(ctx, oracle):
     d = star.gen_star(9, n_fact=1 << 18, dim_rows=SMALL_DIMS)
     d.fk[0][::7] = 0
-    d.fk[1][::11] = SMALL_DIMS[1] + 3
+    d.fk[1][::11] = SMALL_DIMS[1] + 3  # not a yyyymmdd key of the date dimension
+    d.fk[1][::17] = 19920100
     d.fk[2][::13] = -5
     p = star.StarPlan(ctx, d)
     qs = star.gen_queries(9, 64, d.dims)
@@ -90,6 +91,50 @@ def test_star_foreign_keys_outside_dimension(ctx, oracle):
     ctx.sync()
     check(star.StarPlan.results(out, len(qs)), [oracle.star_query(d, q, threads=cpu_threads()) for q in qs])
     p.close()
+
+
+def test_star_date_keys_are_yyyymmdd(data):
+    """The 2,557-row date dimension is keyed yyyymmdd (1992-01-01 ..
+    1998-12-31), so the batch path uses its hashed dimension table."""
+    date = data.dims[1]
+    assert date.n == 2557 and date.keys is not None
+    assert date.keys[0] == 19920101 and date.keys[-1] == 19981231
+    assert np.isin(data.fk[1], date.keys).all()
+
+
+def test_star_dense_and_hashed_agree(ctx, oracle):
+    """Every dimension hashed (large ones gathered from L2 through the
+    table), and every dimension dense, against the oracle."""
+    rng = np.random.default_rng(31)
+    base = star.gen_star(13, n_fact=1 << 18, dim_rows=SMALL_DIMS)
+    qs = star.gen_queries(13, 64, base.dims)
+    # all dense: the date dimension with keys row + 1
+    dense = star.StarData([star.Dim(d.name, d.n, d.attrs, d.names, d.lo, d.hi, None) for d in base.dims],
+                          [c.copy() for c in base.fk], base.quantity, base.price)
+    rows = np.searchsorted(np.sort(base.dims[1].keys), base.fk[1])
+    dense.fk[1] = (np.argsort(base.dims[1].keys)[rows] + 1).astype(np.int32)
+    # all hashed: scattered distinct keys for every dimension
+    dims_h, fk_h = [], []
+    for d, dim in enumerate(base.dims):
+        keys = rng.choice(np.arange(-(1 << 30), 1 << 30, 7, dtype=np.int64), dim.n, replace=False).astype(np.int32)
+        dims_h.append(star.Dim(dim.name, dim.n, dim.attrs, dim.names, dim.lo, dim.hi, keys))
+        fk_h.append(keys[dense.fk[d] - 1])
+    hashed = star.StarData(dims_h, fk_h, base.quantity, base.price)
+    for data in (dense, hashed):
+        p = star.StarPlan(ctx, data)
+        out = p.run(qs)
+        ctx.sync()
+        check(star.StarPlan.results(out, len(qs)), [oracle.star_query(data, q, threads=cpu_threads()) for q in qs])
+        p.close()
+
+
+def test_star_duplicate_primary_key_refused(ctx):
+    data = star.gen_star(3, n_fact=1 << 12, dim_rows=SMALL_DIMS)
+    data.dims[1].keys = data.dims[1].keys.copy()
+    data.dims[1].keys[100] = data.dims[1].keys[7]
+    with pytest.raises(abi.GbjError) as e:
+        star.StarPlan(ctx, data)
+    assert e.value.code == abi.ERR_INVALID
 
 
 def test_star_invalid_requests(ctx, plan, data):

@@ -20,7 +20,13 @@ def numpy_star(data, q):
         if q.pred_attr[d] >= 0:
             col = dim.attrs[q.pred_attr[d]].astype(np.int64)
             ok = (col >= q.pred_lo[d]) & (col <= q.pred_hi[d])
-        r = data.fk[d].astype(np.int64) - 1
+        if dim.keys is None:
+            r = data.fk[d].astype(np.int64) - 1
+        else:  # key -> row through the sorted keys
+            order = np.argsort(dim.keys, kind="stable")
+            pos = np.searchsorted(dim.keys[order], data.fk[d])
+            posc = np.minimum(pos, dim.n - 1)
+            r = np.where(dim.keys[order][posc] == data.fk[d], order[posc], -1).astype(np.int64)
         inr = (r >= 0) & (r < dim.n)
         keep &= inr
         rc = np.where(inr, r, 0)
@@ -55,7 +61,8 @@ def test_oracle_matches_numpy(small, oracle):
 def test_oracle_foreign_keys_outside_dimension(oracle):
     data = star.gen_star(5, n_fact=1 << 16, dim_rows=SMALL_DIMS)
     data.fk[0][::7] = 0
-    data.fk[1][::11] = SMALL_DIMS[1] + 3
+    data.fk[1][::11] = 19920100  # not a date key
+    data.fk[1][::13] = SMALL_DIMS[1] + 3
     q = star.Query(join_mask=0b0011, group_dim=[0, 1], group_attr=[1, 1])
     exp = numpy_star(data, q)
     got = oracle.star_query(data, q, threads=2)
@@ -66,7 +73,10 @@ def test_oracle_foreign_keys_outside_dimension(oracle):
 def test_workload_shape(lib):
     data = star.gen_star(3, n_fact=1 << 16, dim_rows=SMALL_DIMS)
     for d, dim in enumerate(data.dims):
-        assert data.fk[d].min() >= 1 and data.fk[d].max() <= dim.n
+        if dim.keys is None:
+            assert data.fk[d].min() >= 1 and data.fk[d].max() <= dim.n
+        else:
+            assert np.isin(data.fk[d], dim.keys).all() and len(np.unique(dim.keys)) == dim.n
         for col, lo, hi in zip(dim.attrs, dim.lo, dim.hi):
             assert col.min() >= lo and col.max() <= hi
     assert data.quantity.min() >= 1 and data.quantity.max() <= 50
