@@ -668,14 +668,27 @@ class Serve:
             return srv.submit(None, None, pk, pv, self.shapes[t].cardinality, out, table=tables[t])
         return srv.submit(*self.dev[t], self.shapes[t].cardinality, out)
 
-    def _closed(self, srv, n, salt, tables=None):
+    def _closed(self, srv, n, salt, tables=None, busy=None):
+        """Closed loop of n queries -> (queries/s, errors); `busy` (a dict)
+        gets the fraction of the wall time the batches kept the GPU busy."""
         order = self._order(n, salt)
+        b0 = srv.busy_ms()
         t0 = time.perf_counter()
         tickets = [self._submit(srv, t, self.ring_outs[i % self.ring], tables) for i, t in enumerate(order)]
         srv.drain()
         dt = time.perf_counter() - t0
+        if busy is not None:
+            busy["batch_gpu_s"] = round((srv.busy_ms() - b0) / 1e3, 4)
+            busy["wall_s"] = round(dt, 4)
+            busy["gpu_busy_frac"] = round((srv.busy_ms() - b0) / 1e3 / dt, 3)
         bad = sum(srv.wait(tk) != 0 for tk in tickets)
         return n / dt, bad
+
+    # size classes of the templates by probe rows (p99 is reported per class)
+    CLASSES = (("small", 1 << 20), ("medium", 1 << 24), ("large", 1 << 62))
+
+    def _class_of(self, t):
+        return next(name for name, lim in self.CLASSES if self.shapes[t].n_probe < lim)
 
     def _open(self, srv, rate, n, salt, tables=None):
         from proteus_gb300 import serve
@@ -706,6 +719,13 @@ class Serve:
         summ = serve.latency_summary(lat)
         summ.update({"rate": round(rate, 1), "throughput": round(n / (last - first), 1),
                      "errors": bad, "mismatch_vs_alone": mism})
+        by = {}
+        for name, _ in self.CLASSES:
+            sel = [x for x, t in zip(lat, order) if self._class_of(t) == name]
+            if sel:
+                c = serve.latency_summary(sel)
+                by[name] = {"p50_ms": c["p50_ms"], "p99_ms": c["p99_ms"], "n": c["n"]}
+        summ["by_class"] = by
         return summ
 
     SLOS_MS = (5.0, 10.0, 20.0, 50.0)
@@ -735,7 +755,8 @@ class Serve:
             assert plain.wait(tk) == 0
             self.alone.append(o.sorted())
         self._closed(plain, 256, 1)
-        plain_cap, bad_p = self._closed(plain, 768, 2)
+        plain_busy = {}
+        plain_cap, bad_p = self._closed(plain, 768, 2, busy=plain_busy)
         p_runs = self._sweep(plain, plain_cap, 10)
         plain.close()
 
@@ -745,7 +766,8 @@ class Serve:
 
         batched = batched_server()
         self._closed(batched, 256, 4)
-        bat_cap, bad_b = self._closed(batched, 1536, 5)
+        bat_busy = {}
+        bat_cap, bad_b = self._closed(batched, 1536, 5, busy=bat_busy)
         b_runs = self._sweep(batched, bat_cap, 20)
         st = batched.stats()
         batched.close()
@@ -769,8 +791,8 @@ class Serve:
         head = slo[f"p99<={self.HEADLINE_SLO_MS:g}ms"]
         return head["batched_qps"], {
             "slo_ms": self.HEADLINE_SLO_MS,
-            "plain": {"capacity_qps": round(plain_cap, 1), "sweep": p_runs},
-            "batched": {"capacity_qps": round(bat_cap, 1), "sweep": b_runs,
+            "plain": {"capacity_qps": round(plain_cap, 1), "closed_loop": plain_busy, "sweep": p_runs},
+            "batched": {"capacity_qps": round(bat_cap, 1), "closed_loop": bat_busy, "sweep": b_runs,
                         "batches": st["batches"], "peak_pool_bytes": st["peak_bytes"]},
             "batched_resident_tables": {"capacity_qps": round(res_cap, 1), "sweep": r_runs,
                                         "batches": st_r["batches"], "table_bytes": table_bytes,
@@ -779,6 +801,7 @@ class Serve:
             "batched_over_plain_at_equal_p99": head["ratio"],
             "batched_resident_over_plain_at_equal_p99": head["resident_ratio"],
             "batched_over_plain_capacity": round(bat_cap / plain_cap, 2),
+            "class_probe_rows": {name: lim for name, lim in self.CLASSES[:-1]},
             "batched_resident_over_plain_capacity": round(res_cap / plain_cap, 2),
             "closed_loop_errors": bad_p + bad_b + bad_r,
             "mismatch_vs_alone": sum(r["mismatch_vs_alone"] for r in p_runs + b_runs + r_runs),

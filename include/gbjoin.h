@@ -577,6 +577,11 @@ int gbj_server_drain(gbj_server *srv);
 /* Totals: queries completed, batches launched, peak budget bytes held. */
 int gbj_server_stats(gbj_server *srv, uint64_t *completed, uint64_t *batches,
                      uint64_t *peak_bytes);
+/* Device time of the completed batches, each from before its first
+ * operation to after its last (milliseconds, summed; batches of different
+ * in-flight slots may overlap, so with one slot in flight the sum is the
+ * time the GPU spent on the server's work). */
+int gbj_server_busy(gbj_server *srv, double *batch_ms);
 /* Drains, stops the request loop and frees the server. */
 int gbj_server_destroy(gbj_server *srv);
 /* Builds the join table and group-key map of one build relation once and

@@ -134,6 +134,7 @@ SIGNATURES = {
     "gbj_server_cancel": (C.c_int, [vp, u64, P(i32)]),
     "gbj_server_pause": (C.c_int, [vp, i32]),
     "gbj_server_retries": (C.c_int, [vp, P(u64)]),
+    "gbj_server_busy": (C.c_int, [vp, P(C.c_double)]),
     "gbj_server_stats": (C.c_int, [vp, P(u64), P(u64), P(u64)]),
     "gbj_server_destroy": (C.c_int, [vp]),
     "gbj_server_register_table": (C.c_int, [vp, vp, vp, u64, u64, P(u64)]),

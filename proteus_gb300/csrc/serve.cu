@@ -374,6 +374,7 @@ struct QueryRec {
 
 struct Slot {
   cudaStream_t stream = nullptr;
+  cudaEvent_t start = nullptr;  // before the batch's first operation (timing)
   cudaEvent_t done = nullptr;
   SBatch *h_desc = nullptr;    // pinned
   SBatch *d_desc = nullptr;    // pool
@@ -415,6 +416,7 @@ struct gbj_server {
   Slot slots[kMaxSlots];
   int nslots = 0;
   uint64_t held = 0, peak = 0, completed = 0, batches = 0, retried = 0;
+  double batch_ms = 0;  // device time of the completed batches, start to done
   bool stop = false;
   bool paused = false;  // gbj_server_pause: no new batches are launched
   std::thread th;
@@ -513,6 +515,9 @@ uint64_t enqueue_rec(gbj_server *sv, uint64_t ticket);
 // being its own group, which cannot overflow; other failures complete it.
 void complete_slot(gbj_server *sv, Slot &sl) {
   const double t = sv->now();
+  float ms = 0;
+  if (cudaEventElapsedTime(&ms, sl.start, sl.done) == cudaSuccess) sv->batch_ms += ms;
+  else (void)cudaGetLastError();
   for (size_t i = 0; i < sl.tickets.size(); ++i) {
     QueryRec &r = sv->recs[sl.tickets[i] - 1];
     const uint32_t bits = sl.h_status[i];
@@ -623,7 +628,8 @@ bool launch_batch(gbj_server *sv, Slot &sl) {
     sl.items[ph] = items[ph];
   }
   int rc = GBJ_OK;
-  if (sv->prm.use_graph && !sl.large) {
+  if (cudaEventRecord(sl.start, sl.stream) != cudaSuccess) rc = cuda_error(ctx, cudaGetLastError(), "cudaEventRecord");
+  if (rc == GBJ_OK && sv->prm.use_graph && !sl.large) {
     if (!sl.exec) {
       cudaError_t e = cudaStreamBeginCapture(sl.stream, cudaStreamCaptureModeThreadLocal);
       if (e != cudaSuccess) rc = cuda_error(ctx, e, "cudaStreamBeginCapture");
@@ -648,7 +654,7 @@ bool launch_batch(gbj_server *sv, Slot &sl) {
       // the launches were counted at capture; count the replay's kernels
       else ctx->launches.fetch_add(5, std::memory_order_relaxed);
     }
-  } else {
+  } else if (rc == GBJ_OK) {
     rc = enqueue_batch(sv, sl, false);
   }
   if (rc == GBJ_OK) {
@@ -722,6 +728,7 @@ void free_slots(gbj_server *sv) {
     Slot &sl = sv->slots[i];
     if (sl.exec) cudaGraphExecDestroy(sl.exec);
     if (sl.done) cudaEventDestroy(sl.done);
+    if (sl.start) cudaEventDestroy(sl.start);
     if (sl.h_desc) cudaFreeHost(sl.h_desc);
     if (sl.h_status) cudaFreeHost(sl.h_status);
     if (sl.d_desc) pool_release(sv->ctx, sl.d_desc, sl.stream);
@@ -766,7 +773,8 @@ extern "C" int gbj_server_create(gbj_ctx *ctx, const gbj_server_params *params, 
     sl.large = i >= sv->nslots - prm.large_slots;
     const int prio = prm.large_slots == 0 ? 0 : (sl.large ? prio_low : prio_high);
     cudaError_t e = cudaStreamCreateWithPriority(&sl.stream, cudaStreamNonBlocking, prio);
-    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&sl.done, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreate(&sl.done);
+    if (e == cudaSuccess) e = cudaEventCreate(&sl.start);
     if (e == cudaSuccess) e = cudaHostAlloc(reinterpret_cast<void **>(&sl.h_desc), sizeof(SBatch), cudaHostAllocDefault);
     if (e == cudaSuccess)
       e = cudaHostAlloc(reinterpret_cast<void **>(&sl.h_status), sizeof(uint32_t) * kMaxB, cudaHostAllocDefault);
@@ -917,6 +925,13 @@ extern "C" int gbj_server_stats(gbj_server *sv, uint64_t *completed, uint64_t *b
   if (completed) *completed = sv->completed;
   if (batches) *batches = sv->batches;
   if (peak_bytes) *peak_bytes = sv->peak;
+  return GBJ_OK;
+}
+
+extern "C" int gbj_server_busy(gbj_server *sv, double *batch_ms) {
+  if (!sv || !batch_ms) return GBJ_ERR_INVALID;
+  std::lock_guard<std::mutex> lk(sv->mu);
+  *batch_ms = sv->batch_ms;
   return GBJ_OK;
 }
 

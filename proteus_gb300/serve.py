@@ -175,6 +175,12 @@ class Server:
         self.ctx.check(self.ctx.lib.gbj_server_drain(self.handle))
         self._keep.clear()
 
+    def busy_ms(self) -> float:
+        """Summed device time of the completed batches (gbj_server_busy)."""
+        ms = C.c_double()
+        self.ctx.check(self.ctx.lib.gbj_server_busy(self.handle, C.byref(ms)))
+        return float(ms.value)
+
     def stats(self):
         c, b, p = C.c_uint64(), C.c_uint64(), C.c_uint64()
         self.ctx.check(self.ctx.lib.gbj_server_stats(self.handle, C.byref(c), C.byref(b), C.byref(p)))
