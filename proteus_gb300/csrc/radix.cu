@@ -44,11 +44,22 @@ using namespace gbj;
 
 namespace {
 
-constexpr int kTile = 4096;          // tuples per tile of a partition pass
-constexpr int kTileThreads = 512;
-constexpr int kTilePer = kTile / kTileThreads;  // tuples per thread
-constexpr int kTileCtas = 2;                    // CTAs per SM (register budget)
-constexpr int kTileWarps = kTileThreads / 32;
+// Tile shapes of the partition passes: 0 = 2048 tuples x 256 threads (4
+// CTAs per SM), for passes of up to 7 digit bits with 8-byte pair output;
+// 1 = 4096 x 512 (2 CTAs per SM), for 8-bit passes and 4-byte column
+// output, whose digit runs would be too short in a smaller tile.  Measured
+// on GB300 (radix join, R 2^27, S 2^29, 14 bits; ms of tile passes per 60
+// launches): 2048 x 256 66.0, 3072 x 256 68.1, 4096 x 512 70.1, 4096 x 256
+// 80.7, 2048 x 512 85.0, 4096 x 1024 95.6, 1024 x 256 102.4; the group-by's
+// 8-bit column passes ran 60 % longer with the small tile.
+template <int kSh>
+struct TileShape {
+  static constexpr int tile = kSh == 0 ? 2048 : 4096;
+  static constexpr int threads = kSh == 0 ? 256 : 512;  // >= 256: one thread per digit in the scans
+  static constexpr int per = tile / threads;            // tuples per thread
+  static constexpr int warps = threads / 32;
+  static constexpr int ctas = 1024 / threads;  // CTAs per SM (64 registers per thread)
+};
 constexpr int kMaxDigits = 256;      // <= 8 digit bits per pass
 #ifndef GBJ_TILE_TMA
 #define GBJ_TILE_TMA 0
@@ -118,9 +129,10 @@ __global__ void __launch_bounds__(1024)
     if (sh[p]) atomicAdd(&ghist[p], sh[p]);
 }
 
+template <int kSh>
 struct TileSmem {
-  uint32_t whist[kTileWarps][kMaxDigits];  // per-warp digit counts, then each warp's run start
-  int2 sorted[kTile];
+  uint32_t whist[TileShape<kSh>::warps][kMaxDigits];  // per-warp digit counts, then each warp's run start
+  int2 sorted[TileShape<kSh>::tile];
   uint32_t gdelta[kMaxDigits];  // output position of sorted[i] = gdelta[digit] + i
   uint32_t wsum[8];
 };
@@ -140,17 +152,19 @@ struct TileSmem {
 // values: one tile ahead) -- instead of through registers.  A copy covers
 // the 16-byte aligned middle of the tile; the (at most three) tuples either
 // side of it are loaded directly.  Input columns must be 16-byte aligned.
-constexpr uint32_t kRingBytes = kTile * 8;
-template <int kDigit, bool kPairsIn, bool kAoSOut, bool kHashLoad, bool kTma>
-__global__ void __launch_bounds__(kTileThreads, kTileCtas)
+template <int kDigit, bool kPairsIn, bool kAoSOut, bool kHashLoad, bool kTma, int kSh>
+__global__ void __launch_bounds__(TileShape<kSh>::threads, TileShape<kSh>::ctas)
     k_tile_pass(const int32_t *__restrict__ keys, const int32_t *__restrict__ vals,
                 const int2 *__restrict__ pin, uint32_t n, int dshift, uint32_t dmask,
                 const uint64_t *__restrict__ bucket_off, const uint64_t *__restrict__ tile_off,
                 uint32_t nb, uint32_t *__restrict__ cursor, int2 *__restrict__ out_pairs,
                 int32_t *__restrict__ out_k, int32_t *__restrict__ out_v, uint32_t *status) {
+  constexpr int kTile = TileShape<kSh>::tile, kTileThreads = TileShape<kSh>::threads;
+  constexpr int kTilePer = TileShape<kSh>::per, kTileWarps = TileShape<kSh>::warps;
+  constexpr uint32_t kRingBytes = kTile * 8;
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  TileSmem &S = *reinterpret_cast<TileSmem *>(smem_raw);
-  unsigned char *ring = smem_raw + sizeof(TileSmem);
+  TileSmem<kSh> &S = *reinterpret_cast<TileSmem<kSh> *>(smem_raw);
+  unsigned char *ring = smem_raw + sizeof(TileSmem<kSh>);
   uint64_t *bars = reinterpret_cast<uint64_t *>(ring + kRingBytes);
   const uint32_t stage_bytes = (kPairsIn || vals) ? kRingBytes : kRingBytes / 2;
   const uint32_t nst = kRingBytes / stage_bytes;  // stages: 1 or 2
@@ -382,10 +396,11 @@ __global__ void k_cursors(const uint64_t *__restrict__ off, uint32_t P, int bits
   if (cursor1 && p == 0) bucket_off[P >> bits2] = off[P];
 }
 
-__global__ void k_bucket_tiles(const uint64_t *__restrict__ bucket_off, uint32_t nb,
+// Tiles of `tile` tuples per pass-1 bucket (the second pass's tile shape).
+__global__ void k_bucket_tiles(const uint64_t *__restrict__ bucket_off, uint32_t nb, uint32_t tile,
                                uint64_t *__restrict__ tiles) {
   const uint32_t b = blockIdx.x * blockDim.x + threadIdx.x;
-  if (b < nb) tiles[b] = (bucket_off[b + 1] - bucket_off[b] + kTile - 1) / kTile;
+  if (b < nb) tiles[b] = (bucket_off[b + 1] - bucket_off[b] + tile - 1) / tile;
 }
 
 // ---------------------------------------------------------------- join
@@ -775,26 +790,44 @@ int launch_join_agg(gbj_ctx *ctx, bool by_rows, const AggSpec &spec, const int2 
                                                           d_out, ctr, s);
 }
 
+// The tile shape of a pass with `ndig` digits and pair (AoS) or column output.
+int tile_shape_for(uint32_t ndig, bool aos) { return ndig <= 128 && aos ? 0 : 1; }
+
+template <int kDigit, bool kPairsIn, bool kAoSOut, bool kHashLoad, int kSh>
+int launch_tile_pass_sh(gbj_ctx *ctx, const int32_t *keys, const int32_t *vals, const int2 *pin,
+                        uint64_t n, int dshift, uint32_t dmask, const uint64_t *bucket_off,
+                        const uint64_t *tile_off, uint32_t nb, uint32_t *cursor, int2 *op, int32_t *ok,
+                        int32_t *ov, cudaStream_t s) {
+  using TS = TileShape<kSh>;
+  // bulk-copy loads when the input columns are 16-byte aligned
+  auto al16 = [](const void *p) { return (reinterpret_cast<uintptr_t>(p) & 15) == 0; };
+  const bool tma = kTileTma && (kPairsIn ? al16(pin) : (al16(keys) && (!vals || al16(vals))));
+  auto kern = tma ? k_tile_pass<kDigit, kPairsIn, kAoSOut, kHashLoad, true, kSh>
+                  : k_tile_pass<kDigit, kPairsIn, kAoSOut, kHashLoad, false, kSh>;
+  const size_t smem = sizeof(TileSmem<kSh>) + (tma ? (size_t)TS::tile * 8 + 16 : 0);
+  GBJ_CHECK_CUDA(ctx, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  int per_sm = 0;
+  GBJ_CHECK_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, TS::threads, smem));
+  if (per_sm < 1) per_sm = 1;
+  const uint64_t tiles_hint = (n + TS::tile - 1) / TS::tile + nb;
+  const uint64_t grid = std::max<uint64_t>(1, std::min<uint64_t>((uint64_t)ctx->sm_count * per_sm, tiles_hint));
+  kern<<<(unsigned)grid, TS::threads, smem, s>>>(keys, vals, pin, (uint32_t)n, dshift, dmask, bucket_off, tile_off,
+                                                 nb, cursor, op, ok, ov, ctx->d_status);
+  return after_launch(ctx, "k_tile_pass", s);
+}
+
 template <int kDigit, bool kPairsIn, bool kAoSOut, bool kHashLoad>
 int launch_tile_pass(gbj_ctx *ctx, const int32_t *keys, const int32_t *vals, const int2 *pin,
                      uint64_t n, int dshift, uint32_t dmask, const uint64_t *bucket_off,
                      const uint64_t *tile_off, uint32_t nb, uint32_t *cursor, int2 *op, int32_t *ok,
                      int32_t *ov, cudaStream_t s) {
-  // bulk-copy loads when the input columns are 16-byte aligned
-  auto al16 = [](const void *p) { return (reinterpret_cast<uintptr_t>(p) & 15) == 0; };
-  const bool tma = kTileTma && (kPairsIn ? al16(pin) : (al16(keys) && (!vals || al16(vals))));
-  auto kern = tma ? k_tile_pass<kDigit, kPairsIn, kAoSOut, kHashLoad, true>
-                  : k_tile_pass<kDigit, kPairsIn, kAoSOut, kHashLoad, false>;
-  const size_t smem = sizeof(TileSmem) + (tma ? kRingBytes + 16 : 0);
-  GBJ_CHECK_CUDA(ctx, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  int per_sm = 0;
-  GBJ_CHECK_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kTileThreads, smem));
-  if (per_sm < 1) per_sm = 1;
-  const uint64_t tiles_hint = (n + kTile - 1) / kTile + nb;
-  const uint64_t grid = std::max<uint64_t>(1, std::min<uint64_t>((uint64_t)ctx->sm_count * per_sm, tiles_hint));
-  kern<<<(unsigned)grid, kTileThreads, smem, s>>>(keys, vals, pin, (uint32_t)n, dshift, dmask, bucket_off,
-                                                  tile_off, nb, cursor, op, ok, ov, ctx->d_status);
-  return after_launch(ctx, "k_tile_pass", s);
+  if (tile_shape_for(dmask + 1, kAoSOut) == 0)
+    return launch_tile_pass_sh<kDigit, kPairsIn, kAoSOut, kHashLoad, 0>(ctx, keys, vals, pin, n, dshift, dmask,
+                                                                       bucket_off, tile_off, nb, cursor, op, ok,
+                                                                       ov, s);
+  return launch_tile_pass_sh<kDigit, kPairsIn, kAoSOut, kHashLoad, 1>(ctx, keys, vals, pin, n, dshift, dmask,
+                                                                     bucket_off, tile_off, nb, cursor, op, ok, ov,
+                                                                     s);
 }
 
 // kHashOut: the tuples leave with fmix32(key) in place of the key (the
@@ -855,10 +888,12 @@ int partition_impl(gbj_ctx *ctx, const int32_t *keys, const int32_t *vals, uint6
     GBJ_TRY((launch_tile_pass<kPass, false, true, kHashOut>(ctx, keys, vals, nullptr, n, shift + bits2, B1 - 1,
                                                             nullptr, nullptr, 1, cursor1, tmp, nullptr, nullptr,
                                                             s)));
-    k_bucket_tiles<<<(B1 + 255) / 256, 256, 0, s>>>(bucket_off, B1, tiles);
+    const uint32_t m2 = (1u << bits2) - 1;
+    const uint32_t tile2 = tile_shape_for(m2 + 1, out_pairs != nullptr) == 0 ? TileShape<0>::tile
+                                                                            : TileShape<1>::tile;
+    k_bucket_tiles<<<(B1 + 255) / 256, 256, 0, s>>>(bucket_off, B1, tile2, tiles);
     GBJ_TRY(after_launch(ctx, "k_bucket_tiles", s));
     GBJ_TRY(scan_u64(ctx, tiles, tiles, B1, s));
-    const uint32_t m2 = (1u << bits2) - 1;
     if (out_pairs)
       GBJ_TRY((launch_tile_pass<kPass, true, true, false>(ctx, nullptr, nullptr, tmp, n, shift, m2, bucket_off,
                                                           tiles, B1, cursor2, out_pairs, nullptr, nullptr, s)));
