@@ -529,8 +529,8 @@ __global__ void __launch_bounds__(kThreads, kCtas)
   __shared__ int64_t red[32 * GBJ_MAX_AGGS];
   __shared__ JoinItem s_it;
   __shared__ int s_dup;
-  gbjd::Acc acc;
-  acc.init(spec);
+  gbjd::Acc acc;  // the specialised accumulators fill it only at the end
+  if (kAgg != kAggCountXor && kAgg != kAggCountProduct) acc.init(spec);
   int64_t a_cnt = 0, a_sum = 0;
   const unsigned long long total = item_off[P];
   // thread 0: claims the next item and resolves its extent
@@ -666,28 +666,63 @@ __global__ void __launch_bounds__(kThreads, kCtas)
           nxt[u] = j < ns ? __ldcs(Sp + j) : make_int2(0, 0);
         }
         uint32_t qn = 0;  // warp-uniform queue length
+        if (unique && kAgg != kAggGeneric && kAgg != kAggRows) {
+          uint32_t more = 0;  // bit u: tuple u must go on past its home bucket
+          // the specialised aggregates: the match folded in without a
+          // branch (at most one slot matches; the value load is issued
+          // whether or not it did), and the queue touched only when some
+          // lane of the warp must go on
 #pragma unroll
-        for (int u = 0; u < 4; ++u) {
-          const bool valid = j0 + threadIdx.x + u * kThreads < ns;
-          const uint32_t h = (uint32_t)t[u].x;
-          const uint32_t b = home_bucket(h, nb);
-          bool more;
-          if (unique) {
+          for (int u = 0; u < 4; ++u) {
+            const bool valid = j0 + threadIdx.x + u * kThreads < ns;
+            const uint32_t b = home_bucket((uint32_t)t[u].x, nb);
             const int4 kk = tk4[b];
-            const bool e0 = kk.x == t[u].x, e1 = kk.y == t[u].x, e2 = kk.z == t[u].x, e3 = kk.w == t[u].x;
+            const int32_t k = t[u].x;
+            const bool e0 = kk.x == k, e1 = kk.y == k, e2 = kk.z == k, e3 = kk.w == k;
             const bool room = (kk.x == kEmpty) | (kk.y == kEmpty) | (kk.z == kEmpty) | (kk.w == kEmpty);
             const bool found = valid & (e0 | e1 | e2 | e3);
-            if (found) {
-              const uint32_t idx = e0 ? 0 : e1 ? 1 : e2 ? 2 : 3;
-              join_match<kAgg>(spec, rc, acc, a_cnt, a_sum, h, tval[4 * b + idx], t[u].y);
-            }
-            more = valid & !found & !room;
-          } else {
-            more = valid && !bucket(h, t[u].y, b);
+            const int32_t bv = tval[4 * b + (e0 ? 0 : e1 ? 1 : e2 ? 2 : 3)];
+            a_cnt += found;
+            if (kAgg == kAggCountXor) a_sum += found ? (uint32_t)(bv ^ t[u].y) : 0u;
+            else a_sum += found ? (int64_t)bv * (int64_t)t[u].y : 0;
+            more |= (uint32_t)(valid & !found & !room) << u;
           }
-          const unsigned bal = __ballot_sync(0xffffffffu, more);
-          if (more) wq[qn + __popc(bal & lt)] = make_int4(t[u].x, t[u].y, (int)(b + 1 == nb ? 0 : b + 1), 0);
-          qn += __popc(bal);
+          if (__any_sync(0xffffffffu, more != 0)) {
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+              const bool mo = (more >> u) & 1u;
+              const unsigned bal = __ballot_sync(0xffffffffu, mo);
+              if (mo) {
+                const uint32_t b = home_bucket((uint32_t)t[u].x, nb);
+                wq[qn + __popc(bal & lt)] = make_int4(t[u].x, t[u].y, (int)(b + 1 == nb ? 0 : b + 1), 0);
+              }
+              qn += __popc(bal);
+            }
+          }
+        } else {
+#pragma unroll
+          for (int u = 0; u < 4; ++u) {
+            const bool valid = j0 + threadIdx.x + u * kThreads < ns;
+            const uint32_t h = (uint32_t)t[u].x;
+            const uint32_t b = home_bucket(h, nb);
+            bool mo;
+            if (unique) {
+              const int4 kk = tk4[b];
+              const bool e0 = kk.x == t[u].x, e1 = kk.y == t[u].x, e2 = kk.z == t[u].x, e3 = kk.w == t[u].x;
+              const bool room = (kk.x == kEmpty) | (kk.y == kEmpty) | (kk.z == kEmpty) | (kk.w == kEmpty);
+              const bool found = valid & (e0 | e1 | e2 | e3);
+              if (found) {
+                const uint32_t idx = e0 ? 0 : e1 ? 1 : e2 ? 2 : 3;
+                join_match<kAgg>(spec, rc, acc, a_cnt, a_sum, h, tval[4 * b + idx], t[u].y);
+              }
+              mo = valid & !found & !room;
+            } else {
+              mo = valid && !bucket(h, t[u].y, b);
+            }
+            const unsigned bal = __ballot_sync(0xffffffffu, mo);
+            if (mo) wq[qn + __popc(bal & lt)] = make_int4(t[u].x, t[u].y, (int)(b + 1 == nb ? 0 : b + 1), 0);
+            qn += __popc(bal);
+          }
         }
         if (qn) {
           __syncwarp();
@@ -732,6 +767,7 @@ __global__ void __launch_bounds__(kThreads, kCtas)
     __syncthreads();
   }
   if (kAgg == kAggCountXor || kAgg == kAggCountProduct) {
+    acc.init(spec);
     acc.v[0] = a_cnt;
     acc.v[1] = a_sum;
   }
