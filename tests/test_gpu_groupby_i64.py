@@ -64,3 +64,14 @@ def test_groupby_i64_refusals(ctx):
         ctx.sync()
     assert e.value.code == abi.ERR_CAPACITY
     assert int(host(res[5])[0]) == 5000
+
+
+def test_groupby_i64_empty_and_tail(ctx, oracle):
+    e = np.zeros(0, np.int64)
+    res = ctx.groupby(dev(e), dev(np.zeros(0, np.int32)), 4)
+    ctx.sync()
+    assert int(host(res[5])[0]) == 0
+    rng = np.random.default_rng(17)
+    k = rng.integers(-5, 5, 1001).astype(np.int64) << 33  # keys equal in their low words
+    v = rng.integers(-100, 100, 1001).astype(np.int32)
+    check(ctx, oracle, k, v, expected_groups=10)

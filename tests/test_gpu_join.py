@@ -140,3 +140,26 @@ def test_invalid_aggregate(ctx):
     assert e.value.code == abi.ERR_INVALID
     with pytest.raises(abi.GbjError):
         ctx.join_probe_agg(t, dev(rk), dev(rp), [(9, abi.VAL_ONE)])
+
+
+def test_probe_pairs_payload_table_and_int32_min(ctx, oracle):
+    """Pairs from a table built with a payload (rows kept beside the
+    buckets) and INT32_MIN keys on both sides (the side list)."""
+    rng = np.random.default_rng(12)
+    rk = rng.integers(-300, 300, 4000).astype(np.int32)
+    rk[::50] = np.iinfo(np.int32).min
+    rp = rng.integers(-1000, 1000, len(rk)).astype(np.int32)
+    sk = rng.integers(-400, 400, 9000).astype(np.int32)
+    sk[::70] = np.iinfo(np.int32).min
+    eb, ep = oracle.join_pairs(rk, sk)
+    t = ctx.join_build(dev(rk), dev(rp))
+    b, p, cnt = ctx.join_probe_pairs(t, dev(sk), capacity=len(eb) + 10)
+    ctx.sync()
+    m = int(host(cnt)[0])
+    assert m == len(eb)
+    got = sorted(zip(host(b)[:m].tolist(), host(p)[:m].tolist()))
+    assert got == sorted(zip(eb.tolist(), ep.tolist()))
+    # and the aggregates over the same table
+    out = ctx.join_probe_agg(t, dev(sk), dev(sk), ALL_AGGS)
+    ctx.sync()
+    assert host(out).tolist() == oracle.join_agg(rk, rp, sk, sk, ALL_AGGS)

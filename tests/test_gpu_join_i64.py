@@ -107,3 +107,12 @@ def test_join_i64_table_kind_is_checked(ctx):
     assert ctx.join_probe_agg(t64, k64, None, [(abi.AGG_COUNT, abi.VAL_ONE)]).cpu().tolist() == [10]
     t64.destroy()
     t32.destroy()
+
+
+def test_join_i64_empty_sides(ctx, oracle):
+    rng = np.random.default_rng(13)
+    k = rng.integers(-(1 << 40), 1 << 40, 100).astype(np.int64)
+    p = rng.integers(-9, 9, 100).astype(np.int32)
+    e64, e32 = np.zeros(0, np.int64), np.zeros(0, np.int32)
+    assert gpu_join(ctx, e64, e32, k, p, AGGS) == oracle.join_agg_i64(e64, e32, k, p, AGGS)
+    assert gpu_join(ctx, k, p, e64, e32, AGGS) == oracle.join_agg_i64(k, p, e64, e32, AGGS)
