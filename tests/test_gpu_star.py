@@ -120,7 +120,14 @@ def test_star_dense_and_hashed_agree(ctx, oracle):
         dims_h.append(star.Dim(dim.name, dim.n, dim.attrs, dim.names, dim.lo, dim.hi, keys))
         fk_h.append(keys[dense.fk[d] - 1])
     hashed = star.StarData(dims_h, fk_h, base.quantity, base.price)
-    for data in (dense, hashed):
+    # strided keys (7 + 3 row): range-indexed, the larger dimensions through L2
+    dims_s, fk_s = [], []
+    for d, dim in enumerate(base.dims):
+        keys = (7 + 3 * np.arange(dim.n, dtype=np.int64)).astype(np.int32)[::-1].copy()
+        dims_s.append(star.Dim(dim.name, dim.n, dim.attrs, dim.names, dim.lo, dim.hi, keys))
+        fk_s.append(keys[dense.fk[d] - 1])
+    strided = star.StarData(dims_s, fk_s, base.quantity, base.price)
+    for data in (dense, hashed, strided):
         p = star.StarPlan(ctx, data)
         out = p.run(qs)
         ctx.sync()
