@@ -296,8 +296,8 @@ class PlainJoin:
         return self.ns
 
     def kernel_bytes(self, name):
-        return {"k_join_probe_agg": 8 * self.ns,   # probe key + payload
-                "k_join_build": 12 * self.nr}.get(name)  # key read + slot write
+        return {"k_jb_probe_agg": 8 * self.ns,   # probe key + payload
+                "k_jb_build": 12 * self.nr}.get(name)  # key + payload read, bucket slot write
 
     def extra(self, ms, steps, peak):
         comp = 8 * (self.nr + self.ns) * steps

@@ -880,7 +880,7 @@ int gbj_join_build(gbj_ctx *ctx, const int32_t *d_keys,
                                                                 reinterpret_cast<JBucket *>(mem), t->rows,
                                                                 (uint32_t)(nbk - 1), t->meta, t->side,
                                                                 ctx->d_status);
-    rc = after_launch(ctx, "k_join_build", s);
+    rc = after_launch(ctx, "k_jb_build", s);
     if (rc) {
       pool_release(ctx, mem, s);
       delete t;
@@ -920,7 +920,7 @@ int gbj_join_probe_agg(gbj_ctx *ctx, const gbj_table *t, const int32_t *d_keys,
   GBJ_TRY(init_agg_out(ctx, spec, d_out, s));
   if (n == 0) return GBJ_OK;
   launch_jb_probe(ctx->sm_count, t, d_keys, d_payload, n, spec, d_out, s);
-  return after_launch(ctx, "k_join_probe_agg", s);
+  return after_launch(ctx, "k_jb_probe_agg", s);
 }
 
 int gbj_join_probe_pairs(gbj_ctx *ctx, const gbj_table *t, const int32_t *d_keys,
@@ -945,7 +945,7 @@ int gbj_join_probe_pairs(gbj_ctx *ctx, const gbj_table *t, const int32_t *d_keys
     k_jb_probe_pairs<false><<<grid_for(ctx, n, kThreads), kThreads, 0, s>>>(
         d_keys, d_probe_rows, n, bk, nullptr, bmask, t->meta, t->side, d_build_rows, d_out_probe_rows, capacity,
         (unsigned long long *)d_count, ctx->d_status);
-  return after_launch(ctx, "k_join_probe_pairs", s);
+  return after_launch(ctx, "k_jb_probe_pairs", s);
 }
 
 int gbj_join_build_i64(gbj_ctx *ctx, const int64_t *d_keys, const int32_t *d_payload, uint64_t n,
@@ -990,7 +990,7 @@ int gbj_join_build_i64(gbj_ctx *ctx, const int64_t *d_keys, const int32_t *d_pay
     k_jb64_build<<<grid_for(ctx, n, kThreads), kThreads, 0, s>>>(d_keys, d_payload, n,
                                                                   reinterpret_cast<JBucket64 *>(mem), nbk - 1,
                                                                   t->meta, t->side, ctx->d_status);
-    rc = after_launch(ctx, "k_join_build", s);
+    rc = after_launch(ctx, "k_jb64_build", s);
     if (rc) {
       pool_release(ctx, mem, s);
       delete t;
@@ -1022,7 +1022,7 @@ int gbj_join_probe_agg_i64(gbj_ctx *ctx, const gbj_table *t, const int64_t *d_ke
   k_jb64_probe_agg<<<grid_for(ctx, (n + 3) / 4, kThreads, 2), kThreads, 0, s>>>(
       d_keys, d_payload, n, static_cast<const JBucket64 *>(t->slots), (t->mask + 1) / 2 - 1, t->payload, t->meta,
       t->side, spec, d_out);
-  return after_launch(ctx, "k_join_probe_agg", s);
+  return after_launch(ctx, "k_jb64_probe_agg", s);
 }
 
 int gbj_join_probe_pairs_i64(gbj_ctx *ctx, const gbj_table *t, const int64_t *d_keys,
@@ -1038,7 +1038,7 @@ int gbj_join_probe_pairs_i64(gbj_ctx *ctx, const gbj_table *t, const int64_t *d_
   k_jb64_probe_pairs<<<grid_for(ctx, n, kThreads), kThreads, 0, s>>>(
       d_keys, d_probe_rows, n, static_cast<const JBucket64 *>(t->slots), (t->mask + 1) / 2 - 1, t->meta, t->side,
       d_build_rows, d_out_probe_rows, capacity, (unsigned long long *)d_count, ctx->d_status);
-  return after_launch(ctx, "k_join_probe_pairs", s);
+  return after_launch(ctx, "k_jb64_probe_pairs", s);
 }
 
 int gbj_reduce(gbj_ctx *ctx, const int32_t *d_col, const int32_t *d_rows,
