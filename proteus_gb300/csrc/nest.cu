@@ -7,6 +7,8 @@
 // every tuple of a key into that key's group (core/platform/lib/util/radix/
 // aggregations/radix-aggr.cpp:163-259), and for the twin's RJStepwise
 // (radix-aggr.cpp:261-358), which counts the (R, S) pairs with equal keys.
+// The same grouping engine serves HashGroupByChained over int64 keys with
+// int32 values (gbj_groupby_i64, hash-group-by-chained.cpp:267-853).
 //
 // GB300 design: for few groups an on-chip level per CTA (32-bit shared
 // reductions only) in front of the global table; otherwise one global
