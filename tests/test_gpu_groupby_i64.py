@@ -75,3 +75,13 @@ def test_groupby_i64_empty_and_tail(ctx, oracle):
     k = rng.integers(-5, 5, 1001).astype(np.int64) << 33  # keys equal in their low words
     v = rng.integers(-100, 100, 1001).astype(np.int32)
     check(ctx, oracle, k, v, expected_groups=10)
+
+
+def test_groupby_i64_hot_key(ctx, oracle):
+    """One key on most rows (more than 65535 per CTA: the on-chip level's
+    flush path) with a few cold keys, hinted and unhinted."""
+    rng = np.random.default_rng(29)
+    k = np.where(rng.random(1 << 21) < 0.9, np.int64(-7) << 50, rng.integers(0, 64, 1 << 21)).astype(np.int64)
+    v = rng.integers(I32.min, I32.max, len(k), dtype=np.int64).astype(np.int32)
+    check(ctx, oracle, k, v, expected_groups=65)
+    check(ctx, oracle, k, v)

@@ -116,3 +116,21 @@ def test_join_i64_empty_sides(ctx, oracle):
     e64, e32 = np.zeros(0, np.int64), np.zeros(0, np.int32)
     assert gpu_join(ctx, e64, e32, k, p, AGGS) == oracle.join_agg_i64(e64, e32, k, p, AGGS)
     assert gpu_join(ctx, k, p, e64, e32, AGGS) == oracle.join_agg_i64(k, p, e64, e32, AGGS)
+
+
+def test_join_i64_pairs_side_list_and_duplicates(ctx, oracle):
+    """Pairs with INT64_MIN keys on both sides (the side list) and duplicate
+    build keys, against the oracle."""
+    rng = np.random.default_rng(23)
+    rk = rng.integers(-20, 20, 5000).astype(np.int64) * ((1 << 40) + 3)
+    rk[::40] = np.iinfo(np.int64).min
+    sk = rng.integers(-25, 25, 8000).astype(np.int64) * ((1 << 40) + 3)
+    sk[::90] = np.iinfo(np.int64).min
+    eb, ep = oracle.join_pairs_i64(rk, sk)
+    t = ctx.join_build(dev(rk))
+    b, p, cnt = ctx.join_probe_pairs(t, dev(sk), len(eb) + 16)
+    ctx.sync()
+    m = int(host(cnt)[0])
+    assert m == len(eb)
+    assert sorted(zip(host(b)[:m].tolist(), host(p)[:m].tolist())) == sorted(zip(eb.tolist(), ep.tolist()))
+    t.destroy()
